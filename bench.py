@@ -1,0 +1,352 @@
+"""Benchmark of the patchVVC decode path on GB300.
+
+Workload (one step): decode a whole synthetic sequence -- 300 frames of
+~800k points on a 1024^3 grid, GoP 30 (an intra frame plus 29 rigid-motion
+predicted frames), ~500 patches per frame with lognormal sizes (median 1500,
+clipped to [200, 8000]), quantisation step --qp (default 8).  The 10 GoPs are
+independent, so all of them decode concurrently in one pvvc_decode call (4
+kernels).  The data are seeded synthetic stand-ins for the 8i vox10
+sequences.  Inputs + outputs (~4 GB per step) exceed the 129 MB L2, so no L2
+flush is needed between steps.
+
+  value   decoded Mpts/s, device-resident payload, CUDA events on the stream
+  e2e     Mpts/s through pvvc_decode_frames_host: .frame bytes in host
+          memory -> parse -> H2D -> decode -> D2H of xyz+rgb+status
+  roofline  the decode pass's algorithmic bytes (the reference accounting:
+          payload + cached occupancy re-read + reference YUV read/write +
+          15 B/point output + mv) / its device time, against the measured
+          HBM copy bandwidth
+  cpu_baseline  the oracle port of the reference CPU decoder (thread pool
+          over slices, pvvc_decompression.cc:86-150) on a bounded sample
+
+`--impl reference` times the CPU reference path (the oracle port, all host
+cores) on the same workload and prints its own line.
+
+Multi-GPU: one process per GPU (torchrun); every rank decodes its own replica
+sequence (weak scaling), no collective on the data path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "patchvvc-plus_gb300"))
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--qp", type=int, default=8)
+    ap.add_argument("--frames", type=int, default=300)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def make_workload(args, rank):
+    import pvvc
+    t0 = time.time()
+    cfg = pvvc.config("seq300", nframes=args.frames, qp_i=args.qp, qp_p=args.qp, seed=rank)
+    s = pvvc.Synth(cfg)
+    s.encode()
+    frames = s.frames()
+    log(f"[rank {rank}] generated + encoded {len(frames)} frames in {time.time() - t0:.1f}s")
+    return s, frames
+
+
+def algorithmic_bytes(parsed):
+    """Reference accounting of the decode's bytes (payload, cached occupancy
+    bytes re-read by predictive slices, reference YUV read by predictive and
+    written by intra slices, 15 B/point of xyz+rgb output, 64 B of mv)."""
+    occ = {}
+    tot = 0
+    for fr in parsed:
+        for i in range(fr.n):
+            n = int(fr.size[i])
+            g, c = len(fr.geometry[i]), len(fr.color[i])
+            tot += g + c + 64 + 15 * n
+            if fr.type[i] & 0x02:
+                tot += occ.get(int(fr.index[i]), 0) + 12 * n
+            else:
+                occ[int(fr.index[i])] = max(g - 25, 0)
+                tot += 12 * n
+    return tot
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.samples = []
+        self.gpu = gpu
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if len(s) > 3 + i and s[3 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(frames, seconds):
+    """The oracle port of the reference CPU decoder on a bounded sample: the
+    first frames of the sequence, in order, with all host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pvvc
+    from oracle import Oracle
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    decs = [o.decoder() for _ in range(4096)]
+    pts = 0
+    nfr = 0
+    t0 = time.perf_counter()
+    for b in frames:
+        fr = pvvc.parse_frame(b)
+        _, _, st = o.decode_frame(decs, fr, nthreads=cores)
+        assert (st == 0).all()
+        pts += fr.points
+        nfr += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": pts / dt / 1e6, "unit": "Mpts/s", "cores": cores, "kind": "port",
+            "sample": f"first {nfr} frames of the sequence ({pts} points), {dt:.1f}s"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    s, frames = make_workload(args, 0)
+    per = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline(frames, max(2.0, args.cpu_seconds / 2))
+        if i >= args.warmup:
+            per.append(cb["value"])
+    v = float(np.median(per))
+    cb["value"] = v
+    pts_per_step = float(cb["sample"].split("(")[1].split(" ")[0])
+    line = {"impl": "reference", "metric": "decoded Mpts/s (seq300, GoP 30, ~800k pts/frame)", "value": v,
+            "unit": "Mpts/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": pts_per_step / v / 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "config": _config(args, len(frames)), "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _config(args, nframes):
+    return {"workload": f"seq300: {nframes} frames x ~800k points, 1024^3 grid, GoP 30, ~500 lognormal patches, q={args.qp}",
+            "frames": nframes, "gof": 30, "qp": args.qp, "l2": "inputs+outputs per step > L2 (no flush)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def run_ours(args):
+    import torch
+
+    import pvvc
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    s, frames = make_workload(args, rank)
+    parsed = [pvvc.parse_frame(b) for b in frames]
+    gof = 30
+    ngof = (len(parsed) + gof - 1) // gof
+    stride = max(int(f.index.max()) + 1 for f in parsed)
+    batches = [pvvc.pack_frames(parsed[g * gof:(g + 1) * gof]) for g in range(ngof)]
+    batch = pvvc.concat_batches(batches, slot_stride=stride)
+    plan = pvvc.Plan(batch)
+    P = plan.total_points
+    dec = pvvc.Decoder(nslots=stride * ngof, max_leaves=8192, max_nodes=16384)
+    dev = torch.device("cuda", local)
+    pay = torch.from_numpy(batch.payload).to(dev)
+    xyz = torch.empty((P, 3), dtype=torch.float32, device=dev)
+    rgb = torch.empty((P, 3), dtype=torch.uint8, device=dev)
+    st = torch.empty(batch.nslices, dtype=torch.int32, device=dev)
+    ws = torch.empty(plan.workspace_bytes, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    import ctypes
+    evp = (ctypes.c_void_p * 5)(*[e.cuda_event for e in ev])
+    for e in ev:
+        e.record(stream)  # materialise the events
+    lib = pvvc.lib()
+
+    def step(profiled=False):
+        if profiled:
+            rc = lib.pvvc_decode_profiled(plan.h, dec.h, pay.data_ptr(), xyz.data_ptr(), rgb.data_ptr(), None, st.data_ptr(),
+                                          ws.data_ptr(), ws.numel(), sp, evp)
+        else:
+            rc = lib.pvvc_decode(plan.h, dec.h, pay.data_ptr(), xyz.data_ptr(), rgb.data_ptr(), None, st.data_ptr(),
+                                 ws.data_ptr(), ws.numel(), sp)
+        if rc:
+            raise pvvc.PvvcError(rc, "pvvc_decode")
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    assert (st.cpu().numpy() == 0).all(), "decode reported slice errors"
+
+    # timed region
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    with Clocks(local) as clk:
+        t0.record(stream)
+        for _ in range(args.steps):
+            step()
+        t1.record(stream)
+        barrier()
+    ms = t0.elapsed_time(t1) / args.steps
+    if dist is not None:
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = P * world / (ms / 1e3) / 1e6
+
+    # per-kernel device time (CUDA events on the launching stream)
+    kt = np.zeros(4)
+    for _ in range(3):
+        step(profiled=True)
+        torch.cuda.synchronize()
+        kt += np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(4)])
+    kt /= 3
+    names = ["k_tree", "k_rlgr", "k_raht(intra)", "k_raht(predictive)"]
+
+    out = None
+    if rank == 0:
+        alg = algorithmic_bytes(parsed)
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+        dev_ms = float(kt.sum())
+        achieved = alg / (dev_ms / 1e3) / 1e9
+        dom = int(np.argmax(kt))
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "decode pass (4 kernels, serial on one stream)",
+                "dominant_kernel": names[dom], "kernel_ms": {n: float(t) for n, t in zip(names, kt)},
+                "algorithmic_bytes_per_step": alg, "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}
+        e2e = None
+        if not args.no_e2e:
+            e2e = measure_e2e(args, pvvc, frames, P, torch, stream)
+        cb = cpu_baseline(frames, args.cpu_seconds)
+        out = {"metric": "decoded Mpts/s (seq300, GoP 30, ~800k pts/frame)", "value": value, "unit": "Mpts/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
+               "clocks": clk.summary(), "gpu_launches": 4 * args.steps, "points_per_step": P * world}
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return out
+
+
+def measure_e2e(args, pvvc, frames, P, torch, stream):
+    """pvvc_decode_frames_host on host bytes: parse, inflate, H2D, decode, D2H."""
+    import ctypes
+    lib = pvvc.lib()
+    nf = len(frames)
+    bufs = [np.frombuffer(b, np.uint8) for b in frames]
+    ptrs = (ctypes.POINTER(ctypes.c_uint8) * nf)(*[b.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)) for b in bufs])
+    lens = np.array([len(b) for b in frames], np.uint64)
+    nsl = sum(pvvc.parse_frame(b).n for b in frames)
+    xyz = torch.empty((P, 3), dtype=torch.float32).pin_memory()
+    rgb = torch.empty((P, 3), dtype=torch.uint8).pin_memory()
+    st = np.zeros(nsl, np.int32)
+    dec = pvvc.Decoder(nslots=1024, max_leaves=8192, max_nodes=16384)
+    npts = ctypes.c_uint64(0)
+    sp = stream.cuda_stream
+
+    def call():
+        rc = lib.pvvc_decode_frames_host(dec.h, nf, ptrs, lens.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                         ctypes.cast(xyz.data_ptr(), ctypes.POINTER(ctypes.c_float)),
+                                         ctypes.cast(rgb.data_ptr(), ctypes.POINTER(ctypes.c_uint8)), P, ctypes.byref(npts),
+                                         st.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), nsl, sp)
+        if rc:
+            raise pvvc.PvvcError(rc, "pvvc_decode_frames_host")
+
+    for _ in range(2):
+        call()
+    assert (st == 0).all()
+    n = max(2, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        call()
+    dt = (time.perf_counter() - t0) / n
+    h2d = int(sum(len(b) for b in frames))
+    return {"value": P / dt / 1e6, "unit": "Mpts/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(15 * P + 4 * nsl),
+            "ms_per_step": dt * 1e3, "steps": n,
+            "note": "host .frame bytes -> parse -> H2D -> decode (one batch per GoP, slot = patch index) -> D2H"}
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

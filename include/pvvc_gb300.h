@@ -1,0 +1,161 @@
+/*
+ * pvvc_gb300.h -- C ABI of the GB300-native patchVVC per-patch codec path.
+ *
+ * Every entry point is extern "C" with plain pointers and sizes.  Device
+ * pointers are CUDA device memory owned by the caller; `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).  Calls that
+ * take a stream are stream-ordered and do not synchronise unless stated.
+ * Errors are returned as PVVC_* status codes; per-slice decode failures are
+ * reported in a caller-provided status array and never abort the batch.
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the patchVVC-plus project root).
+ */
+#ifndef PVVC_GB300_H_
+#define PVVC_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define PVVC_OK 0
+#define PVVC_ERR_ARG 1          /* invalid argument                               */
+#define PVVC_ERR_OVERRUN 2      /* colour bitstream ended before 3*size symbols    */
+#define PVVC_ERR_GEOMETRY 3     /* occupancy stream short or malformed            */
+#define PVVC_ERR_SIZE 4         /* leaf count != slice size, or size > capacity   */
+#define PVVC_ERR_NO_REFERENCE 5 /* predictive slice before any intra slice        */
+#define PVVC_ERR_BAD_SLICE 6    /* slice type lacks the VALID bit                 */
+#define PVVC_ERR_NOMEM 7        /* allocation failed                              */
+#define PVVC_ERR_CUDA 8         /* a CUDA runtime call failed                     */
+#define PVVC_ERR_ZSTD 9         /* zstd payload without libzstd, or corrupt       */
+#define PVVC_ERR_FORMAT 10      /* .frame / .slice bytes malformed                */
+#define PVVC_ERR_CAPACITY 11    /* output / workspace too small                   */
+#define PVVC_ERR_TREE 12        /* tree deeper or wider than the state slot holds */
+
+/* slice type bits, include/common/common.h:31-56 */
+#define PVVC_TYPE_VALID 0x01
+#define PVVC_TYPE_PREDICT 0x02
+#define PVVC_TYPE_SKIP 0x04
+#define PVVC_TYPE_GEO_ZSTD 0x08
+#define PVVC_TYPE_COLOR_ZSTD 0x10
+
+const char* pvvc_status_string(int status);
+
+/* ---- per-patch decoder state ---------------------------------------------
+ * Replaces the caller-allocated device array of persistent
+ * vvc::client::octree::InvertRAHTOctree objects (include/cuda/octree.cuh,
+ * src/cuda/common/manager.cc:235-238) and the CPU decoder's per-index
+ * handlers (src/codec/pvvc_decompression.cc:119-122).  A state holds `nslots`
+ * slots; slot i keeps the tree, leaf centres and reference colours of the
+ * last intra slice decoded into it (at most max_leaves leaves and max_nodes
+ * internal octree nodes).  Device memory, allocated here. */
+typedef struct pvvc_state pvvc_state;
+int pvvc_state_create(int32_t nslots, int32_t max_leaves, int32_t max_nodes, pvvc_state** out);
+int pvvc_state_destroy(pvvc_state* st);
+/* Mark every slot empty (a predictive slice then reports NO_REFERENCE). */
+int pvvc_state_reset(pvvc_state* st, void* stream);
+
+/* ---- decode plan ---------------------------------------------------------
+ * HOST-side slice metadata of one batch (any mix of intra and predictive
+ * slices of any frames, at most one intra slice per slot).  It replaces the
+ * host staging of src/cuda/common/manager.cc:41-72 and
+ * test/test_decode_only.cc:97-123: the per-slice index/type/size/qp/mv and
+ * payload pointers become offsets into one device payload buffer, and
+ * inner_offset becomes out_off. */
+typedef struct {
+    int32_t nslices;
+    const int32_t* slot;      /* state slot per slice (the patch index)           */
+    const uint8_t* type;      /* slice type bits                                   */
+    const uint32_t* size;     /* decoded point count                               */
+    const uint8_t* qp;        /* quantisation step                                 */
+    const float* mv;          /* nslices x 16 floats, row-major (.frame layout)    */
+    const uint64_t* geo_off;  /* byte offset of the raw geometry payload (intra)   */
+    const uint32_t* geo_size; /* 0 for predictive slices                           */
+    const uint64_t* col_off;  /* byte offset of the raw colour (RLGR) payload      */
+    const uint32_t* col_size;
+    const uint64_t* out_off;  /* first output point of the slice                   */
+} pvvc_batch_desc;
+
+typedef struct pvvc_plan pvvc_plan;
+/* Sorts the batch into the work queue (intra first, then by size) and uploads
+ * it (synchronous).  The plan is reusable for any payload with the same
+ * layout, and pvvc_decode on it is CUDA-graph capturable. */
+int pvvc_plan_create(const pvvc_batch_desc* desc, pvvc_plan** out);
+int pvvc_plan_destroy(pvvc_plan* plan);
+/* total output points, device workspace bytes pvvc_decode needs */
+int pvvc_plan_query(const pvvc_plan* plan, uint64_t* total_points, uint64_t* workspace_bytes);
+
+/* Decode one planned batch: RLGR -> dequantise -> (intra: occupancy tree
+ * expansion) -> inverse RAHT -> (+ reference colours) -> YUV->RGB -> rigid
+ * transform.  Replaces launch_cudaProcess / processCUDA
+ * (src/cuda/render/CUDA2OpenGL.cu:37-74, include/cuda/render.cuh:42-57) and
+ * the CPU path InvertRAHTOctree::SetSlice/GetPatch + the transform loop
+ * (src/octree/invert_raht_octree.cc:22-120, pvvc_decompression.cc:141-150).
+ *   payload      device bytes the plan's offsets index (raw, not zstd)
+ *   xyz          device float[3*points] transformed coordinates (or NULL)
+ *   rgb          device uint8[3*points] colours rounded as the CPU decoder
+ *                rounds them, clamped to [0,255] (or NULL)
+ *   points24     device float[6*points] in the reference GPU layout
+ *                {x,y,z,r/255,g/255,b/255} (CUDA2OpenGL.cu:12-16,44-58) (or NULL)
+ *   status       device int32[nslices]: per-slice PVVC_* status (or NULL)
+ *   workspace    device scratch of pvvc_plan_query's size */
+int pvvc_decode(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
+                float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, void* stream);
+
+/* pvvc_decode with a CUDA event recorded on `stream` before the first and
+ * after each of its four kernels (tree expansion, RLGR, inverse RAHT of the
+ * intra slices, inverse RAHT of the predictive slices): events[0..4] must be
+ * created by the caller.  No reference counterpart: the reference only
+ * prints wall-clock frame times (test/test_decode_only.cc:129-150). */
+int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
+                         float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, void* stream,
+                         void* const* events);
+
+/* ---- end-to-end host call ------------------------------------------------
+ * Decode whole .frame files held in HOST memory (the bytes of one or more
+ * consecutive frames of one sequence, in decode order) into HOST arrays.
+ * Mirrors io::LoadFrame + the H2D staging + launch_cudaProcess + the D2H
+ * read-back (src/cuda/common/slice_io.cu:143-275, manager.cc:41-72,230-270):
+ * zstd payloads are inflated on the host, payloads are copied to the device,
+ * decoded, and xyz/rgb are copied back.  Slot = patch index.  Synchronises
+ * `stream` before returning.  status_host receives one entry per slice, in
+ * file order. */
+int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* const* frame_bytes, const uint64_t* frame_len,
+                            float* xyz_host, uint8_t* rgb_host, uint64_t cap_points, uint64_t* npoints_out,
+                            int32_t* status_host, int32_t status_cap, void* stream);
+
+/* ---- reference-signature shim --------------------------------------------
+ * Same arguments as launch_cudaProcess (include/cuda/render.cuh:42-57) with
+ * the decoder array replaced by a pvvc_state (slot = index[i]).  All arrays
+ * are device memory as in the reference; out receives the 24-byte Points
+ * layout.  Unlike the reference, it runs on `stream`, returns a status, and
+ * copies the small metadata arrays to the host to plan (it synchronises). */
+int pvvc_launch_cudaProcess(int grid, int block, float* out_points24, int timestamp, int* inner_offset, int* index,
+                            uint8_t* type, float** mv, uint32_t* size, uint8_t* qp, uint8_t** geometry,
+                            uint32_t* geometry_size, uint8_t** color, uint32_t* color_size, pvvc_state* decoders,
+                            int patch_size, void* stream);
+
+/* ---- encoder (CPU) -------------------------------------------------------
+ * GoP encoding of one patch: the octree of the shared geometry
+ * (RAHTOctree::MakeTree/GetOctree, src/octree/raht_octree.cc:47-187), one
+ * RAHT + quantisation + RLGR payload per frame (raht_octree.cc:189-247,
+ * src/patch/GoP_encoding.cc:172-205, src/common/entropy_codec.cc:65-159).
+ * xyz: n x 3 points; yuv: nframes x n x 3 colours per input point, frame 0
+ * absolute and frames >0 residuals; qp per frame.  Outputs are host buffers;
+ * *geo_len / col_len[f] receive sizes; leaf_count receives the slice size. */
+int pvvc_encode_patch_gop(const float* xyz, uint32_t n, const float* yuv, int32_t nframes, const uint8_t* qp,
+                          uint8_t* geo_out, uint64_t geo_cap, uint64_t* geo_len, uint8_t* col_out, uint64_t col_cap_per_frame,
+                          uint64_t* col_len, uint32_t* leaf_count);
+
+/* RLGR codec on host buffers (entropy_codec.cc:65-283) */
+int64_t pvvc_rlgr_encode(const int64_t* sym, uint64_t n, uint8_t* out, uint64_t cap);
+int pvvc_rlgr_decode_host(const uint8_t* in, uint64_t nbytes, uint64_t nsym, int64_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

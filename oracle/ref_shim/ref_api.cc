@@ -1,0 +1,237 @@
+/*
+ * ref_api.cc -- a C ABI over the reference's own codec classes, compiled from
+ * the unmodified reference sources against the shim headers in this folder.
+ *
+ * TEST INFRASTRUCTURE ONLY (the oracle's pin).  It is built by
+ * `make -C oracle ref` into oracle/_ref/libpvvc_ref.so when the reference
+ * tree is present, and used to validate the C restatement (pvvc_oracle.c)
+ * and to generate the committed golden fixtures (tests/golden/).
+ *
+ * Classes driven here: vvc::common::RLGREncoder/RLGRDecoder and
+ * ZstdEncoder/ZstdDecoder (src/common/entropy_codec.cc),
+ * vvc::octree::RAHTOctree (src/octree/raht_octree.cc),
+ * vvc::octree::InvertRAHTOctree (src/octree/invert_raht_octree.cc),
+ * vvc::io::SaveSlice/LoadSlice/ChangeSliceToFrame (src/io/slice_io.cc).
+ */
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "common/entropy_codec.h"
+#include "io/slice_io.h"
+#include "octree/octree.h"
+
+using namespace vvc;
+
+namespace {
+common::PVVCParam_t::Ptr make_params(int zstd_level) {
+    auto p = std::make_shared<common::PVVCParam_t>();
+    p->octree.resolution = 1.0f;
+    p->zstd_level = zstd_level;
+    p->thread_num = 1;
+    return p;
+}
+}  // namespace
+
+extern "C" {
+
+/* ---- RLGR ---- */
+long ref_rlgr_encode(const int64_t* sym, size_t n, uint8_t* out, size_t cap) {
+    try {
+        auto data = std::make_shared<std::vector<common::FIX_DATA_INT>>(sym, sym + n);
+        common::RLGREncoder enc;
+        enc.Encode(data);
+        auto r = enc.GetResult();
+        if (r->size() > cap) return -2;
+        if (!r->empty()) std::memcpy(out, r->data(), r->size());
+        return (long)r->size();
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+/* Decodes and returns how many symbols the decoder produced (it may exceed
+ * nsym by a run's overshoot); copies min(produced, nsym). */
+long ref_rlgr_decode(const uint8_t* in, size_t nbytes, size_t nsym, int64_t* out) {
+    try {
+        auto data = std::make_shared<std::vector<uint8_t>>(in, in + nbytes);
+        common::RLGRDecoder dec;
+        dec.Decode(data, (int)nsym);
+        auto r = dec.GetResult();
+        size_t m = r->size() < nsym ? r->size() : nsym;
+        if (m) std::memcpy(out, r->data(), m * sizeof(int64_t));
+        return (long)r->size();
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+/* ---- zstd wrappers (entropy_codec.cc:289-373) ---- */
+long ref_zstd_encode(const uint8_t* in, size_t n, int level, uint8_t* out, size_t cap) {
+    try {
+        common::ZstdEncoder enc;
+        enc.SetParams(make_params(level));
+        enc.Encode(std::make_shared<std::vector<uint8_t>>(in, in + n));
+        auto r = enc.GetResult();
+        if (r->size() > cap) return -2;
+        std::memcpy(out, r->data(), r->size());
+        return (long)r->size();
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+long ref_zstd_decode(const uint8_t* in, size_t n, uint8_t* out, size_t cap) {
+    try {
+        common::ZstdDecoder dec;
+        dec.Decode(std::make_shared<std::vector<uint8_t>>(in, in + n));
+        auto r = dec.GetResult();
+        if (r->size() > cap) return -2;
+        std::memcpy(out, r->data(), r->size());
+        return (long)r->size();
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+/* ---- encoder octree + RAHT ---- */
+struct ref_encoder {
+    octree::RAHTOctree tree;
+    pcl::PointCloud<pcl::PointXYZRGB>::Ptr cloud;
+};
+
+void* ref_encoder_new(const float* xyz, size_t n) {
+    try {
+        auto* e = new ref_encoder();
+        e->cloud.reset(new pcl::PointCloud<pcl::PointXYZRGB>());
+        for (size_t i = 0; i < n; ++i) {
+            pcl::PointXYZRGB p;
+            p.x = xyz[3 * i];
+            p.y = xyz[3 * i + 1];
+            p.z = xyz[3 * i + 2];
+            e->cloud->push_back(p);
+        }
+        e->tree.SetParams(make_params(22));
+        e->tree.SetSourceCloud(e->cloud);
+        e->tree.MakeTree();
+        return e;
+    } catch (const common::Exception&) {
+        return nullptr;
+    }
+}
+
+void ref_encoder_free(void* h) { delete static_cast<ref_encoder*>(h); }
+
+long ref_encoder_geometry(void* h, uint8_t* out, size_t cap) {
+    auto r = static_cast<ref_encoder*>(h)->tree.GetOctree();
+    if (r->size() > cap) return -2;
+    std::memcpy(out, r->data(), r->size());
+    return (long)r->size();
+}
+
+/* yuv: n x 3 per input point; coef_out: leaf_count x 3 in stream order. */
+long ref_encoder_raht(void* h, const float* yuv, size_t n, float* coef_out, size_t cap_leaves) {
+    try {
+        auto* e = static_cast<ref_encoder*>(h);
+        auto colors = std::make_shared<std::vector<common::ColorYUV>>();
+        for (size_t i = 0; i < n; ++i) colors->emplace_back(yuv[3 * i], yuv[3 * i + 1], yuv[3 * i + 2], true);
+        e->tree.SetSourceColors(colors);
+        e->tree.RAHT();
+        auto r = e->tree.GetRAHTResult();
+        if (r->size() > cap_leaves) return -2;
+        for (size_t i = 0; i < r->size(); ++i) {
+            coef_out[3 * i] = r->at(i).y;
+            coef_out[3 * i + 1] = r->at(i).u;
+            coef_out[3 * i + 2] = r->at(i).v;
+        }
+        return (long)r->size();
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+/* ---- decoder ---- */
+struct ref_decoder {
+    octree::InvertRAHTOctree tree;
+    common::Patch last;
+};
+
+void* ref_decoder_new(void) {
+    auto* d = new ref_decoder();
+    d->tree.SetParams(make_params(22));
+    return d;
+}
+
+void ref_decoder_free(void* h) { delete static_cast<ref_decoder*>(h); }
+
+/* mv is column-major (as a Slice holds it).  Payloads as stored in a slice
+ * (possibly zstd frames, per the type bits). */
+int ref_decoder_set_slice(void* h, uint8_t type, int timestamp, int index, uint64_t size, uint8_t qp, const float* mv_colmajor,
+                          const uint8_t* geo, size_t gsz, const uint8_t* col, size_t csz) {
+    try {
+        auto* d = static_cast<ref_decoder*>(h);
+        common::Slice s;
+        s.type = type;
+        s.timestamp = timestamp;
+        s.index = index;
+        s.size = size;
+        s.qp = qp;
+        std::memcpy(s.mv.d, mv_colmajor, 16 * sizeof(float));
+        if (geo && gsz) s.geometry = std::make_shared<std::vector<uint8_t>>(geo, geo + gsz);
+        if (col && csz) s.color = std::make_shared<std::vector<uint8_t>>(col, col + csz);
+        d->tree.SetSlice(s);
+        d->last = d->tree.GetPatch();
+        return 0;
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+/* Points of the last decoded patch: pre-transform xyz and rgb as the
+ * reference casts it. */
+long ref_decoder_get_patch(void* h, float* xyz, uint8_t* rgb, size_t cap) {
+    auto* d = static_cast<ref_decoder*>(h);
+    if (!d->last.cloud) return -1;
+    size_t n = d->last.cloud->size();
+    if (n > cap) return -2;
+    for (size_t i = 0; i < n; ++i) {
+        const auto& p = d->last.cloud->at(i);
+        xyz[3 * i] = p.x;
+        xyz[3 * i + 1] = p.y;
+        xyz[3 * i + 2] = p.z;
+        rgb[3 * i] = p.r;
+        rgb[3 * i + 1] = p.g;
+        rgb[3 * i + 2] = p.b;
+    }
+    return (long)n;
+}
+
+/* ---- slice / frame files ---- */
+int ref_save_slice(const char* path, uint8_t type, int timestamp, int index, uint64_t size, uint8_t qp, const float* mv_colmajor,
+                   const uint8_t* geo, size_t gsz, const uint8_t* col, size_t csz) {
+    try {
+        common::Slice s;
+        s.type = type;
+        s.timestamp = timestamp;
+        s.index = index;
+        s.size = size;
+        s.qp = qp;
+        std::memcpy(s.mv.d, mv_colmajor, 16 * sizeof(float));
+        if (geo && gsz) s.geometry = std::make_shared<std::vector<uint8_t>>(geo, geo + gsz);
+        if (col && csz) s.color = std::make_shared<std::vector<uint8_t>>(col, col + csz);
+        return io::SaveSlice(s, path);
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+int ref_change_slice_to_frame(const char* dir, const char* out_name) {
+    try {
+        io::ChangeSliceToFrame(dir, out_name);
+        return 0;
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,480 @@
+// decode_api.cu -- host side of the decode path: state pools, work-queue
+// plans, the stream-ordered decode call, the end-to-end host call and the
+// reference-signature shim.  See include/pvvc_gb300.h for the contract.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "../host/bitstream.h"
+#include "decode_types.h"
+#include "pvvc_gb300.h"
+
+namespace pvvc {
+cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payload, const StateView& st, int32_t* tstatus,
+                        cudaStream_t s);
+cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
+                        int32_t* rstatus, cudaStream_t s);
+cudaError_t launch_raht(const SliceWork* work, int first, int count, const StateView& st, const float* coef, float* fallback,
+                        const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz, uint8_t* rgb, float* p24,
+                        int32_t* status, int wcap, cudaStream_t s);
+
+// level-signal capacity (nodes) of the shared-memory path of k_raht
+constexpr int kRahtWcap = 2048;
+
+namespace {
+inline uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+// grow-only device buffer
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) cap = n;
+        return e;
+    }
+};
+struct HostBuf {  // pinned, grow-only
+    void* p = nullptr;
+    size_t cap = 0;
+    ~HostBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMallocHost(&p, n);
+        if (e == cudaSuccess) cap = n;
+        return e;
+    }
+};
+}  // namespace
+}  // namespace pvvc
+
+struct pvvc_plan {
+    int32_t nslices = 0, nintra = 0, max_slot = -1;
+    uint64_t total_points = 0;
+    uint64_t ws_coef = 0, ws_fb = 0, ws_tstatus = 0, ws_rstatus = 0, ws_fstatus = 0, ws_bytes = 0;
+    std::vector<pvvc::SliceWork> work;
+    std::vector<int32_t> order;
+    pvvc::DevBuf d_work, d_order;
+};
+
+struct pvvc_state {
+    pvvc::StateView v{};
+    // buffers of the end-to-end host call, kept across calls
+    pvvc::DevBuf payload, xyz, rgb, ws, status;
+    pvvc::HostBuf h_payload;
+    pvvc_plan plan;
+};
+
+namespace pvvc {
+namespace {
+
+int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
+    if (!d || d->nslices < 0) return PVVC_ERR_ARG;
+    const int n = d->nslices;
+    if (n > 0 && (!d->slot || !d->type || !d->size || !d->qp || !d->mv || !d->geo_off || !d->geo_size || !d->col_off ||
+                  !d->col_size || !d->out_off))
+        return PVVC_ERR_ARG;
+    std::vector<int32_t> intra, pred;
+    int32_t max_slot = -1;
+    for (int i = 0; i < n; ++i) {
+        if (d->slot[i] < 0) return PVVC_ERR_ARG;
+        max_slot = std::max(max_slot, d->slot[i]);
+        ((d->type[i] & PVVC_TYPE_PREDICT) ? pred : intra).push_back(i);
+    }
+    // at most one intra slice per slot in a batch (it rebuilds the slot)
+    {
+        std::vector<int32_t> s;
+        for (int i : intra) s.push_back(d->slot[i]);
+        std::sort(s.begin(), s.end());
+        if (std::adjacent_find(s.begin(), s.end()) != s.end()) return PVVC_ERR_ARG;
+    }
+    auto by_size = [&](int32_t a, int32_t b) { return d->size[a] != d->size[b] ? d->size[a] > d->size[b] : a < b; };
+    std::stable_sort(intra.begin(), intra.end(), by_size);
+    std::stable_sort(pred.begin(), pred.end(), by_size);
+    p->nslices = n;
+    p->nintra = (int32_t)intra.size();
+    p->max_slot = max_slot;
+    p->work.resize(n);
+    uint64_t coef = 0, fb = 0, pts = 0;
+    auto fill = [&](int q, int i) {
+        SliceWork& w = p->work[q];
+        std::memset(&w, 0, sizeof(w));
+        w.col_off = d->col_off[i];
+        w.geo_off = d->geo_off[i];
+        w.out_off = d->out_off[i];
+        w.csz = d->col_size[i];
+        w.gsz = d->geo_size[i];
+        w.n = d->size[i];
+        w.slot = d->slot[i];
+        w.orig = i;
+        w.type = d->type[i];
+        w.qp = d->qp[i];
+        for (int k = 0; k < 12; ++k) w.mv[k] = d->mv[16ull * i + k];
+        w.coef_off = coef;
+        coef += 3ull * w.n;
+        if (w.n > (uint32_t)kRahtWcap) {
+            w.fb_off = fb;
+            fb += 6ull * w.n;
+        } else {
+            w.fb_off = ~0ull;
+        }
+        pts = std::max<uint64_t>(pts, d->out_off[i] + w.n);
+    };
+    int q = 0;
+    for (int i : intra) fill(q++, i);
+    for (int i : pred) fill(q++, i);
+    p->total_points = pts;
+    // RLGR order: all slices by size, so that a warp decodes similar lengths
+    p->order.resize(n);
+    std::iota(p->order.begin(), p->order.end(), 0);
+    std::stable_sort(p->order.begin(), p->order.end(), [&](int32_t a, int32_t b) { return p->work[a].n > p->work[b].n; });
+    // workspace layout
+    uint64_t off = 0;
+    p->ws_coef = off;
+    off = align_up(off + coef * 4, 256);
+    p->ws_fb = off;
+    off = align_up(off + fb * 4, 256);
+    p->ws_tstatus = off;
+    off = align_up(off + 4ull * n, 256);
+    p->ws_rstatus = off;
+    off = align_up(off + 4ull * n, 256);
+    p->ws_fstatus = off;
+    off = align_up(off + 4ull * n, 256);
+    p->ws_bytes = std::max<uint64_t>(off, 256);
+    // upload
+    if (n > 0) {
+        if (p->d_work.ensure(sizeof(SliceWork) * n) != cudaSuccess) return PVVC_ERR_NOMEM;
+        if (p->d_order.ensure(4ull * n) != cudaSuccess) return PVVC_ERR_NOMEM;
+        if (cudaMemcpy(p->d_work.p, p->work.data(), sizeof(SliceWork) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        if (cudaMemcpy(p->d_order.p, p->order.data(), 4ull * n, cudaMemcpyHostToDevice) != cudaSuccess) return PVVC_ERR_CUDA;
+    }
+    return PVVC_OK;
+}
+
+int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb, float* p24,
+               int32_t* status, void* ws, uint64_t ws_bytes, cudaStream_t s, void* const* events = nullptr) {
+    if (!p || !st) return PVVC_ERR_ARG;
+    if (p->nslices == 0) return PVVC_OK;
+    if (!payload || (reinterpret_cast<uintptr_t>(payload) & 3u)) return PVVC_ERR_ARG;
+    if (!ws || ws_bytes < p->ws_bytes || (reinterpret_cast<uintptr_t>(ws) & 255u)) return PVVC_ERR_CAPACITY;
+    if (p->max_slot >= st->v.nslots) return PVVC_ERR_ARG;
+    uint8_t* w = static_cast<uint8_t*>(ws);
+    float* coef = reinterpret_cast<float*>(w + p->ws_coef);
+    float* fb = reinterpret_cast<float*>(w + p->ws_fb);
+    int32_t* ts = reinterpret_cast<int32_t*>(w + p->ws_tstatus);
+    int32_t* rs = reinterpret_cast<int32_t*>(w + p->ws_rstatus);
+    int32_t* fs = reinterpret_cast<int32_t*>(w + p->ws_fstatus);
+    const SliceWork* dw = static_cast<const SliceWork*>(p->d_work.p);
+    const int32_t* ord = static_cast<const int32_t*>(p->d_order.p);
+    auto mark = [&](int i) {
+        return !events || cudaEventRecord(static_cast<cudaEvent_t>(events[i]), s) == cudaSuccess;
+    };
+    if (!mark(0)) return PVVC_ERR_CUDA;
+    if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) return PVVC_ERR_CUDA;
+    if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, s) != cudaSuccess || !mark(2)) return PVVC_ERR_CUDA;
+    if (launch_raht(dw, 0, p->nintra, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap, s) != cudaSuccess ||
+        !mark(3))
+        return PVVC_ERR_CUDA;
+    if (launch_raht(dw, p->nintra, p->nslices - p->nintra, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap,
+                    s) != cudaSuccess ||
+        !mark(4))
+        return PVVC_ERR_CUDA;
+    return PVVC_OK;
+}
+
+}  // namespace
+}  // namespace pvvc
+
+using namespace pvvc;
+
+extern "C" const char* pvvc_status_string(int s) {
+    switch (s) {
+        case PVVC_OK: return "ok";
+        case PVVC_ERR_ARG: return "invalid argument";
+        case PVVC_ERR_OVERRUN: return "colour bitstream ended before all symbols were decoded";
+        case PVVC_ERR_GEOMETRY: return "occupancy stream short or malformed";
+        case PVVC_ERR_SIZE: return "leaf count does not match the slice size";
+        case PVVC_ERR_NO_REFERENCE: return "predictive slice without an intra slice";
+        case PVVC_ERR_BAD_SLICE: return "invalid slice type";
+        case PVVC_ERR_NOMEM: return "out of memory";
+        case PVVC_ERR_CUDA: return "CUDA runtime error";
+        case PVVC_ERR_ZSTD: return "zstd payload cannot be decoded";
+        case PVVC_ERR_FORMAT: return "malformed .frame / .slice bytes";
+        case PVVC_ERR_CAPACITY: return "output or workspace too small";
+        case PVVC_ERR_TREE: return "octree exceeds the state slot capacity";
+        default: return "unknown status";
+    }
+}
+
+extern "C" int pvvc_state_create(int32_t nslots, int32_t max_leaves, int32_t max_nodes, pvvc_state** out) {
+    if (!out || nslots <= 0 || max_leaves <= 0 || max_nodes <= 0) return PVVC_ERR_ARG;
+    *out = nullptr;
+    auto st = std::make_unique<pvvc_state>();
+    StateView& v = st->v;
+    v.nslots = nslots;
+    v.max_leaves = max_leaves;
+    v.max_nodes = max_nodes;
+    const size_t S = (size_t)nslots, Nn = (size_t)max_nodes, Nl = (size_t)max_leaves;
+    bool ok = true;
+    auto alloc = [&](void** p, size_t bytes) {
+        if (!ok) return;
+        if (cudaMalloc(p, bytes) != cudaSuccess) ok = false;
+    };
+    alloc((void**)&v.info, sizeof(SlotInfo) * S);
+    alloc((void**)&v.occ, S * Nn);
+    alloc((void**)&v.mask, S * Nn);
+    alloc((void**)&v.cbase, 4 * S * Nn);
+    alloc((void**)&v.coff, 4 * S * Nn);
+    alloc((void**)&v.ab, sizeof(float2) * 7 * S * Nn);
+    alloc((void**)&v.wsum, 4 * S * Nn);
+    alloc((void**)&v.ctr, 12 * S * Nn);
+    alloc((void**)&v.xyz, 12 * S * Nl);
+    alloc((void**)&v.ref, 12 * S * Nl);
+    if (!ok || cudaMemset(v.info, 0, sizeof(SlotInfo) * S) != cudaSuccess) {
+        pvvc_state_destroy(st.release());
+        return PVVC_ERR_NOMEM;
+    }
+    *out = st.release();
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_state_destroy(pvvc_state* st) {
+    if (!st) return PVVC_ERR_ARG;
+    StateView& v = st->v;
+    void* ptrs[] = {v.info, v.occ, v.mask, v.cbase, v.coff, v.ab, v.wsum, v.ctr, v.xyz, v.ref};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete st;
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_state_reset(pvvc_state* st, void* stream) {
+    if (!st) return PVVC_ERR_ARG;
+    return cudaMemsetAsync(st->v.info, 0, sizeof(SlotInfo) * st->v.nslots, (cudaStream_t)stream) == cudaSuccess ? PVVC_OK
+                                                                                                                : PVVC_ERR_CUDA;
+}
+
+extern "C" int pvvc_plan_create(const pvvc_batch_desc* desc, pvvc_plan** out) {
+    if (!out) return PVVC_ERR_ARG;
+    *out = nullptr;
+    auto p = std::make_unique<pvvc_plan>();
+    int s = build_plan(desc, p.get());
+    if (s) return s;
+    *out = p.release();
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_plan_destroy(pvvc_plan* p) {
+    if (!p) return PVVC_ERR_ARG;
+    delete p;
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_plan_query(const pvvc_plan* p, uint64_t* total_points, uint64_t* workspace_bytes) {
+    if (!p) return PVVC_ERR_ARG;
+    if (total_points) *total_points = p->total_points;
+    if (workspace_bytes) *workspace_bytes = p->ws_bytes;
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_decode(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
+                           float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, void* stream) {
+    return run_decode(plan, st, payload, xyz, rgb, points24, status, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
+                                    float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, void* stream,
+                                    void* const* events) {
+    if (!events) return PVVC_ERR_ARG;
+    return run_decode(plan, st, payload, xyz, rgb, points24, status, workspace, workspace_bytes, (cudaStream_t)stream, events);
+}
+
+extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* const* frame_bytes,
+                                       const uint64_t* frame_len, float* xyz_host, uint8_t* rgb_host, uint64_t cap_points,
+                                       uint64_t* npoints_out, int32_t* status_host, int32_t status_cap, void* stream) {
+    if (!st || nframes < 0 || (nframes && (!frame_bytes || !frame_len))) return PVVC_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    // parse (io::LoadFrame) and inflate zstd on the host
+    std::vector<Frame> frames(nframes);
+    for (int f = 0; f < nframes; ++f) {
+        int r = parse_frame(frame_bytes[f], frame_len[f], &frames[f]);
+        if (r) return r;
+        r = frame_inflate(&frames[f]);
+        if (r) return r;
+    }
+    // pack payloads (4-byte aligned) and build the batch description
+    uint64_t bytes = 0, pts = 0;
+    int32_t nsl = 0;
+    for (auto& fr : frames) {
+        for (size_t i = 0; i < fr.count(); ++i) {
+            bytes = align_up(bytes + fr.geometry[i].size(), 4);
+            bytes = align_up(bytes + fr.color[i].size(), 4);
+            pts += fr.size[i];
+        }
+        nsl += (int32_t)fr.count();
+    }
+    if (npoints_out) *npoints_out = pts;
+    if (pts > cap_points || (status_host && status_cap < nsl)) return PVVC_ERR_CAPACITY;
+    if (st->h_payload.ensure(std::max<uint64_t>(bytes, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    uint8_t* hp = static_cast<uint8_t*>(st->h_payload.p);
+    std::vector<int32_t> slot(nsl);
+    std::vector<uint8_t> type(nsl), qp(nsl);
+    std::vector<uint32_t> size(nsl), gsz(nsl), csz(nsl);
+    std::vector<float> mv(16ull * nsl);
+    std::vector<uint64_t> goff(nsl), coff(nsl), oo(nsl);
+    uint64_t off = 0, po = 0;
+    int32_t k = 0;
+    for (auto& fr : frames)
+        for (size_t i = 0; i < fr.count(); ++i, ++k) {
+            slot[k] = fr.index[i];
+            type[k] = fr.type[i];
+            qp[k] = fr.qp[i];
+            size[k] = fr.size[i];
+            std::memcpy(&mv[16ull * k], &fr.mv[16 * i], 64);
+            goff[k] = off;
+            gsz[k] = (uint32_t)fr.geometry[i].size();
+            if (gsz[k]) std::memcpy(hp + off, fr.geometry[i].data(), gsz[k]);
+            off = align_up(off + gsz[k], 4);
+            coff[k] = off;
+            csz[k] = (uint32_t)fr.color[i].size();
+            if (csz[k]) std::memcpy(hp + off, fr.color[i].data(), csz[k]);
+            off = align_up(off + csz[k], 4);
+            oo[k] = po;
+            po += size[k];
+        }
+    // intra slices of different frames of one call may hit the same slot:
+    // decode frame groups in order, one batch per run without a repeated slot
+    pvvc_batch_desc d{};
+    int32_t first = 0;
+    int rc = PVVC_OK;
+    if (st->payload.ensure(std::max<uint64_t>(bytes, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (bytes && cudaMemcpyAsync(st->payload.p, hp, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return PVVC_ERR_CUDA;
+    std::vector<uint8_t> seen(std::max(st->v.nslots, 1), 0);
+    size_t fstart = 0;
+    k = 0;
+    std::vector<int32_t> bounds;  // slice index where each batch starts
+    bounds.push_back(0);
+    for (auto& fr : frames) {
+        bool clash = false;
+        for (size_t i = 0; i < fr.count(); ++i)
+            if (!(fr.type[i] & PVVC_TYPE_PREDICT) && fr.index[i] >= 0 && fr.index[i] < st->v.nslots && seen[fr.index[i]])
+                clash = true;
+        if (clash) {
+            bounds.push_back(k);
+            std::fill(seen.begin(), seen.end(), 0);
+        }
+        for (size_t i = 0; i < fr.count(); ++i, ++k)
+            if (fr.index[i] >= 0 && fr.index[i] < st->v.nslots) seen[fr.index[i]] = 1;
+    }
+    bounds.push_back(nsl);
+    (void)fstart;
+    for (size_t b = 0; b + 1 < bounds.size() && rc == PVVC_OK; ++b) {
+        first = bounds[b];
+        const int32_t cnt = bounds[b + 1] - first;
+        if (cnt <= 0) continue;
+        d.nslices = cnt;
+        d.slot = slot.data() + first;
+        d.type = type.data() + first;
+        d.size = size.data() + first;
+        d.qp = qp.data() + first;
+        d.mv = mv.data() + 16ull * first;
+        d.geo_off = goff.data() + first;
+        d.geo_size = gsz.data() + first;
+        d.col_off = coff.data() + first;
+        d.col_size = csz.data() + first;
+        d.out_off = oo.data() + first;
+        rc = build_plan(&d, &st->plan);
+        if (rc) break;
+        if (st->ws.ensure(st->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
+        rc = run_decode(&st->plan, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
+                        static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
+                        st->ws.cap, s);
+        // the plan's host arrays are rebuilt by the next batch: finish this one first
+        if (rc == PVVC_OK && bounds.size() > 2 && cudaStreamSynchronize(s) != cudaSuccess) rc = PVVC_ERR_CUDA;
+    }
+    if (rc) return rc;
+    if (xyz_host && pts && cudaMemcpyAsync(xyz_host, st->xyz.p, 12 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return PVVC_ERR_CUDA;
+    if (rgb_host && pts && cudaMemcpyAsync(rgb_host, st->rgb.p, 3 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return PVVC_ERR_CUDA;
+    if (status_host && nsl && cudaMemcpyAsync(status_host, st->status.p, 4ull * nsl, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        return PVVC_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return PVVC_ERR_CUDA;
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_launch_cudaProcess(int grid, int block, float* out_points24, int timestamp, int* inner_offset, int* index,
+                                       uint8_t* type, float** mv, uint32_t* size, uint8_t* qp, uint8_t** geometry,
+                                       uint32_t* geometry_size, uint8_t** color, uint32_t* color_size, pvvc_state* decoders,
+                                       int patch_size, void* stream) {
+    (void)grid;
+    (void)block;
+    (void)timestamp;
+    if (!decoders || patch_size < 0 || !out_points24) return PVVC_ERR_ARG;
+    if (patch_size == 0) return PVVC_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const int n = patch_size;
+    std::vector<int> h_off(n), h_idx(n);
+    std::vector<uint8_t> h_type(n), h_qp(n);
+    std::vector<uint32_t> h_size(n), h_gsz(n), h_csz(n);
+    std::vector<float*> h_mv(n);
+    std::vector<uint8_t*> h_geo(n), h_col(n);
+    auto d2h = [&](void* dst, const void* src, size_t b) {
+        return cudaMemcpyAsync(dst, src, b, cudaMemcpyDeviceToHost, s) == cudaSuccess;
+    };
+    if (!d2h(h_off.data(), inner_offset, 4ull * n) || !d2h(h_idx.data(), index, 4ull * n) || !d2h(h_type.data(), type, n) ||
+        !d2h(h_qp.data(), qp, n) || !d2h(h_size.data(), size, 4ull * n) || !d2h(h_gsz.data(), geometry_size, 4ull * n) ||
+        !d2h(h_csz.data(), color_size, 4ull * n) || !d2h(h_mv.data(), mv, sizeof(float*) * n) ||
+        !d2h(h_geo.data(), geometry, sizeof(uint8_t*) * n) || !d2h(h_col.data(), color, sizeof(uint8_t*) * n))
+        return PVVC_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return PVVC_ERR_CUDA;
+    std::vector<float> h_m(16ull * n);
+    for (int i = 0; i < n; ++i)
+        if (!d2h(&h_m[16ull * i], h_mv[i], 64)) return PVVC_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return PVVC_ERR_CUDA;
+    // payload base: the lowest payload pointer; offsets are address differences
+    uintptr_t base = UINTPTR_MAX;
+    for (int i = 0; i < n; ++i) {
+        if (h_gsz[i] && h_geo[i]) base = std::min(base, reinterpret_cast<uintptr_t>(h_geo[i]));
+        if (h_csz[i] && h_col[i]) base = std::min(base, reinterpret_cast<uintptr_t>(h_col[i]));
+    }
+    if (base == UINTPTR_MAX) return PVVC_ERR_ARG;
+    base &= ~uintptr_t(3);
+    std::vector<int32_t> slot(n);
+    std::vector<uint64_t> goff(n), coff(n), oo(n);
+    for (int i = 0; i < n; ++i) {
+        slot[i] = h_idx[i];
+        goff[i] = h_gsz[i] ? reinterpret_cast<uintptr_t>(h_geo[i]) - base : 0;
+        coff[i] = h_csz[i] ? reinterpret_cast<uintptr_t>(h_col[i]) - base : 0;
+        oo[i] = (uint64_t)h_off[i];
+    }
+    pvvc_batch_desc d{n, slot.data(), h_type.data(), h_size.data(), h_qp.data(), h_m.data(), goff.data(), h_gsz.data(),
+                      coff.data(), h_csz.data(), oo.data()};
+    int rc = build_plan(&d, &decoders->plan);
+    if (rc) return rc;
+    if (decoders->ws.ensure(decoders->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
+    rc = run_decode(&decoders->plan, decoders, reinterpret_cast<const uint8_t*>(base), nullptr, nullptr, out_points24, nullptr,
+                    decoders->ws.p, decoders->ws.cap, s);
+    if (rc) return rc;
+    return cudaStreamSynchronize(s) == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
+}

@@ -1,0 +1,51 @@
+// decode_types.h -- device-side layouts shared by the decode kernels and
+// their host launchers.
+#pragma once
+
+#include <cstdint>
+
+namespace pvvc {
+
+constexpr int kMaxLevels = 32;  // octree height limit (the header stores a u8)
+
+// One slice in the work queue (queue order = intra first, then by size).
+struct SliceWork {
+    uint64_t col_off;   // colour payload byte offset
+    uint64_t geo_off;   // geometry payload byte offset (intra)
+    uint64_t out_off;   // first output point
+    uint64_t coef_off;  // float offset of the slice's 3 coefficient planes in workspace
+    uint64_t fb_off;    // float offset of the level-buffer fallback region (~0: none)
+    uint32_t csz, gsz;
+    uint32_t n;         // slice size (points)
+    int32_t slot;       // state slot
+    int32_t orig;       // index in the caller's arrays (status)
+    uint8_t type, qp, pad0, pad1;
+    float mv[12];       // first three rows of the row-major 4x4
+};
+
+// Per-slot header of a decoded tree (device).
+struct SlotInfo {
+    int32_t valid;          // an intra slice populated the slot
+    int32_t height;         // octree height H (levels 0..H-1, leaves at H-1)
+    int32_t nodes;          // internal nodes (levels 0..H-2)
+    int32_t leaves;         // leaf count (= slice size)
+    int32_t max_width;      // widest internal level
+    int32_t level_start[kMaxLevels + 1];  // first internal node of each level
+};
+
+// Device pointers of a state pool (slot-major arrays).
+struct StateView {
+    SlotInfo* info;          // [nslots]
+    uint8_t* occ;            // [nslots * max_nodes] occupancy byte
+    uint8_t* mask;           // [nslots * max_nodes] coded-coefficient bits (1..7)
+    uint32_t* cbase;         // [nslots * max_nodes] first child (index within next level)
+    uint32_t* coff;          // [nslots * max_nodes] first coefficient index
+    float2* ab;              // [nslots * max_nodes * 7] butterfly (a,b) per i = 1..7
+    uint32_t* wsum;          // [nslots * max_nodes] subtree leaf count (build scratch)
+    float* ctr;              // [nslots * max_nodes * 3] node centres (build scratch)
+    float* xyz;              // [nslots * max_leaves * 3] leaf centres
+    float* ref;              // [nslots * max_leaves * 3] reference YUV (intra result)
+    int32_t nslots, max_leaves, max_nodes;
+};
+
+}  // namespace pvvc

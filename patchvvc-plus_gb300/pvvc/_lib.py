@@ -1,0 +1,112 @@
+"""Loads libpvvc_gb300.so (built in-tree next to this package) and declares
+the C ABI of include/pvvc_gb300.h for ctypes.  There is no fallback: if the
+library is missing, importing the decoder raises."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_PKG_ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(_PKG_ROOT, "libpvvc_gb300.so")
+
+u8p = C.POINTER(C.c_uint8)
+f32p = C.POINTER(C.c_float)
+i32p = C.POINTER(C.c_int32)
+u32p = C.POINTER(C.c_uint32)
+i64p = C.POINTER(C.c_int64)
+u64p = C.POINTER(C.c_uint64)
+vp = C.c_void_p
+
+STATUS = {
+    0: "PVVC_OK", 1: "PVVC_ERR_ARG", 2: "PVVC_ERR_OVERRUN", 3: "PVVC_ERR_GEOMETRY", 4: "PVVC_ERR_SIZE",
+    5: "PVVC_ERR_NO_REFERENCE", 6: "PVVC_ERR_BAD_SLICE", 7: "PVVC_ERR_NOMEM", 8: "PVVC_ERR_CUDA", 9: "PVVC_ERR_ZSTD",
+    10: "PVVC_ERR_FORMAT", 11: "PVVC_ERR_CAPACITY", 12: "PVVC_ERR_TREE",
+}
+
+
+class BatchDesc(C.Structure):
+    _fields_ = [("nslices", C.c_int32), ("slot", i32p), ("type", u8p), ("size", u32p), ("qp", u8p), ("mv", f32p),
+                ("geo_off", u64p), ("geo_size", u32p), ("col_off", u64p), ("col_size", u32p), ("out_off", u64p)]
+
+
+class IcpParams(C.Structure):
+    _fields_ = [("max_corr_dist", C.c_float), ("max_iter", C.c_int32), ("fitness_eps", C.c_float),
+                ("transform_eps", C.c_float)]
+
+
+class SynthConfig(C.Structure):
+    _fields_ = [("grid_bits", C.c_int32), ("nprims", C.c_int32), ("axis_min", C.c_float), ("axis_max", C.c_float),
+                ("target_points", C.c_int32), ("nframes", C.c_int32), ("gof", C.c_int32), ("size_mode", C.c_int32),
+                ("size_a", C.c_float), ("size_b", C.c_float), ("size_min", C.c_float), ("size_max", C.c_float),
+                ("qp_i", C.c_uint8), ("qp_p", C.c_uint8), ("rot_deg", C.c_float), ("trans_vox", C.c_float),
+                ("jitter", C.c_float), ("color_noise", C.c_float), ("seed", C.c_uint64), ("nthreads", C.c_int32)]
+
+
+# (name, restype, argtypes) of every exported entry point
+SIGNATURES = [
+    ("pvvc_status_string", C.c_char_p, [C.c_int]),
+    ("pvvc_state_create", C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(vp)]),
+    ("pvvc_state_destroy", C.c_int, [vp]),
+    ("pvvc_state_reset", C.c_int, [vp, vp]),
+    ("pvvc_plan_create", C.c_int, [C.POINTER(BatchDesc), C.POINTER(vp)]),
+    ("pvvc_plan_destroy", C.c_int, [vp]),
+    ("pvvc_plan_query", C.c_int, [vp, u64p, u64p]),
+    ("pvvc_decode", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, vp]),
+    ("pvvc_decode_profiled", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, vp, C.POINTER(vp)]),
+    ("pvvc_decode_frames_host", C.c_int, [vp, C.c_int32, C.POINTER(u8p), u64p, f32p, u8p, C.c_uint64, u64p, i32p,
+                                          C.c_int32, vp]),
+    ("pvvc_launch_cudaProcess", C.c_int, [C.c_int, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                          C.c_int, vp]),
+    ("pvvc_encode_patch_gop", C.c_int, [f32p, C.c_uint32, f32p, C.c_int32, u8p, u8p, C.c_uint64, u64p, u8p,
+                                        C.c_uint64, u64p, u32p]),
+    ("pvvc_rlgr_encode", C.c_int64, [i64p, C.c_uint64, u8p, C.c_uint64]),
+    ("pvvc_rlgr_decode_host", C.c_int, [u8p, C.c_uint64, C.c_uint64, i64p]),
+    # synthetic sequences (not part of the drop-in boundary)
+    ("pvvc_synth_create", C.c_int, [C.POINTER(SynthConfig), C.POINTER(vp)]),
+    ("pvvc_synth_destroy", None, [vp]),
+    ("pvvc_synth_gof_count", C.c_int32, [vp]),
+    ("pvvc_synth_patch_count", C.c_int32, [vp, C.c_int32]),
+    ("pvvc_synth_patch", C.c_int, [vp, C.c_int32, C.c_int32, f32p, f32p, f32p, u32p, i32p]),
+    ("pvvc_synth_encode", C.c_int, [vp]),
+    ("pvvc_synth_frame", C.c_int, [vp, C.c_int32, C.POINTER(u8p), u64p]),
+    ("pvvc_synth_frame_points", C.c_uint64, [vp, C.c_int32]),
+]
+
+_LIB = None
+
+
+def lib():
+    """The loaded library.  Raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it first (python patchvvc-plus_gb300/build.py)")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+class PvvcError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {STATUS.get(status, status)} ({lib().pvvc_status_string(status).decode()})")
+
+
+def check(status: int, what: str = "") -> None:
+    if status != 0:
+        raise PvvcError(status, what)
+
+
+def build_library(verbose: bool = False) -> str:
+    """Compile libpvvc_gb300.so in-tree (patchvvc-plus_gb300/build.py)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("pvvc_gb300_build", os.path.join(_PKG_ROOT, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(verbose=verbose)

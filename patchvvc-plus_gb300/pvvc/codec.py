@@ -1,0 +1,152 @@
+"""Python mirror of the reference's codec interface over the C ABI.
+
+  Decoder           ~ the per-patch-index InvertRAHTOctree handlers plus
+                      PVVCDecompression (src/octree/invert_raht_octree.cc,
+                      src/codec/pvvc_decompression.cc): decode .frame bytes.
+  Plan / decode     ~ launch_cudaProcess (src/cuda/render/CUDA2OpenGL.cu:68-74)
+                      on device-resident batches.
+  encode_patch_gop  ~ GoPEncoding::Encode's per-patch back end
+                      (src/patch/GoP_encoding.cc:152-205).
+  rlgr_encode/_decode ~ RLGREncoder / RLGRDecoder (src/common/entropy_codec.cc).
+Errors raise PvvcError carrying the PVVC_* status, as the reference raises
+vvc::common::Exception.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .frame import Batch
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+def rlgr_encode(sym) -> bytes:
+    sym = np.ascontiguousarray(sym, np.int64)
+    cap = 16 * sym.size + 64
+    out = np.zeros(cap, np.uint8)
+    n = L.lib().pvvc_rlgr_encode(_p(sym, L.i64p), sym.size, _p(out, L.u8p), cap)
+    if n < 0:
+        raise L.PvvcError(int(-n), "rlgr_encode")
+    return out[:n].tobytes()
+
+
+def rlgr_decode(data: bytes, nsym: int) -> np.ndarray:
+    buf = np.frombuffer(data, np.uint8).copy() if data else np.zeros(1, np.uint8)
+    out = np.zeros(max(nsym, 1), np.int64)
+    L.check(L.lib().pvvc_rlgr_decode_host(_p(buf, L.u8p), len(data), nsym, _p(out, L.i64p)), "rlgr_decode")
+    return out[:nsym]
+
+
+def encode_patch_gop(xyz: np.ndarray, yuv: np.ndarray, qps) -> tuple[bytes, int, list[bytes]]:
+    """Geometry payload, slice size and one colour payload per frame.
+    yuv: (nframes, n, 3): frame 0 absolute, later frames residuals."""
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    yuv = np.ascontiguousarray(yuv, np.float32)
+    n = xyz.shape[0]
+    nf = yuv.shape[0]
+    qp = np.ascontiguousarray(qps, np.uint8)
+    gcap = 25 + 32 * n + 64
+    ccap = 64 * n + 256
+    geo = np.zeros(gcap, np.uint8)
+    col = np.zeros(nf * ccap, np.uint8)
+    glen = C.c_uint64(0)
+    clen = np.zeros(nf, np.uint64)
+    nl = C.c_uint32(0)
+    L.check(L.lib().pvvc_encode_patch_gop(_p(xyz, L.f32p), n, _p(yuv, L.f32p), nf, _p(qp, L.u8p), _p(geo, L.u8p), gcap,
+                                          C.byref(glen), _p(col, L.u8p), ccap, _p(clen, L.u64p), C.byref(nl)),
+            "encode_patch_gop")
+    cols = [col[f * ccap:f * ccap + int(clen[f])].tobytes() for f in range(nf)]
+    return geo[:glen.value].tobytes(), int(nl.value), cols
+
+
+class Decoder:
+    """Device-resident per-patch decoder state (pvvc_state): `nslots` slots,
+    each holding one patch's octree (<= max_leaves leaves, <= max_nodes
+    internal nodes) and reference colours."""
+
+    def __init__(self, nslots: int = 1024, max_leaves: int = 10000, max_nodes: int | None = None):
+        if max_nodes is None:
+            max_nodes = max_leaves * 2
+        h = L.vp()
+        L.check(L.lib().pvvc_state_create(nslots, max_leaves, max_nodes, C.byref(h)), "pvvc_state_create")
+        self.h = h
+        self.nslots, self.max_leaves, self.max_nodes = nslots, max_leaves, max_nodes
+
+    def close(self):
+        if self.h:
+            L.lib().pvvc_state_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reset(self, stream: int = 0):
+        L.check(L.lib().pvvc_state_reset(self.h, stream), "pvvc_state_reset")
+
+    def decode_frames(self, frames: list[bytes], stream: int = 0):
+        """End-to-end host call: .frame bytes in, (xyz float32 [P,3], rgb
+        uint8 [P,3], per-slice status int32) out."""
+        nf = len(frames)
+        bufs = [np.frombuffer(b, np.uint8) for b in frames]
+        ptrs = (L.u8p * max(nf, 1))(*[_p(b, L.u8p) for b in bufs])
+        lens = np.array([len(b) for b in frames], np.uint64)
+        npts = C.c_uint64(0)
+        # query the point and slice counts first
+        rc = L.lib().pvvc_decode_frames_host(self.h, nf, ptrs, _p(lens, L.u64p), None, None, 0, C.byref(npts), None, 0,
+                                             stream)
+        if rc not in (0, 11):
+            raise L.PvvcError(rc, "pvvc_decode_frames_host")
+        from .frame import parse_frame
+        nsl = sum(parse_frame(b).n for b in frames)
+        P = int(npts.value)
+        xyz = np.zeros((max(P, 1), 3), np.float32)
+        rgb = np.zeros((max(P, 1), 3), np.uint8)
+        st = np.zeros(max(nsl, 1), np.int32)
+        L.check(L.lib().pvvc_decode_frames_host(self.h, nf, ptrs, _p(lens, L.u64p), _p(xyz, L.f32p), _p(rgb, L.u8p), P,
+                                                C.byref(npts), _p(st, L.i32p), nsl, stream), "pvvc_decode_frames_host")
+        return xyz[:P], rgb[:P], st[:nsl]
+
+
+class Plan:
+    """A device work queue for one packed Batch (pvvc_plan)."""
+
+    def __init__(self, b: Batch):
+        self.batch = b
+        self._keep = [np.ascontiguousarray(x) for x in (b.slot, b.type, b.size, b.qp, b.mv, b.geo_off, b.geo_size,
+                                                         b.col_off, b.col_size, b.out_off)]
+        k = self._keep
+        d = L.BatchDesc(b.nslices, _p(k[0], L.i32p), _p(k[1], L.u8p), _p(k[2], L.u32p), _p(k[3], L.u8p), _p(k[4], L.f32p),
+                        _p(k[5], L.u64p), _p(k[6], L.u32p), _p(k[7], L.u64p), _p(k[8], L.u32p), _p(k[9], L.u64p))
+        h = L.vp()
+        L.check(L.lib().pvvc_plan_create(C.byref(d), C.byref(h)), "pvvc_plan_create")
+        self.h = h
+        tp = C.c_uint64(0)
+        wb = C.c_uint64(0)
+        L.check(L.lib().pvvc_plan_query(h, C.byref(tp), C.byref(wb)), "pvvc_plan_query")
+        self.total_points = int(tp.value)
+        self.workspace_bytes = int(wb.value)
+
+    def close(self):
+        if self.h:
+            L.lib().pvvc_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def decode(self, dec: Decoder, payload_ptr: int, xyz_ptr: int, rgb_ptr: int, points24_ptr: int, status_ptr: int,
+               workspace_ptr: int, workspace_bytes: int, stream: int = 0) -> None:
+        """pvvc_decode with raw device pointers (0 = not wanted)."""
+        L.check(L.lib().pvvc_decode(self.h, dec.h, payload_ptr, xyz_ptr or None, rgb_ptr or None, points24_ptr or None,
+                                    status_ptr or None, workspace_ptr, workspace_bytes, stream), "pvvc_decode")

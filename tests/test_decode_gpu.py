@@ -1,0 +1,223 @@
+"""GPU decode path (libpvvc_gb300.so on cuda:0) against the oracle and the
+reference's golden outputs.  Geometry must be bit-identical; colours must
+equal the reference's wherever its uint8 cast is defined (see
+conftest.rgb_matches), which makes them bit-identical in practice."""
+import ctypes
+import ctypes.util
+
+import numpy as np
+import pytest
+
+from conftest import golden_expected, golden_frames, rgb_matches
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch():
+    import torch as t
+    assert t.cuda.is_available(), "GPU tests need a CUDA device"
+    return t
+
+
+def _dev(torch, a: np.ndarray):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda")
+
+
+def decode_batch(torch, pvvc, dec, batch, points24=False):
+    """Plan + pvvc_decode through the C ABI with torch-allocated buffers."""
+    plan = pvvc.Plan(batch)
+    P = max(plan.total_points, 1)
+    pay = _dev(torch, batch.payload)
+    xyz = torch.zeros((P, 3), dtype=torch.float32, device="cuda")
+    rgb = torch.zeros((P, 3), dtype=torch.uint8, device="cuda")
+    p24 = torch.zeros((P, 6), dtype=torch.float32, device="cuda") if points24 else None
+    st = torch.full((max(batch.nslices, 1),), -1, dtype=torch.int32, device="cuda")
+    ws = torch.empty(max(plan.workspace_bytes, 256), dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream().cuda_stream
+    plan.decode(dec, pay.data_ptr(), xyz.data_ptr(), rgb.data_ptr(), p24.data_ptr() if points24 else 0, st.data_ptr(),
+                ws.data_ptr(), ws.numel(), stream)
+    torch.cuda.synchronize()
+    out = (xyz.cpu().numpy()[:plan.total_points], rgb.cpu().numpy()[:plan.total_points], st.cpu().numpy()[:batch.nslices])
+    if points24:
+        out = out + (p24.cpu().numpy()[:plan.total_points],)
+    return out
+
+
+def oracle_decode(oracle, pvvc, frames, ndec):
+    decs = [oracle.decoder() for _ in range(ndec)]
+    res = []
+    for b in frames:
+        fr = pvvc.parse_frame(b)
+        xyz, rgb, st = oracle.decode_frame(decs, fr, nthreads=4)
+        # per-slice YUV for the colour rule, in frame order
+        yuv = np.concatenate([decs[int(i)].get_patch()[1] for i in fr.index]) if fr.n else np.zeros((0, 3), np.float32)
+        res.append((xyz, rgb, st, yuv))
+    return res
+
+
+def test_golden_gop_host_api(pvvc_lib, oracle, torch):
+    exp = golden_expected()
+    frames = golden_frames("raw")
+    ref = oracle_decode(oracle, pvvc_lib, frames, 8)
+    dec = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
+    # the whole GoP in one call, then again frame by frame (state persists)
+    xyz, rgb, st = dec.decode_frames(frames)
+    assert (st == 0).all()
+    off = 0
+    for f in range(4):
+        n = exp[f"xyz_{f}"].shape[0]
+        assert np.array_equal(xyz[off:off + n].view(np.uint32), exp[f"xyz_{f}"].view(np.uint32))
+        assert rgb_matches(rgb[off:off + n], exp[f"rgb_{f}"], ref[f][3]).all()
+        off += n
+    for f in range(4):
+        x1, r1, s1 = dec.decode_frames([frames[f]])
+        assert (s1 == 0).all()
+        assert np.array_equal(x1.view(np.uint32), exp[f"xyz_{f}"].view(np.uint32))
+        assert rgb_matches(r1, exp[f"rgb_{f}"], ref[f][3]).all()
+
+
+def test_golden_gop_zstd_payloads(pvvc_lib, oracle, torch):
+    if ctypes.util.find_library("zstd") is None:
+        try:
+            ctypes.CDLL("libzstd.so.1")
+        except OSError:
+            pytest.skip("libzstd is not installed on this host (zstd payloads are inflated on the host)")
+    exp = golden_expected()
+    ref = oracle_decode(oracle, pvvc_lib, golden_frames("raw"), 8)
+    dec = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
+    xyz, rgb, st = dec.decode_frames(golden_frames("zstd"))
+    assert (st == 0).all()
+    off = 0
+    for f in range(4):
+        n = exp[f"xyz_{f}"].shape[0]
+        assert np.array_equal(xyz[off:off + n].view(np.uint32), exp[f"xyz_{f}"].view(np.uint32))
+        assert rgb_matches(rgb[off:off + n], exp[f"rgb_{f}"], ref[f][3]).all()
+        off += n
+
+
+@pytest.mark.parametrize("qp", [4, 8, 16, 32])
+def test_synthetic_gop_device_api_vs_oracle(pvvc_lib, oracle, torch, qp):
+    s = pvvc_lib.Synth(pvvc_lib.config("gof8", qp_i=qp, qp_p=qp, seed=qp))
+    frames = s.frames()
+    parsed = [pvvc_lib.parse_frame(b) for b in frames]
+    batch = pvvc_lib.pack_frames(parsed)
+    dec = pvvc_lib.Decoder(nslots=128, max_leaves=4096)
+    xyz, rgb, st = decode_batch(torch, pvvc_lib, dec, batch)
+    assert (st == 0).all()
+    ref = oracle_decode(oracle, pvvc_lib, frames, 128)
+    for f, (ox, orgb, ost, oyuv) in enumerate(ref):
+        a, b = batch.frame_first_point[f], batch.frame_first_point[f + 1]
+        assert (ost == 0).all()
+        assert np.array_equal(xyz[a:b].view(np.uint32), ox.view(np.uint32)), f
+        assert np.array_equal(rgb[a:b], orgb), f  # oracle colours (clamped) are the product's contract
+
+
+def test_concurrent_gops_in_one_batch(pvvc_lib, torch):
+    s1 = pvvc_lib.Synth(pvvc_lib.config("tiny", seed=1))
+    s2 = pvvc_lib.Synth(pvvc_lib.config("tiny", seed=2))
+    b1 = pvvc_lib.pack_frames([pvvc_lib.parse_frame(b) for b in s1.frames()])
+    b2 = pvvc_lib.pack_frames([pvvc_lib.parse_frame(b) for b in s2.frames()])
+    dec = pvvc_lib.Decoder(nslots=256, max_leaves=4096)
+    x1, r1, t1 = decode_batch(torch, pvvc_lib, dec, b1)
+    x2, r2, t2 = decode_batch(torch, pvvc_lib, dec, b2)
+    both = pvvc_lib.concat_batches([b1, b2], slot_stride=128)
+    x, r, t = decode_batch(torch, pvvc_lib, dec, both)
+    assert (t == 0).all() and (t1 == 0).all() and (t2 == 0).all()
+    assert np.array_equal(x, np.concatenate([x1, x2])) and np.array_equal(r, np.concatenate([r1, r2]))
+
+
+def test_points24_layout_matches_reference_gpu_formula(pvvc_lib, oracle, torch):
+    frames = golden_frames("raw")
+    ref = oracle_decode(oracle, pvvc_lib, frames, 8)
+    batch = pvvc_lib.pack_frames([pvvc_lib.parse_frame(b) for b in frames])
+    dec = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
+    xyz, rgb, st, p24 = decode_batch(torch, pvvc_lib, dec, batch, points24=True)
+    assert (st == 0).all()
+    assert np.array_equal(p24[:, :3], xyz)
+    f = np.float32
+    for fi, (_, _, _, yuv) in enumerate(ref):
+        a, b = batch.frame_first_point[fi], batch.frame_first_point[fi + 1]
+        y, u, v = yuv[:, 0], yuv[:, 1], yuv[:, 2]
+        want = np.stack([(y + f(1.402) * (v - f(128))) / f(255),
+                         ((y - f(0.3441) * (u - f(128))) - f(0.7141) * (v - f(128))) / f(255),
+                         (y + f(1.772) * (u - f(128))) / f(255)], 1).astype(np.float32)
+        # patches under 10 points are painted white (CUDA2OpenGL.cu:54-58)
+        sizes = pvvc_lib.parse_frame(frames[fi]).size
+        small = np.repeat(sizes < 10, sizes.astype(np.int64))
+        want[small] = 1.0
+        assert np.array_equal(p24[a:b, 3:], want)
+
+
+def test_corrupt_and_missing_slices_report_status(pvvc_lib, torch):
+    frames = [pvvc_lib.parse_frame(b) for b in golden_frames("raw")]
+    f0, f1 = frames[0], frames[1]
+    # frame 0: slice 1 colour truncated, slice 2 geometry truncated, slice 3 wrong size, slice 5 invalid type
+    f0.color[1] = f0.color[1][: len(f0.color[1]) // 4]
+    f0.geometry[2] = f0.geometry[2][:30]
+    f0.size = f0.size.copy(); f0.size[3] += 1
+    f0.type = f0.type.copy(); f0.type[5] = 0x00
+    batch = pvvc_lib.pack_frames([f0])
+    dec = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
+    _, _, st = decode_batch(torch, pvvc_lib, dec, batch)
+    assert st[1] == 2 and st[2] == 3 and st[3] == 4 and st[5] == 6
+    assert st[0] == 0 and st[4] == 0 and st[6] == 0 and st[7] == 0
+    # predictive slices of the broken patches now lack a reference; a fresh
+    # state has no reference at all
+    _, _, st1 = decode_batch(torch, pvvc_lib, dec, pvvc_lib.pack_frames([f1]))
+    assert st1[0] == 0 and st1[1] == 5 and st1[2] == 5 and st1[3] == 5 and st1[5] == 5
+    fresh = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
+    _, _, st2 = decode_batch(torch, pvvc_lib, fresh, pvvc_lib.pack_frames([f1]))
+    assert (st2 == 5).all()
+
+
+def test_tree_capacity_is_reported_not_overrun(pvvc_lib, torch):
+    frames = [pvvc_lib.parse_frame(b) for b in golden_frames("raw")]
+    dec = pvvc_lib.Decoder(nslots=16, max_leaves=600, max_nodes=100000)  # patches above 600 points do not fit
+    _, _, st = decode_batch(torch, pvvc_lib, dec, pvvc_lib.pack_frames([frames[0]]))
+    big = frames[0].size > 600
+    assert (st[big] == 12).all() and (st[~big] == 0).all()
+
+
+def test_launch_cudaProcess_signature(pvvc_lib, oracle, torch):
+    """Reference-signature entry point: device arrays of per-slice pointers,
+    24-byte Points output at inner_offset."""
+    frames = [pvvc_lib.parse_frame(b) for b in golden_frames("raw")]
+    dec = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
+    ref_dec = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
+    lib = pvvc_lib.lib()
+    keep = []
+    for fr in frames:
+        n = fr.n
+        geo = [_dev(torch, np.frombuffer(g or b"\0", np.uint8).copy()) for g in fr.geometry]
+        col = [_dev(torch, np.frombuffer(c, np.uint8).copy()) for c in fr.color]
+        mvs = [_dev(torch, fr.mv[i].copy()) for i in range(n)]
+        keep += geo + col + mvs
+        off = np.concatenate([[0], np.cumsum(fr.size.astype(np.int64))[:-1]]).astype(np.int32)
+        d = dict(off=_dev(torch, off), idx=_dev(torch, fr.index), typ=_dev(torch, fr.type), size=_dev(torch, fr.size.astype(np.int32)),
+                 qp=_dev(torch, fr.qp), gsz=_dev(torch, np.array([len(g) for g in fr.geometry], np.int32)),
+                 csz=_dev(torch, np.array([len(c) for c in fr.color], np.int32)),
+                 mvp=_dev(torch, np.array([t.data_ptr() for t in mvs], np.int64)),
+                 gp=_dev(torch, np.array([t.data_ptr() for t in geo], np.int64)),
+                 cp=_dev(torch, np.array([t.data_ptr() for t in col], np.int64)))
+        keep += list(d.values())
+        P = fr.points
+        out = torch.zeros((P, 6), dtype=torch.float32, device="cuda")
+        rc = lib.pvvc_launch_cudaProcess(n, 1, out.data_ptr(), fr.timestamp, d["off"].data_ptr(), d["idx"].data_ptr(),
+                                         d["typ"].data_ptr(), d["mvp"].data_ptr(), d["size"].data_ptr(), d["qp"].data_ptr(),
+                                         d["gp"].data_ptr(), d["gsz"].data_ptr(), d["cp"].data_ptr(), d["csz"].data_ptr(),
+                                         dec.h, n, torch.cuda.current_stream().cuda_stream)
+        assert rc == 0
+        _, _, st, p24 = decode_batch(torch, pvvc_lib, ref_dec, pvvc_lib.pack_frames([fr]), points24=True)
+        assert (st == 0).all()
+        assert np.array_equal(out.cpu().numpy(), p24)
+
+
+def test_decode_is_deterministic(pvvc_lib, torch):
+    s = pvvc_lib.Synth(pvvc_lib.config("tiny", seed=9))
+    batch = pvvc_lib.pack_frames([pvvc_lib.parse_frame(b) for b in s.frames()])
+    dec = pvvc_lib.Decoder(nslots=64, max_leaves=4096)
+    a = decode_batch(torch, pvvc_lib, dec, batch)
+    b = decode_batch(torch, pvvc_lib, dec, batch)
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
