@@ -223,10 +223,11 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
     sp = stream.cuda_stream
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+    for e in ev:
+        e.record(stream)  # torch creates the CUDA event on first record
+    torch.cuda.synchronize()
     import ctypes
     evp = (ctypes.c_void_p * 5)(*[e.cuda_event for e in ev])
-    for e in ev:
-        e.record(stream)  # materialise the events
     lib = pvvc.lib()
 
     def step(profiled=False):

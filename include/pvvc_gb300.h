@@ -155,6 +155,44 @@ int pvvc_encode_patch_gop(const float* xyz, uint32_t n, const float* yuv, int32_
 int64_t pvvc_rlgr_encode(const int64_t* sym, uint64_t n, uint8_t* out, uint64_t cap);
 int pvvc_rlgr_decode_host(const uint8_t* in, uint64_t nbytes, uint64_t nsym, int64_t* out);
 
+/* ---- batched GPU ICP (encoder) -------------------------------------------
+ * Point-to-point ICP of many (source, target) patch pairs in one launch.
+ * Replaces the per-pair registration::ICP::Align (src/registration/icp.cc:21-102,
+ * pcl::IterativeClosestPoint) as called by PatchFitting::AddPatch
+ * (src/patch/patch_fitting.cc:58-79) and PatchesRegistration::Task
+ * (src/registration/patches_registration.cc:80-90).  Device arrays:
+ *   src_xyz/tgt_xyz  float[3*total] points of all pairs, concatenated
+ *   src_off/tgt_off  uint32[npairs+1] point ranges
+ *   init             float[npairs*16] row-major initial transforms (or NULL = I)
+ *   T_out            float[npairs*16] row-major final transforms
+ *   mse_out          float[npairs] final mean squared NN distance (fitness)
+ *   iters_out        int32[npairs], converged_out uint8[npairs] (may be NULL)
+ * Semantics of the PCL criteria the reference configures (icp.cc:56-96):
+ * correspondences beyond max_corr_dist are dropped; fewer than 3 stop the
+ * pair unconverged; the loop ends at max_iter (converged), when the update's
+ * rotation cosine >= 1 - transform_eps and its squared translation <=
+ * transform_eps, or when the correspondence MSE changes by less than
+ * mse_abs_eps absolute or fitness_eps relative.  mse_out is the fitness score of the
+ * final transform (mean squared NN distance of all source points). */
+typedef struct {
+    float max_corr_dist;  /* icp.correspondence_ths */
+    int32_t max_iter;     /* icp.iteration_ths */
+    float fitness_eps;    /* stop when |delta MSE| < fitness_eps (icp.mse_ths) */
+    float transform_eps;  /* stop when the update is below this (icp.transformation_ths) */
+    float mse_abs_eps;    /* stop when |delta MSE| < this (PCL's absolute MSE threshold, 1e-12 by default) */
+} pvvc_icp_params;
+/* device workspace bytes of pvvc_icp_batch / pvvc_cloud_mse_batch */
+int pvvc_icp_workspace_size(int32_t npairs, uint64_t total_src_points, uint64_t total_tgt_points, uint64_t* bytes);
+int pvvc_icp_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
+                   const uint32_t* tgt_off, const float* init, const pvvc_icp_params* params, float* T_out,
+                   float* mse_out, int32_t* iters_out, uint8_t* converged_out, void* workspace,
+                   uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream);
+/* Symmetric NN mean squared distance of each pair after applying T
+ * (ICPBase::CloudMSE, src/registration/registration_base.cc:114-158). */
+int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
+                         const uint32_t* tgt_off, const float* T, float* mse_out, void* workspace,
+                         uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -69,7 +69,8 @@ class _PvoFrame(C.Structure):
 
 
 class _IcpParams(C.Structure):
-    _fields_ = [("max_corr_dist", C.c_float), ("max_iter", C.c_int), ("fitness_eps", C.c_float), ("transform_eps", C.c_float)]
+    _fields_ = [("max_corr_dist", C.c_float), ("max_iter", C.c_int), ("fitness_eps", C.c_float), ("transform_eps", C.c_float),
+                ("mse_abs_eps", C.c_float)]
 
 
 class Oracle:
@@ -205,14 +206,14 @@ class Oracle:
         return xyz[:total], rgb[:total], st[:n]
 
     # ---- ICP ----
-    def icp_align(self, src, tgt, init=None, max_corr_dist=1e6, max_iter=50, fitness_eps=1e-6, transform_eps=1e-6):
+    def icp_align(self, src, tgt, init=None, max_corr_dist=1e6, max_iter=50, fitness_eps=1e-6, transform_eps=1e-6, mse_abs_eps=1e-12):
         src = np.ascontiguousarray(src, np.float32)
         tgt = np.ascontiguousarray(tgt, np.float32)
         T = np.zeros(16, np.float32)
         fit = C.c_float(0)
         it = C.c_int(0)
         conv = C.c_int(0)
-        p = _IcpParams(max_corr_dist, max_iter, fitness_eps, transform_eps)
+        p = _IcpParams(max_corr_dist, max_iter, fitness_eps, transform_eps, mse_abs_eps)
         ini = None if init is None else _ptr(np.ascontiguousarray(init, np.float32).reshape(16), _f32p)
         st = self.lib.pvo_icp_align(_ptr(src, _f32p), src.shape[0], _ptr(tgt, _f32p), tgt.shape[0], ini, C.byref(p), _ptr(T, _f32p), C.byref(fit), C.byref(it), C.byref(conv))
         if st:

@@ -112,6 +112,7 @@ typedef struct {
     int max_iter;            /* icp.iteration_ths */
     float fitness_eps;       /* icp.mse_ths (Euclidean fitness epsilon) */
     float transform_eps;     /* icp.transformation_ths */
+    float mse_abs_eps;       /* absolute MSE change threshold (PCL default 1e-12) */
 } pvo_icp_params;
 
 /* Align src onto tgt starting from init (row-major 4x4, may be NULL = identity).

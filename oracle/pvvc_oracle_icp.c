@@ -1,2 +1,272 @@
-/* placeholder, replaced below */
+/*
+ * pvvc_oracle_icp.c -- CPU restatement of point-to-point ICP as the reference
+ * calls it through pcl::IterativeClosestPoint (src/registration/icp.cc:21-102)
+ * and of ICPBase::CloudMSE (src/registration/registration_base.cc:114-158).
+ *
+ * TEST INFRASTRUCTURE ONLY.  PCL (>= 1.10, not vendored, not installed here)
+ * holds the algorithm; this is written from its documented semantics, not
+ * from its source:
+ *   - correspondences: exact nearest target point of each transformed source
+ *     point, kept if its squared distance <= max_corr_dist^2;
+ *   - fewer than 3 correspondences: not converged, stop;
+ *   - rigid estimate per iteration: centroids, cross-covariance, SVD
+ *     (Kabsch / Umeyama without scale), reflection fixed; composed as
+ *     T = T_inc * T;
+ *   - convergence after each iteration, in order: iteration cap (counts as
+ *     converged); |R_inc| close to I (cos angle >= 1 - transform_eps) and
+ *     |t_inc|^2 <= transform_eps; |mse - mse_prev| < mse_abs_eps (absolute, PCL
+ *     default 1e-12); relative
+ *     |mse - mse_prev| / mse_prev < fitness_eps; mse = mean squared distance
+ *     of the iteration's correspondences, mse_prev starts at DBL_MAX;
+ *   - fitness score: mean squared NN distance of the finally transformed
+ *     source (getFitnessScore with max_range = DBL_MAX).
+ * ICP parity is therefore unpinned against PCL itself.  Computed in double
+ * precision with an exact grid nearest-neighbour search.
+ */
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
 #include "pvvc_oracle.h"
+
+/* ---- exact nearest neighbour on a uniform grid ---- */
+typedef struct {
+    double lo[3], h;
+    int dim[3];
+    int* start; /* cell -> first point (+ sentinel) */
+    float* pts; /* points sorted by cell */
+    size_t n;
+} grid_t;
+
+static int grid_build(grid_t* g, const float* p, size_t n) {
+    double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+    for (size_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            if (p[3 * i + a] < lo[a]) lo[a] = p[3 * i + a];
+            if (p[3 * i + a] > hi[a]) hi[a] = p[3 * i + a];
+        }
+    double ext = 0;
+    for (int a = 0; a < 3; ++a) ext = fmax(ext, hi[a] - lo[a]);
+    g->h = fmax(ext / 24.0, 1.0);
+    for (int a = 0; a < 3; ++a) {
+        g->lo[a] = lo[a];
+        g->dim[a] = (int)floor((hi[a] - lo[a]) / g->h) + 1;
+    }
+    size_t nc = (size_t)g->dim[0] * g->dim[1] * g->dim[2];
+    g->start = (int*)calloc(nc + 1, sizeof(int));
+    g->pts = (float*)malloc(3 * n * sizeof(float) + 4);
+    int* cell = (int*)malloc(n * sizeof(int) + 4);
+    if (!g->start || !g->pts || !cell) { free(cell); return PVO_ERR_NOMEM; }
+    for (size_t i = 0; i < n; ++i) {
+        int c[3];
+        for (int a = 0; a < 3; ++a) {
+            c[a] = (int)floor((p[3 * i + a] - g->lo[a]) / g->h);
+            if (c[a] >= g->dim[a]) c[a] = g->dim[a] - 1;
+        }
+        cell[i] = (c[2] * g->dim[1] + c[1]) * g->dim[0] + c[0];
+        g->start[cell[i] + 1]++;
+    }
+    for (size_t c = 0; c < nc; ++c) g->start[c + 1] += g->start[c];
+    int* fill = (int*)malloc((nc + 1) * sizeof(int));
+    memcpy(fill, g->start, (nc + 1) * sizeof(int));
+    for (size_t i = 0; i < n; ++i) memcpy(g->pts + 3 * fill[cell[i]]++, p + 3 * i, 3 * sizeof(float));
+    free(fill);
+    free(cell);
+    g->n = n;
+    return PVO_OK;
+}
+
+static void grid_free(grid_t* g) {
+    free(g->start);
+    free(g->pts);
+}
+
+/* squared distance to the nearest point, exact: rings of cells in growing
+ * Chebyshev radius until the ring cannot hold anything closer */
+static double grid_nn(const grid_t* g, const double q[3], int* idx) {
+    /* rings of cells around the query's cell clamped into the grid; a point in
+     * ring r lies at least (r-1)*h from the query (also for queries outside) */
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+        double t = floor((q[a] - g->lo[a]) / g->h);
+        if (t < 0) t = 0;
+        if (t > g->dim[a] - 1) t = g->dim[a] - 1;
+        c[a] = (int)t;
+    }
+    double best = DBL_MAX;
+    int bi = -1;
+    int maxr = g->dim[0];
+    if (g->dim[1] > maxr) maxr = g->dim[1];
+    if (g->dim[2] > maxr) maxr = g->dim[2];
+    for (int r = 0; r <= maxr; ++r) {
+        if (r > 0 && bi >= 0) {
+            double lb = (r - 1) * g->h;
+            if (lb * lb > best) break;
+        }
+        for (int z = c[2] - r; z <= c[2] + r; ++z) {
+            if (z < 0 || z >= g->dim[2]) continue;
+            for (int y = c[1] - r; y <= c[1] + r; ++y) {
+                if (y < 0 || y >= g->dim[1]) continue;
+                for (int x = c[0] - r; x <= c[0] + r; ++x) {
+                    if (x < 0 || x >= g->dim[0]) continue;
+                    if (abs(x - c[0]) != r && abs(y - c[1]) != r && abs(z - c[2]) != r) continue;
+                    int cc = (z * g->dim[1] + y) * g->dim[0] + x;
+                    for (int k = g->start[cc]; k < g->start[cc + 1]; ++k) {
+                        double dx = g->pts[3 * k] - q[0], dy = g->pts[3 * k + 1] - q[1], dz = g->pts[3 * k + 2] - q[2];
+                        double d = dx * dx + dy * dy + dz * dz;
+                        if (d < best) { best = d; bi = k; }
+                    }
+                }
+            }
+        }
+    }
+    if (idx) *idx = bi;
+    return best;
+}
+
+/* ---- 3x3 SVD by one-sided Jacobi (double) ---- */
+static void svd3(const double A[9], double U[9], double S[3], double V[9]) {
+    double B[9];
+    memcpy(B, A, sizeof(B));
+    for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        double off = 0;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                double a = 0, b = 0, c = 0;
+                for (int i = 0; i < 3; ++i) {
+                    a += B[3 * i + p] * B[3 * i + p];
+                    b += B[3 * i + q] * B[3 * i + q];
+                    c += B[3 * i + p] * B[3 * i + q];
+                }
+                off += c * c;
+                if (fabs(c) < 1e-300) continue;
+                double zeta = (b - a) / (2 * c);
+                double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+                double cs = 1 / sqrt(1 + t * t), sn = cs * t;
+                for (int i = 0; i < 3; ++i) {
+                    double bp = B[3 * i + p], bq = B[3 * i + q];
+                    B[3 * i + p] = cs * bp - sn * bq;
+                    B[3 * i + q] = sn * bp + cs * bq;
+                    double vp = V[3 * i + p], vq = V[3 * i + q];
+                    V[3 * i + p] = cs * vp - sn * vq;
+                    V[3 * i + q] = sn * vp + cs * vq;
+                }
+            }
+        if (off < 1e-30) break;
+    }
+    for (int j = 0; j < 3; ++j) {
+        double s = sqrt(B[j] * B[j] + B[3 + j] * B[3 + j] + B[6 + j] * B[6 + j]);
+        S[j] = s;
+        for (int i = 0; i < 3; ++i) U[3 * i + j] = s > 1e-300 ? B[3 * i + j] / s : (i == j ? 1.0 : 0.0);
+    }
+}
+
+static double det3(const double M[9]) {
+    return M[0] * (M[4] * M[8] - M[5] * M[7]) - M[1] * (M[3] * M[8] - M[5] * M[6]) + M[2] * (M[3] * M[7] - M[4] * M[6]);
+}
+
+/* rigid transform (R,t) minimising sum |R p + t - q|^2 from the sums */
+static void kabsch(double n, const double sp[3], const double sq[3], const double spq[9], double R[9], double t[3]) {
+    double cp[3], cq[3], H[9];
+    for (int a = 0; a < 3; ++a) { cp[a] = sp[a] / n; cq[a] = sq[a] / n; }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) H[3 * i + j] = spq[3 * i + j] - n * cp[i] * cq[j];
+    double U[9], S[3], V[9];
+    svd3(H, U, S, V);
+    /* R = V U^T */
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) R[3 * i + j] = V[3 * i] * U[3 * j] + V[3 * i + 1] * U[3 * j + 1] + V[3 * i + 2] * U[3 * j + 2];
+    if (det3(R) < 0) {
+        /* flip the axis of the smallest singular value */
+        int k = 0;
+        for (int j = 1; j < 3; ++j) if (S[j] < S[k]) k = j;
+        for (int i = 0; i < 3; ++i) V[3 * i + k] = -V[3 * i + k];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) R[3 * i + j] = V[3 * i] * U[3 * j] + V[3 * i + 1] * U[3 * j + 1] + V[3 * i + 2] * U[3 * j + 2];
+    }
+    for (int i = 0; i < 3; ++i) t[i] = cq[i] - (R[3 * i] * cp[0] + R[3 * i + 1] * cp[1] + R[3 * i + 2] * cp[2]);
+}
+
+int pvo_icp_align(const float* src, size_t ns, const float* tgt, size_t nt, const float* init, const pvo_icp_params* p,
+                  float* T_out, float* fitness, int* iters, int* converged) {
+    if (!src || !tgt || !ns || !nt || !p || !T_out) return PVO_ERR_ARG;
+    grid_t g;
+    if (grid_build(&g, tgt, nt)) return PVO_ERR_NOMEM;
+    double T[16];
+    for (int i = 0; i < 16; ++i) T[i] = init ? init[i] : ((i % 5 == 0) ? 1.0 : 0.0);
+    const double corr2 = (double)p->max_corr_dist * (double)p->max_corr_dist;
+    double prev_mse = DBL_MAX;
+    int it = 0, conv = 0;
+    for (;;) {
+        double sp[3] = {0, 0, 0}, sq[3] = {0, 0, 0}, spq[9] = {0}, sd = 0, cnt = 0;
+        for (size_t i = 0; i < ns; ++i) {
+            double x = src[3 * i], y = src[3 * i + 1], z = src[3 * i + 2], q[3];
+            for (int r = 0; r < 3; ++r) q[r] = T[4 * r] * x + T[4 * r + 1] * y + T[4 * r + 2] * z + T[4 * r + 3];
+            int k;
+            double d = grid_nn(&g, q, &k);
+            if (k < 0 || d > corr2) continue;
+            const float* m = g.pts + 3 * k;
+            for (int a = 0; a < 3; ++a) { sp[a] += q[a]; sq[a] += m[a]; }
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) spq[3 * a + b] += q[a] * m[b];
+            sd += d;
+            cnt += 1;
+        }
+        if (cnt < 3) { conv = 0; break; }
+        double R[9], t[3];
+        kabsch(cnt, sp, sq, spq, R, t);
+        double Tn[16];
+        for (int i = 0; i < 3; ++i) {
+            for (int j = 0; j < 4; ++j) Tn[4 * i + j] = R[3 * i] * T[j] + R[3 * i + 1] * T[4 + j] + R[3 * i + 2] * T[8 + j] + (j == 3 ? t[i] : 0.0);
+        }
+        for (int j = 0; j < 4; ++j) Tn[12 + j] = T[12 + j];
+        memcpy(T, Tn, sizeof(T));
+        ++it;
+        /* convergence (DefaultConvergenceCriteria semantics) */
+        if (it >= p->max_iter) { conv = 1; break; }
+        double cosang = 0.5 * (R[0] + R[4] + R[8] - 1.0);
+        double tr2 = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+        if (cosang >= 1.0 - (double)p->transform_eps && tr2 <= (double)p->transform_eps) { conv = 1; break; }
+        double mse = sd / cnt;
+        if (fabs(mse - prev_mse) < (double)p->mse_abs_eps) { conv = 1; break; }
+        if (fabs(mse - prev_mse) / prev_mse < (double)p->fitness_eps) { conv = 1; break; }
+        prev_mse = mse;
+    }
+    /* fitness score of the final transform */
+    double fs = 0;
+    for (size_t i = 0; i < ns; ++i) {
+        double x = src[3 * i], y = src[3 * i + 1], z = src[3 * i + 2], q[3];
+        for (int r = 0; r < 3; ++r) q[r] = T[4 * r] * x + T[4 * r + 1] * y + T[4 * r + 2] * z + T[4 * r + 3];
+        fs += grid_nn(&g, q, NULL);
+    }
+    grid_free(&g);
+    for (int i = 0; i < 16; ++i) T_out[i] = (float)T[i];
+    if (fitness) *fitness = (float)(fs / (double)ns);
+    if (iters) *iters = it;
+    if (converged) *converged = conv;
+    return PVO_OK;
+}
+
+/* ICPBase::CloudMSE (registration_base.cc:114-158) */
+float pvo_cloud_mse(const float* a, size_t na, const float* b, size_t nb) {
+    if (!a || !b || !na || !nb) return -1.0f;
+    grid_t ga, gb;
+    if (grid_build(&gb, b, nb)) return -1.0f;
+    if (grid_build(&ga, a, na)) { grid_free(&gb); return -1.0f; }
+    double m1 = 0, m2 = 0;
+    for (size_t i = 0; i < na; ++i) {
+        double q[3] = {a[3 * i], a[3 * i + 1], a[3 * i + 2]};
+        m1 += grid_nn(&gb, q, NULL);
+    }
+    for (size_t i = 0; i < nb; ++i) {
+        double q[3] = {b[3 * i], b[3 * i + 1], b[3 * i + 2]};
+        m2 += grid_nn(&ga, q, NULL);
+    }
+    grid_free(&ga);
+    grid_free(&gb);
+    m1 /= (double)na;
+    m2 /= (double)nb;
+    return (float)(m1 > m2 ? m1 : m2);
+}

@@ -1,0 +1,533 @@
+// icp_kernels.cu -- batched point-to-point ICP for the encoder (sm_103a).
+//
+// Replaces registration::ICP::Align (src/registration/icp.cc:21-102, which
+// wraps pcl::IterativeClosestPoint) for many patch pairs at once, and
+// ICPBase::CloudMSE (src/registration/registration_base.cc:114-158).
+//
+//   k_grid   one CTA per pair: a uniform grid over the target points
+//            (at most 16 cells per axis): bounding box by block reduction,
+//            counting sort of the points into cells (shared-memory
+//            histogram + block scan), written to the workspace.
+//   k_icp    one CTA per pair, all iterations: each thread transforms its
+//            source points, finds the exact nearest target point by rings of
+//            grid cells (FP32), and accumulates the correspondence sums with
+//            Kahan-compensated FP32 additions; the block reduces them in FP64
+//            and one thread solves the 3x3 Kabsch problem by a Jacobi SVD in
+//            FP64 and applies the convergence tests of the PCL criteria.
+//   k_nn_mean  mean squared NN distance of (transformed) query points to a
+//            gridded cloud, per pair.
+#include <cuda_runtime.h>
+
+#include <cfloat>
+#include <cstdint>
+
+#include "pvvc_gb300.h"
+
+namespace pvvc {
+
+constexpr int kGridAxis = 16;
+constexpr int kCells = kGridAxis * kGridAxis * kGridAxis;
+
+struct GridHdr {  // per pair
+    float lo[3];
+    float h;
+    int dim[3];
+    int pad;
+};
+
+// ---------------------------------------------------------------------------
+template <int T>
+__global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const uint32_t* __restrict__ off,
+                                            const float* __restrict__ xform, GridHdr* __restrict__ hdr,
+                                            int* __restrict__ cstart, float* __restrict__ sorted) {
+    __shared__ int s_cnt[kCells + 1];
+    __shared__ float s_red[T / 32][6];
+    __shared__ float s_box[6];
+    __shared__ int s_warp[T / 32];
+    const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t a = off[pair], b = off[pair + 1], n = b - a;
+    float M[12];
+    const bool tr = xform != nullptr;
+    if (tr)
+        for (int i = 0; i < 12; ++i) M[i] = xform[pair * 16 + i];
+    auto load = [&](uint32_t i, float* p) {
+        const float x = pts[3ull * i], y = pts[3ull * i + 1], z = pts[3ull * i + 2];
+        if (!tr) {
+            p[0] = x; p[1] = y; p[2] = z;
+        } else {
+            for (int r = 0; r < 3; ++r) p[r] = M[4 * r] * x + M[4 * r + 1] * y + M[4 * r + 2] * z + M[4 * r + 3];
+        }
+    };
+    // bounding box
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (uint32_t i = a + tid; i < b; i += T) {
+        float p[3];
+        load(i, p);
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = fminf(mn[k], p[k]);
+            mx[k] = fmaxf(mx[k], p[k]);
+        }
+    }
+    for (int o = 16; o; o >>= 1)
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], o));
+            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], o));
+        }
+    if (lane == 0)
+        for (int k = 0; k < 3; ++k) {
+            s_red[wid][k] = mn[k];
+            s_red[wid][3 + k] = mx[k];
+        }
+    for (int c = tid; c <= kCells; c += T) s_cnt[c] = 0;
+    __syncthreads();
+    if (tid == 0) {
+        for (int w = 1; w < T / 32; ++w)
+            for (int k = 0; k < 3; ++k) {
+                s_red[0][k] = fminf(s_red[0][k], s_red[w][k]);
+                s_red[0][3 + k] = fmaxf(s_red[0][3 + k], s_red[w][3 + k]);
+            }
+        float ext = 0.f;
+        for (int k = 0; k < 3; ++k) ext = fmaxf(ext, s_red[0][3 + k] - s_red[0][k]);
+        GridHdr g;
+        g.h = fmaxf(ext / (float)kGridAxis * 1.0001f, 1.0f);
+        for (int k = 0; k < 3; ++k) {
+            g.lo[k] = n ? s_red[0][k] : 0.f;
+            g.dim[k] = n ? min((int)floorf((s_red[0][3 + k] - s_red[0][k]) / g.h) + 1, kGridAxis) : 1;
+            s_box[k] = g.lo[k];
+        }
+        s_box[3] = g.h;
+        s_box[4] = __int_as_float(g.dim[0]);
+        s_box[5] = __int_as_float(g.dim[1] * 1024 + g.dim[2]);
+        g.pad = 0;
+        hdr[pair] = g;
+    }
+    __syncthreads();
+    const float lo0 = s_box[0], lo1 = s_box[1], lo2 = s_box[2], h = s_box[3];
+    const int d0 = __float_as_int(s_box[4]), d12 = __float_as_int(s_box[5]), d1 = d12 / 1024, d2 = d12 % 1024;
+    auto cell_of = [&](const float* p) {
+        int cx = min(max((int)floorf((p[0] - lo0) / h), 0), d0 - 1);
+        int cy = min(max((int)floorf((p[1] - lo1) / h), 0), d1 - 1);
+        int cz = min(max((int)floorf((p[2] - lo2) / h), 0), d2 - 1);
+        return (cz * d1 + cy) * d0 + cx;
+    };
+    for (uint32_t i = a + tid; i < b; i += T) {
+        float p[3];
+        load(i, p);
+        atomicAdd(&s_cnt[cell_of(p) + 1], 1);
+    }
+    __syncthreads();
+    // exclusive scan of kCells+1 counters (serial per warp chunk, then warp offsets)
+    const int per = (kCells + 1 + T - 1) / T;
+    int loc = 0;
+    for (int k = 0; k < per; ++k) {
+        const int c = tid * per + k;
+        if (c <= kCells) loc += s_cnt[c];
+    }
+    int x = loc;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    if (tid == 0)
+        for (int w = 1; w < T / 32; ++w) s_warp[w] += s_warp[w - 1];
+    __syncthreads();
+    int run = (wid ? s_warp[wid - 1] : 0) + x - loc;
+    for (int k = 0; k < per; ++k) {
+        const int c = tid * per + k;
+        if (c <= kCells) {
+            run += s_cnt[c];
+            s_cnt[c] = run;  // inclusive prefix of counts[0..c] == start of cell c (counts shifted by one)
+        }
+    }
+    __syncthreads();
+    int* cs = cstart + (size_t)pair * (kCells + 1);
+    for (int c = tid; c <= kCells; c += T) cs[c] = s_cnt[c];
+    __syncthreads();
+    for (uint32_t i = a + tid; i < b; i += T) {
+        float p[3];
+        load(i, p);
+        const int slot = atomicAdd(&s_cnt[cell_of(p)], 1);
+        float* d = sorted + 3ull * (a + slot);
+        d[0] = p[0];
+        d[1] = p[1];
+        d[2] = p[2];
+    }
+}
+
+// exact nearest neighbour: squared distance (and the point) of the closest
+// gridded point to q, searching rings of cells around q's cell clamped into
+// the grid; a point in ring r lies at least (r-1)*h from q
+__device__ __forceinline__ float grid_nn(const GridHdr& g, const int* __restrict__ cs, const float* __restrict__ sp, uint32_t base,
+                                         float qx, float qy, float qz, float* nx, float* ny, float* nz) {
+    const int cx = min(max((int)floorf((qx - g.lo[0]) / g.h), 0), g.dim[0] - 1);
+    const int cy = min(max((int)floorf((qy - g.lo[1]) / g.h), 0), g.dim[1] - 1);
+    const int cz = min(max((int)floorf((qz - g.lo[2]) / g.h), 0), g.dim[2] - 1);
+    float best = FLT_MAX;
+    float bx = 0.f, by = 0.f, bz = 0.f;
+    const int maxr = max(g.dim[0], max(g.dim[1], g.dim[2]));
+    for (int r = 0; r <= maxr; ++r) {
+        if (r > 0 && best < FLT_MAX) {
+            const float lb = (float)(r - 1) * g.h;
+            if (lb * lb > best) break;
+        }
+        for (int z = max(cz - r, 0); z <= min(cz + r, g.dim[2] - 1); ++z) {
+            const bool zr = (z == cz - r) || (z == cz + r);
+            for (int y = max(cy - r, 0); y <= min(cy + r, g.dim[1] - 1); ++y) {
+                const bool yr = zr || (y == cy - r) || (y == cy + r);
+                // on interior rows only the two x faces belong to the ring
+                int x = max(cx - r, 0);
+                const int xe = min(cx + r, g.dim[0] - 1);
+                const int step = yr ? 1 : max(2 * r, 1);
+                if (!yr && x != cx - r) x = (cx + r <= xe) ? cx + r : xe + 1;
+                for (; x <= xe; x += step) {
+                    const int c = (z * g.dim[1] + y) * g.dim[0] + x;
+                    const int e = __ldg(cs + c + 1);
+                    for (int k = __ldg(cs + c); k < e; ++k) {
+                        const float* p = sp + 3ull * (base + k);
+                        const float px = __ldg(p), py = __ldg(p + 1), pz = __ldg(p + 2);
+                        const float dx = px - qx, dy = py - qy, dz = pz - qz;
+                        const float d = dx * dx + dy * dy + dz * dz;
+                        if (d < best) {
+                            best = d;
+                            bx = px;
+                            by = py;
+                            bz = pz;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    *nx = bx;
+    *ny = by;
+    *nz = bz;
+    return best;
+}
+
+// ---- FP64 3x3 Kabsch (one-sided Jacobi SVD) ---------------------------------
+__device__ void svd3(const double* A, double* U, double* S, double* V) {
+    double B[9];
+    for (int i = 0; i < 9; ++i) {
+        B[i] = A[i];
+        V[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    }
+    for (int sweep = 0; sweep < 40; ++sweep) {
+        double off = 0;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                double a = 0, b = 0, c = 0;
+                for (int i = 0; i < 3; ++i) {
+                    a += B[3 * i + p] * B[3 * i + p];
+                    b += B[3 * i + q] * B[3 * i + q];
+                    c += B[3 * i + p] * B[3 * i + q];
+                }
+                off += c * c;
+                if (fabs(c) < 1e-300) continue;
+                const double zeta = (b - a) / (2 * c);
+                const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1 + zeta * zeta));
+                const double cs = 1 / sqrt(1 + t * t), sn = cs * t;
+                for (int i = 0; i < 3; ++i) {
+                    const double bp = B[3 * i + p], bq = B[3 * i + q];
+                    B[3 * i + p] = cs * bp - sn * bq;
+                    B[3 * i + q] = sn * bp + cs * bq;
+                    const double vp = V[3 * i + p], vq = V[3 * i + q];
+                    V[3 * i + p] = cs * vp - sn * vq;
+                    V[3 * i + q] = sn * vp + cs * vq;
+                }
+            }
+        if (off < 1e-30) break;
+    }
+    for (int j = 0; j < 3; ++j) {
+        const double s = sqrt(B[j] * B[j] + B[3 + j] * B[3 + j] + B[6 + j] * B[6 + j]);
+        S[j] = s;
+        for (int i = 0; i < 3; ++i) U[3 * i + j] = s > 1e-300 ? B[3 * i + j] / s : (i == j ? 1.0 : 0.0);
+    }
+}
+
+__device__ void kabsch(double n, const double* sp, const double* sq, const double* spq, double* R, double* t) {
+    double cp[3], cq[3], H[9], U[9], S[3], V[9];
+    for (int a = 0; a < 3; ++a) {
+        cp[a] = sp[a] / n;
+        cq[a] = sq[a] / n;
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) H[3 * i + j] = spq[3 * i + j] - n * cp[i] * cq[j];
+    svd3(H, U, S, V);
+    auto vut = [&]() {
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) R[3 * i + j] = V[3 * i] * U[3 * j] + V[3 * i + 1] * U[3 * j + 1] + V[3 * i + 2] * U[3 * j + 2];
+    };
+    vut();
+    const double det = R[0] * (R[4] * R[8] - R[5] * R[7]) - R[1] * (R[3] * R[8] - R[5] * R[6]) + R[2] * (R[3] * R[7] - R[4] * R[6]);
+    if (det < 0) {
+        int k = 0;
+        for (int j = 1; j < 3; ++j)
+            if (S[j] < S[k]) k = j;
+        for (int i = 0; i < 3; ++i) V[3 * i + k] = -V[3 * i + k];
+        vut();
+    }
+    for (int i = 0; i < 3; ++i) t[i] = cq[i] - (R[3 * i] * cp[0] + R[3 * i + 1] * cp[1] + R[3 * i + 2] * cp[2]);
+}
+
+// Kahan-compensated FP32 accumulator
+struct KSum {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+constexpr int kIcpThreads = 256;
+constexpr int kNSum = 17;  // count, sum p (3), sum q (3), sum p q^T (9), sum d^2
+
+__global__ void __launch_bounds__(kIcpThreads) k_icp(const float* __restrict__ src, const uint32_t* __restrict__ soff,
+                                                     const uint32_t* __restrict__ toff, const GridHdr* __restrict__ hdr,
+                                                     const int* __restrict__ cstart, const float* __restrict__ tsorted,
+                                                     const float* __restrict__ init, pvvc_icp_params prm,
+                                                     float* __restrict__ T_out, float* __restrict__ mse_out,
+                                                     int32_t* __restrict__ iters_out, uint8_t* __restrict__ conv_out) {
+    __shared__ double s_part[kIcpThreads / 32][kNSum];
+    __shared__ double s_T[16];
+    __shared__ float s_Tf[12];
+    __shared__ int s_done;
+    __shared__ double s_prev;
+    const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t a = soff[pair], b = soff[pair + 1];
+    const GridHdr g = hdr[pair];
+    const int* cs = cstart + (size_t)pair * (kCells + 1);
+    const uint32_t tb = toff[pair];
+    const bool empty_t = toff[pair + 1] == tb;
+    if (tid == 0) {
+        for (int i = 0; i < 16; ++i) s_T[i] = init ? (double)init[pair * 16 + i] : ((i % 5 == 0) ? 1.0 : 0.0);
+        s_done = 0;
+        s_prev = DBL_MAX;
+    }
+    __syncthreads();
+    const double corr2 = (double)prm.max_corr_dist * (double)prm.max_corr_dist;
+    int it = 0, conv = 0;
+    while (true) {
+        if (tid < 12) s_Tf[tid] = (float)s_T[tid];
+        __syncthreads();
+        KSum acc[kNSum];
+        for (uint32_t i = a + tid; i < b && !empty_t; i += kIcpThreads) {
+            const float x = __ldg(src + 3ull * i), y = __ldg(src + 3ull * i + 1), z = __ldg(src + 3ull * i + 2);
+            const float qx = s_Tf[0] * x + s_Tf[1] * y + s_Tf[2] * z + s_Tf[3];
+            const float qy = s_Tf[4] * x + s_Tf[5] * y + s_Tf[6] * z + s_Tf[7];
+            const float qz = s_Tf[8] * x + s_Tf[9] * y + s_Tf[10] * z + s_Tf[11];
+            float mx, my, mz;
+            const float d = grid_nn(g, cs, tsorted, tb, qx, qy, qz, &mx, &my, &mz);
+            if ((double)d > corr2) continue;
+            acc[0].add(1.f);
+            acc[1].add(qx);
+            acc[2].add(qy);
+            acc[3].add(qz);
+            acc[4].add(mx);
+            acc[5].add(my);
+            acc[6].add(mz);
+            acc[7].add(qx * mx);
+            acc[8].add(qx * my);
+            acc[9].add(qx * mz);
+            acc[10].add(qy * mx);
+            acc[11].add(qy * my);
+            acc[12].add(qy * mz);
+            acc[13].add(qz * mx);
+            acc[14].add(qz * my);
+            acc[15].add(qz * mz);
+            acc[16].add(d);
+        }
+        // block reduction in FP64
+#pragma unroll
+        for (int k = 0; k < kNSum; ++k) {
+            double v = acc[k].value();
+            for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0) s_part[wid][k] = v;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double sum[kNSum];
+            for (int k = 0; k < kNSum; ++k) {
+                sum[k] = 0;
+                for (int w = 0; w < kIcpThreads / 32; ++w) sum[k] += s_part[w][k];
+            }
+            const double cnt = sum[0];
+            if (cnt < 3) {
+                s_done = 2;  // too few correspondences: not converged
+            } else {
+                double R[9], t[3];
+                kabsch(cnt, sum + 1, sum + 4, sum + 7, R, t);
+                double Tn[16];
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 4; ++j)
+                        Tn[4 * i + j] = R[3 * i] * s_T[j] + R[3 * i + 1] * s_T[4 + j] + R[3 * i + 2] * s_T[8 + j] + (j == 3 ? t[i] : 0.0);
+                for (int j = 0; j < 4; ++j) Tn[12 + j] = s_T[12 + j];
+                for (int i = 0; i < 16; ++i) s_T[i] = Tn[i];
+                ++it;
+                const double cosang = 0.5 * (R[0] + R[4] + R[8] - 1.0);
+                const double tr2 = t[0] * t[0] + t[1] * t[1] + t[2] * t[2];
+                const double mse = sum[16] / cnt;
+                if (it >= prm.max_iter) s_done = 1;
+                else if (cosang >= 1.0 - (double)prm.transform_eps && tr2 <= (double)prm.transform_eps) s_done = 1;
+                else if (fabs(mse - s_prev) < (double)prm.mse_abs_eps) s_done = 1;
+                else if (fabs(mse - s_prev) / s_prev < (double)prm.fitness_eps) s_done = 1;
+                s_prev = mse;
+            }
+        }
+        __syncthreads();
+        const int done = s_done;
+        if (done) {
+            conv = done == 1;
+            break;
+        }
+        __syncthreads();
+    }
+    // fitness score of the final transform (getFitnessScore)
+    if (tid < 12) s_Tf[tid] = (float)s_T[tid];
+    __syncthreads();
+    KSum fs;
+    for (uint32_t i = a + tid; i < b && !empty_t; i += kIcpThreads) {
+        const float x = __ldg(src + 3ull * i), y = __ldg(src + 3ull * i + 1), z = __ldg(src + 3ull * i + 2);
+        const float qx = s_Tf[0] * x + s_Tf[1] * y + s_Tf[2] * z + s_Tf[3];
+        const float qy = s_Tf[4] * x + s_Tf[5] * y + s_Tf[6] * z + s_Tf[7];
+        const float qz = s_Tf[8] * x + s_Tf[9] * y + s_Tf[10] * z + s_Tf[11];
+        float mx, my, mz;
+        fs.add(grid_nn(g, cs, tsorted, tb, qx, qy, qz, &mx, &my, &mz));
+    }
+    double v = fs.value();
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_part[wid][0] = v;
+    __syncthreads();
+    if (tid == 0) {
+        double tot = 0;
+        for (int w = 0; w < kIcpThreads / 32; ++w) tot += s_part[w][0];
+        for (int i = 0; i < 16; ++i) T_out[pair * 16 + i] = (float)s_T[i];
+        if (mse_out) mse_out[pair] = (b > a && !empty_t) ? (float)(tot / (double)(b - a)) : -1.0f;
+        if (iters_out) iters_out[pair] = it;
+        if (conv_out) conv_out[pair] = (uint8_t)(conv && !empty_t);
+    }
+}
+
+// mean squared NN distance of each pair's (transformed) queries to its grid
+__global__ void __launch_bounds__(kIcpThreads) k_nn_mean(const float* __restrict__ q, const uint32_t* __restrict__ qoff,
+                                                         const float* __restrict__ xform, const uint32_t* __restrict__ goff,
+                                                         const GridHdr* __restrict__ hdr, const int* __restrict__ cstart,
+                                                         const float* __restrict__ sorted, float* __restrict__ out) {
+    __shared__ double s_part[kIcpThreads / 32];
+    const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const uint32_t a = qoff[pair], b = qoff[pair + 1];
+    const GridHdr g = hdr[pair];
+    const int* cs = cstart + (size_t)pair * (kCells + 1);
+    const uint32_t gb = goff[pair];
+    const bool empty = goff[pair + 1] == gb;
+    float M[12];
+    for (int i = 0; i < 12; ++i) M[i] = xform ? xform[pair * 16 + i] : ((i % 5 == 0) ? 1.f : 0.f);
+    KSum acc;
+    for (uint32_t i = a + tid; i < b && !empty; i += kIcpThreads) {
+        const float x = q[3ull * i], y = q[3ull * i + 1], z = q[3ull * i + 2];
+        const float qx = M[0] * x + M[1] * y + M[2] * z + M[3];
+        const float qy = M[4] * x + M[5] * y + M[6] * z + M[7];
+        const float qz = M[8] * x + M[9] * y + M[10] * z + M[11];
+        float mx, my, mz;
+        acc.add(grid_nn(g, cs, sorted, gb, qx, qy, qz, &mx, &my, &mz));
+    }
+    double v = acc.value();
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_part[wid] = v;
+    __syncthreads();
+    if (tid == 0) {
+        double tot = 0;
+        for (int w = 0; w < kIcpThreads / 32; ++w) tot += s_part[w];
+        out[pair] = (b > a && !empty) ? (float)(tot / (double)(b - a)) : -1.0f;
+    }
+}
+
+__global__ void k_max2(const float* __restrict__ a, int n, float* __restrict__ o) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) o[i] = fmaxf(a[i], a[i + n]);
+}
+
+}  // namespace pvvc
+
+using namespace pvvc;
+
+namespace {
+inline uint64_t al(uint64_t v) { return (v + 255) / 256 * 256; }
+struct IcpWs {
+    GridHdr* hdr;
+    int* cstart;
+    float* sorted;
+    GridHdr* hdr2;
+    int* cstart2;
+    float* sorted2;
+    float* tmp;
+};
+uint64_t ws_bytes(int32_t npairs, uint64_t nsrc, uint64_t ntgt, IcpWs* w, void* base) {
+    uint64_t o = 0;
+    auto take = [&](uint64_t b) {
+        uint64_t r = o;
+        o = al(o + b);
+        return r;
+    };
+    const uint64_t h = take(sizeof(GridHdr) * npairs), c = take(4ull * (kCells + 1) * npairs), s = take(12ull * ntgt);
+    const uint64_t h2 = take(sizeof(GridHdr) * npairs), c2 = take(4ull * (kCells + 1) * npairs), s2 = take(12ull * nsrc);
+    const uint64_t t = take(8ull * npairs);
+    if (w && base) {
+        uint8_t* p = static_cast<uint8_t*>(base);
+        w->hdr = reinterpret_cast<GridHdr*>(p + h);
+        w->cstart = reinterpret_cast<int*>(p + c);
+        w->sorted = reinterpret_cast<float*>(p + s);
+        w->hdr2 = reinterpret_cast<GridHdr*>(p + h2);
+        w->cstart2 = reinterpret_cast<int*>(p + c2);
+        w->sorted2 = reinterpret_cast<float*>(p + s2);
+        w->tmp = reinterpret_cast<float*>(p + t);
+    }
+    return o;
+}
+}  // namespace
+
+extern "C" int pvvc_icp_workspace_size(int32_t npairs, uint64_t total_src_points, uint64_t total_tgt_points, uint64_t* bytes) {
+    if (npairs < 0 || !bytes) return PVVC_ERR_ARG;
+    *bytes = ws_bytes(npairs, total_src_points, total_tgt_points, nullptr, nullptr);
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_icp_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
+                              const uint32_t* tgt_off, const float* init, const pvvc_icp_params* params, float* T_out,
+                              float* mse_out, int32_t* iters_out, uint8_t* converged_out, void* workspace,
+                              uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream) {
+    if (npairs < 0 || !params || params->max_iter < 1) return PVVC_ERR_ARG;
+    if (npairs == 0) return PVVC_OK;
+    if (!src_xyz || !src_off || !tgt_xyz || !tgt_off || !T_out || !workspace) return PVVC_ERR_ARG;
+    IcpWs w;
+    if (ws_bytes(npairs, total_src_points, total_tgt_points, &w, workspace) > workspace_bytes) return PVVC_ERR_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    k_grid<256><<<npairs, 256, 0, s>>>(tgt_xyz, tgt_off, nullptr, w.hdr, w.cstart, w.sorted);
+    k_icp<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, tgt_off, w.hdr, w.cstart, w.sorted, init, *params, T_out, mse_out,
+                                         iters_out, converged_out);
+    return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
+}
+
+extern "C" int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
+                                    const uint32_t* tgt_off, const float* T, float* mse_out, void* workspace,
+                                    uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points,
+                                    void* stream) {
+    if (npairs < 0) return PVVC_ERR_ARG;
+    if (npairs == 0) return PVVC_OK;
+    if (!src_xyz || !src_off || !tgt_xyz || !tgt_off || !mse_out || !workspace) return PVVC_ERR_ARG;
+    IcpWs w;
+    if (ws_bytes(npairs, total_src_points, total_tgt_points, &w, workspace) > workspace_bytes) return PVVC_ERR_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    // transformed source -> target, and target -> transformed source; max of both
+    k_grid<256><<<npairs, 256, 0, s>>>(tgt_xyz, tgt_off, nullptr, w.hdr, w.cstart, w.sorted);
+    k_grid<256><<<npairs, 256, 0, s>>>(src_xyz, src_off, T, w.hdr2, w.cstart2, w.sorted2);
+    k_nn_mean<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, T, tgt_off, w.hdr, w.cstart, w.sorted, w.tmp);
+    k_nn_mean<<<npairs, kIcpThreads, 0, s>>>(tgt_xyz, tgt_off, nullptr, src_off, w.hdr2, w.cstart2, w.sorted2,
+                                             w.tmp + npairs);
+    k_max2<<<(npairs + 255) / 256, 256, 0, s>>>(w.tmp, npairs, mse_out);
+    return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
+}

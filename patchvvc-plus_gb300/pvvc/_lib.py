@@ -31,7 +31,7 @@ class BatchDesc(C.Structure):
 
 class IcpParams(C.Structure):
     _fields_ = [("max_corr_dist", C.c_float), ("max_iter", C.c_int32), ("fitness_eps", C.c_float),
-                ("transform_eps", C.c_float)]
+                ("transform_eps", C.c_float), ("mse_abs_eps", C.c_float)]
 
 
 class SynthConfig(C.Structure):
@@ -61,6 +61,10 @@ SIGNATURES = [
                                         C.c_uint64, u64p, u32p]),
     ("pvvc_rlgr_encode", C.c_int64, [i64p, C.c_uint64, u8p, C.c_uint64]),
     ("pvvc_rlgr_decode_host", C.c_int, [u8p, C.c_uint64, C.c_uint64, i64p]),
+    ("pvvc_icp_workspace_size", C.c_int, [C.c_int32, C.c_uint64, C.c_uint64, u64p]),
+    ("pvvc_icp_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, C.POINTER(IcpParams), vp, vp, vp, vp, vp, C.c_uint64,
+                                 C.c_uint64, C.c_uint64, vp]),
+    ("pvvc_cloud_mse_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
     # synthetic sequences (not part of the drop-in boundary)
     ("pvvc_synth_create", C.c_int, [C.POINTER(SynthConfig), C.POINTER(vp)]),
     ("pvvc_synth_destroy", None, [vp]),

@@ -1,0 +1,135 @@
+"""Batched ICP over the C ABI (pvvc_icp_batch / pvvc_cloud_mse_batch) and the
+seeded patch-pair workload that stands in for the encoder's registration
+calls (PatchFitting::AddPatch, src/patch/patch_fitting.cc:58-79;
+PatchesRegistration::Task, src/registration/patches_registration.cc:80-90).
+
+Device buffers are torch tensors (plumbing only); the work runs in
+libpvvc_gb300.so."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+def rotation(axis, deg) -> np.ndarray:
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    th = np.deg2rad(deg)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(th) * K + (1 - np.cos(th)) * (K @ K)
+
+
+@dataclass
+class Pairs:
+    src: list          # float32 [n,3] per pair (int32 10-bit coordinates as floats)
+    tgt: list          # float32 [m,3] per pair
+    T_true: np.ndarray  # [npairs,4,4]: maps src onto the clean target
+
+    @property
+    def n(self) -> int:
+        return len(self.src)
+
+
+def make_pairs(npairs: int, seed: int = 0, max_deg: float = 15.0, max_trans: float = 20.0, noise: float = 0.5,
+               outliers: float = 0.05, synth=None) -> Pairs:
+    """Each source is a patch of the seeded synthetic surface (lognormal sizes,
+    median 1500, clipped to [200, 8000], 10-bit integer coordinates); its
+    target is the source rotated by U(0, max_deg) degrees about a uniform axis
+    through its centroid, translated by U(-max_trans, max_trans)^3, with
+    N(0, noise) jitter and `outliers` x n extra points uniform in its box."""
+    from .synth import Synth, config
+    if synth is None:
+        synth = Synth(config("seq300", nframes=1, gof=1, seed=seed))
+    npat = synth.patch_count(0)
+    rng = np.random.default_rng(seed + 12345)
+    src, tgt, Ts = [], [], []
+    cache = {}
+    for i in range(npairs):
+        p = int(rng.integers(0, npat))
+        if p not in cache:
+            cache[p] = synth.patch(0, p)[0]
+        s = cache[p]
+        c = s.mean(0)
+        R = rotation(rng.normal(size=3), rng.uniform(0, max_deg))
+        t = rng.uniform(-max_trans, max_trans, 3)
+        T = np.eye(4)
+        T[:3, :3] = R
+        T[:3, 3] = c + t - R @ c
+        q = (s.astype(np.float64) - c) @ R.T + c + t + rng.normal(0, noise, s.shape)
+        k = int(round(outliers * s.shape[0]))
+        lo, hi = q.min(0), q.max(0)
+        q = np.concatenate([q, rng.uniform(lo, hi, (k, 3))])
+        src.append(s.astype(np.float32))
+        tgt.append(q.astype(np.float32))
+        Ts.append(T)
+    return Pairs(src, tgt, np.array(Ts))
+
+
+def _pack(clouds):
+    off = np.zeros(len(clouds) + 1, np.uint32)
+    off[1:] = np.cumsum([c.shape[0] for c in clouds])
+    return np.concatenate(clouds).astype(np.float32), off
+
+
+class IcpBatch:
+    """Device-resident batch of (source, target) pairs."""
+
+    def __init__(self, pairs: Pairs, device="cuda"):
+        import torch
+        self.torch = torch
+        s, so = _pack(pairs.src)
+        t, to = _pack(pairs.tgt)
+        self.n = pairs.n
+        self.ns, self.nt = int(so[-1]), int(to[-1])
+        dev = torch.device(device)
+        self.src = torch.from_numpy(s).to(dev)
+        self.tgt = torch.from_numpy(t).to(dev)
+        self.soff = torch.from_numpy(so.astype(np.int32)).to(dev)
+        self.toff = torch.from_numpy(to.astype(np.int32)).to(dev)
+        b = C.c_uint64(0)
+        L.check(L.lib().pvvc_icp_workspace_size(self.n, self.ns, self.nt, C.byref(b)), "pvvc_icp_workspace_size")
+        self.ws = torch.empty(max(int(b.value), 256), dtype=torch.uint8, device=dev)
+        self.T = torch.empty((self.n, 16), dtype=torch.float32, device=dev)
+        self.mse = torch.empty(self.n, dtype=torch.float32, device=dev)
+        self.iters = torch.empty(self.n, dtype=torch.int32, device=dev)
+        self.conv = torch.empty(self.n, dtype=torch.uint8, device=dev)
+        self.dev = dev
+
+    def run(self, init=None, max_corr_dist=1e6, max_iter=50, fitness_eps=0.0, transform_eps=0.0, mse_abs_eps=1e-6,
+            stream=None):
+        """Launch pvvc_icp_batch (stream-ordered, no sync).  init: device
+        tensor [n,16] row-major or None."""
+        prm = L.IcpParams(max_corr_dist, max_iter, fitness_eps, transform_eps, mse_abs_eps)
+        sp = stream if stream is not None else self.torch.cuda.current_stream(self.dev).cuda_stream
+        L.check(L.lib().pvvc_icp_batch(self.n, self.src.data_ptr(), self.soff.data_ptr(), self.tgt.data_ptr(),
+                                       self.toff.data_ptr(), None if init is None else init.data_ptr(), C.byref(prm),
+                                       self.T.data_ptr(), self.mse.data_ptr(), self.iters.data_ptr(), self.conv.data_ptr(),
+                                       self.ws.data_ptr(), self.ws.numel(), self.ns, self.nt, sp), "pvvc_icp_batch")
+
+    def results(self):
+        self.torch.cuda.synchronize(self.dev)
+        return (self.T.cpu().numpy().reshape(-1, 4, 4), self.mse.cpu().numpy(), self.iters.cpu().numpy(),
+                self.conv.cpu().numpy().astype(bool))
+
+    def cloud_mse(self, T=None, stream=None):
+        """ICPBase::CloudMSE of every pair after transforming the source by T
+        (device [n,16], default: the last ICP result)."""
+        T = self.T if T is None else T
+        out = self.torch.empty(self.n, dtype=self.torch.float32, device=self.dev)
+        sp = stream if stream is not None else self.torch.cuda.current_stream(self.dev).cuda_stream
+        L.check(L.lib().pvvc_cloud_mse_batch(self.n, self.src.data_ptr(), self.soff.data_ptr(), self.tgt.data_ptr(),
+                                             self.toff.data_ptr(), T.data_ptr(), out.data_ptr(), self.ws.data_ptr(),
+                                             self.ws.numel(), self.ns, self.nt, sp), "pvvc_cloud_mse_batch")
+        self.torch.cuda.synchronize(self.dev)
+        return out.cpu().numpy()
+
+
+def rotation_error_deg(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """Angle of A[:3,:3] B[:3,:3]^T per pair, degrees."""
+    R = np.einsum("nij,nkj->nik", A[:, :3, :3].astype(np.float64), B[:, :3, :3].astype(np.float64))
+    c = np.clip((np.trace(R, axis1=1, axis2=2) - 1) / 2, -1, 1)
+    return np.rad2deg(np.arccos(c))
