@@ -187,6 +187,25 @@ int pvvc_icp_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off
                    const uint32_t* tgt_off, const float* init, const pvvc_icp_params* params, float* T_out,
                    float* mse_out, int32_t* iters_out, uint8_t* converged_out, void* workspace,
                    uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream);
+/* pvvc_icp_batch without a workspace argument and without any allocation.
+ * No counterpart in the reference.  It exists for callers that cannot
+ * allocate device memory at the point where they register patches: an
+ * encoder embedded in a host application that has already reserved the
+ * GPU's memory for its own pool, or a per-frame callback where cudaMalloc's
+ * implicit device-wide synchronisation would stall work in flight.  The
+ * grid scratch lives in one fixed device array of about 21 MB that every GPU
+ * loading the library holds until exit.  Limits: npairs <= 512 and
+ * total_tgt_points (which must equal tgt_off[npairs]) <= 1,048,576;
+ * larger batches return PVVC_ERR_CAPACITY.  The first call on a device looks
+ * up the array's address (cudaGetSymbolAddress) with that device current;
+ * make that first call before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (different streams, or different host
+ * threads on the same device) race and must be serialised by the caller.
+ * Results are those of pvvc_icp_batch. */
+int pvvc_icp_batch_noalloc(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
+                           const uint32_t* tgt_off, const float* init, const pvvc_icp_params* params, float* T_out,
+                           float* mse_out, int32_t* iters_out, uint8_t* converged_out, uint64_t total_tgt_points,
+                           void* stream);
 /* Symmetric NN mean squared distance of each pair after applying T
  * (ICPBase::CloudMSE, src/registration/registration_base.cc:114-158). */
 int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,

@@ -20,6 +20,7 @@
 
 #include <cfloat>
 #include <cstdint>
+#include <mutex>
 
 #include "pvvc_gb300.h"
 
@@ -446,6 +447,33 @@ __global__ void __launch_bounds__(kIcpThreads) k_nn_mean(const float* __restrict
     }
 }
 
+// ---------------------------------------------------------------------------
+// pvvc_icp_batch_noalloc: the same two kernels as pvvc_icp_batch, with the
+// target grid kept in a fixed file-scope device array instead of a
+// caller-provided workspace, so that the call allocates nothing.
+namespace {
+constexpr int32_t kNoAllocMaxPairs = 512;
+constexpr uint64_t kNoAllocMaxTgtPoints = 1ull << 20;  // 1,048,576 target points
+constexpr uint64_t kNoAllocHdrOff = 0;
+constexpr uint64_t kNoAllocCellOff = (sizeof(GridHdr) * kNoAllocMaxPairs + 255) / 256 * 256;
+constexpr uint64_t kNoAllocSortedOff = kNoAllocCellOff + (4ull * (kCells + 1) * kNoAllocMaxPairs + 255) / 256 * 256;
+constexpr uint64_t kNoAllocBytes = kNoAllocSortedOff + (12ull * kNoAllocMaxTgtPoints + 255) / 256 * 256;  // ~21 MB
+}  // namespace
+}  // namespace pvvc
+
+// Every GPU that loads this library holds this array (~21 MB) until the
+// process exits.  All calls share it and it keeps the last call's contents;
+// the grid build overwrites every byte a call reads, so nothing needs
+// clearing between calls.  Host code must not use the name as a pointer:
+// the device address comes from cudaGetSymbolAddress below.
+static __device__ __align__(256) unsigned char g_icp_noalloc_scratch[pvvc::kNoAllocBytes];
+
+namespace pvvc {
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[128] = {};  // device address of the array, per device ordinal
+}  // namespace
+
 __global__ void k_max2(const float* __restrict__ a, int n, float* __restrict__ o) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) o[i] = fmaxf(a[i], a[i + n]);
@@ -529,5 +557,39 @@ extern "C" int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const 
     k_nn_mean<<<npairs, kIcpThreads, 0, s>>>(tgt_xyz, tgt_off, nullptr, src_off, w.hdr2, w.cstart2, w.sorted2,
                                              w.tmp + npairs);
     k_max2<<<(npairs + 255) / 256, 256, 0, s>>>(w.tmp, npairs, mse_out);
+    return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
+}
+
+extern "C" int pvvc_icp_batch_noalloc(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
+                                      const uint32_t* tgt_off, const float* init, const pvvc_icp_params* params, float* T_out,
+                                      float* mse_out, int32_t* iters_out, uint8_t* converged_out, uint64_t total_tgt_points,
+                                      void* stream) {
+    if (npairs < 0 || !params || params->max_iter < 1) return PVVC_ERR_ARG;
+    if (npairs > kNoAllocMaxPairs || total_tgt_points > kNoAllocMaxTgtPoints) return PVVC_ERR_CAPACITY;
+    if (npairs == 0) return PVVC_OK;
+    if (!src_xyz || !src_off || !tgt_xyz || !tgt_off || !T_out) return PVVC_ERR_ARG;
+    // first call on each device: look up the array's device address with that
+    // device current (the caller's current device)
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PVVC_ERR_CUDA;
+    if (dev < 0 || dev >= 128) return PVVC_ERR_ARG;
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_addr[dev]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_icp_noalloc_scratch) != cudaSuccess || !p) return PVVC_ERR_CUDA;
+            g_noalloc_addr[dev] = p;
+        }
+        base = g_noalloc_addr[dev];
+    }
+    uint8_t* b = static_cast<uint8_t*>(base);
+    GridHdr* hdr = reinterpret_cast<GridHdr*>(b + kNoAllocHdrOff);
+    int* cstart = reinterpret_cast<int*>(b + kNoAllocCellOff);
+    float* sorted = reinterpret_cast<float*>(b + kNoAllocSortedOff);
+    cudaStream_t s = (cudaStream_t)stream;
+    k_grid<256><<<npairs, 256, 0, s>>>(tgt_xyz, tgt_off, nullptr, hdr, cstart, sorted);
+    k_icp<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, tgt_off, hdr, cstart, sorted, init, *params, T_out, mse_out,
+                                         iters_out, converged_out);
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }

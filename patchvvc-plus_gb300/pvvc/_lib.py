@@ -64,6 +64,8 @@ SIGNATURES = [
     ("pvvc_icp_workspace_size", C.c_int, [C.c_int32, C.c_uint64, C.c_uint64, u64p]),
     ("pvvc_icp_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, C.POINTER(IcpParams), vp, vp, vp, vp, vp, C.c_uint64,
                                  C.c_uint64, C.c_uint64, vp]),
+    ("pvvc_icp_batch_noalloc", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, C.POINTER(IcpParams), vp, vp, vp, vp,
+                                         C.c_uint64, vp]),
     ("pvvc_cloud_mse_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
     # synthetic sequences (not part of the drop-in boundary)
     ("pvvc_synth_create", C.c_int, [C.POINTER(SynthConfig), C.POINTER(vp)]),
