@@ -55,6 +55,7 @@ def parse_args():
     ap.add_argument("--frames", type=int, default=300)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--icp-pairs", type=int, default=4096, help="batched ICP workload size (0: skip)")
     return ap.parse_args()
 
 
@@ -291,16 +292,58 @@ def run_ours(args):
         if not args.no_e2e:
             e2e = measure_e2e(args, pvvc, frames, P, torch, stream)
         cb = cpu_baseline(frames, args.cpu_seconds)
+        icp = measure_icp(args, torch, peak) if args.icp_pairs > 0 else None
         out = {"metric": "decoded Mpts/s (seq300, GoP 30, ~800k pts/frame)", "value": value, "unit": "Mpts/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
-               "clocks": clk.summary(), "gpu_launches": 4 * args.steps, "points_per_step": P * world}
+               "clocks": clk.summary(), "gpu_launches": 4 * args.steps, "points_per_step": P * world, "icp": icp}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     return out
+
+
+def measure_icp(args, torch, peak_gbs):
+    """Batched plain ICP from identity on the seeded pair workload: sources are
+    lognormal-sized synthetic patches (10-bit integer coordinates), targets
+    the source rotated 0-15 deg about its centroid, translated +-20 voxels,
+    N(0,0.5) jitter, 5% outliers; max 50 iterations, stop at |dMSE| < 1e-6."""
+    from pvvc.icp import IcpBatch, make_pairs
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    t0 = time.time()
+    pairs = make_pairs(args.icp_pairs, seed=7)
+    b = IcpBatch(pairs)
+    kw = dict(max_corr_dist=1e6, max_iter=50, fitness_eps=0.0, transform_eps=0.0, mse_abs_eps=1e-6)
+    for _ in range(2):
+        b.run(**kw)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record()
+    for _ in range(reps):
+        b.run(**kw)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    T, mse, iters, conv = b.results()
+    nbytes = 12 * (b.ns + b.nt)
+    # CPU baseline: the oracle's restatement of the reference's PCL ICP on a sample, all cores
+    from oracle import Oracle
+    o = Oracle()
+    ns = min(256, args.icp_pairs)
+    cores = os.cpu_count() or 1
+    c0 = time.perf_counter()
+    o.icp_batch(pairs.src[:ns], pairs.tgt[:ns], cores, **kw)
+    cdt = time.perf_counter() - c0
+    log(f"icp: {args.icp_pairs} pairs in {ms:.2f} ms (setup {time.time() - t0:.1f}s)")
+    return {"npairs": args.icp_pairs, "patches_per_s": args.icp_pairs / (ms / 1e3), "ms_per_batch": ms,
+            "mean_iters": float(iters.mean()), "converged": float(conv.mean()), "mean_fitness_mse": float(mse.mean()),
+            "median_fitness_mse": float(np.median(mse)), "points": int(b.ns + b.nt),
+            "hbm_gbs_one_read": nbytes / (ms / 1e3) / 1e9, "hbm_frac_one_read": nbytes / (ms / 1e3) / 1e9 / peak_gbs,
+            "cpu_baseline": {"value": ns / cdt, "unit": "patches/s", "cores": cores, "kind": "port",
+                             "sample": f"first {ns} pairs, {cdt:.1f}s"}}
 
 
 def measure_e2e(args, pvvc, frames, P, torch, stream):

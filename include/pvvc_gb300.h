@@ -106,10 +106,11 @@ int pvvc_plan_query(const pvvc_plan* plan, uint64_t* total_points, uint64_t* wor
 int pvvc_decode(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
                 float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, void* stream);
 
-/* pvvc_decode with a CUDA event recorded on `stream` before the first and
- * after each of its four kernels (tree expansion, RLGR, inverse RAHT of the
- * intra slices, inverse RAHT of the predictive slices): events[0..4] must be
- * created by the caller.  No reference counterpart: the reference only
+/* pvvc_decode with a CUDA event recorded on `stream` before the first kernel
+ * and after each of its four stages (tree expansion; RLGR; inverse RAHT of
+ * the slices that need only this batch's trees, including every intra slice;
+ * inverse RAHT of the predictive slices that need phase-three colours):
+ * events[0..4] must be created by the caller.  No reference counterpart: the reference only
  * prints wall-clock frame times (test/test_decode_only.cc:129-150). */
 int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
                          float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, void* stream,

@@ -110,6 +110,9 @@ class Oracle:
         if hasattr(lib, "pvo_icp_align"):
             lib.pvo_icp_align.restype = C.c_int
             lib.pvo_icp_align.argtypes = [_f32p, C.c_size_t, _f32p, C.c_size_t, _f32p, C.POINTER(_IcpParams), _f32p, _f32p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+            lib.pvo_icp_batch.restype = C.c_int
+            lib.pvo_icp_batch.argtypes = [C.c_int, _f32p, _u32p, _f32p, _u32p, C.POINTER(_IcpParams), _f32p, _f32p,
+                                          C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
             lib.pvo_cloud_mse.restype = C.c_float
             lib.pvo_cloud_mse.argtypes = [_f32p, C.c_size_t, _f32p, C.c_size_t]
 
@@ -219,6 +222,24 @@ class Oracle:
         if st:
             raise RuntimeError(f"icp status {st}")
         return T.reshape(4, 4), float(fit.value), int(it.value), bool(conv.value)
+
+    def icp_batch(self, src_list, tgt_list, nthreads, max_corr_dist=1e6, max_iter=50, fitness_eps=0.0,
+                  transform_eps=0.0, mse_abs_eps=1e-6):
+        """pvo_icp_align over many pairs on nthreads threads."""
+        n = len(src_list)
+        s = np.ascontiguousarray(np.concatenate(src_list), np.float32)
+        t = np.ascontiguousarray(np.concatenate(tgt_list), np.float32)
+        so = np.zeros(n + 1, np.uint32); so[1:] = np.cumsum([x.shape[0] for x in src_list])
+        to = np.zeros(n + 1, np.uint32); to[1:] = np.cumsum([x.shape[0] for x in tgt_list])
+        T = np.zeros((n, 16), np.float32)
+        fit = np.zeros(n, np.float32)
+        it = np.zeros(n, np.int32)
+        cv = np.zeros(n, np.int32)
+        p = _IcpParams(max_corr_dist, max_iter, fitness_eps, transform_eps, mse_abs_eps)
+        self.lib.pvo_icp_batch(n, _ptr(s, _f32p), _ptr(so, _u32p), _ptr(t, _f32p), _ptr(to, _u32p), C.byref(p),
+                               _ptr(T, _f32p), _ptr(fit, _f32p), it.ctypes.data_as(C.POINTER(C.c_int)),
+                               cv.ctypes.data_as(C.POINTER(C.c_int)), nthreads)
+        return T.reshape(n, 4, 4), fit, it, cv.astype(bool)
 
     def cloud_mse(self, a, b) -> float:
         a = np.ascontiguousarray(a, np.float32)

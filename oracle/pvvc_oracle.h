@@ -121,6 +121,9 @@ typedef struct {
 int pvo_icp_align(const float* src, size_t ns, const float* tgt, size_t nt,
                   const float* init, const pvo_icp_params* p,
                   float* T_out, float* fitness, int* iters, int* converged);
+/* pvo_icp_align over many pairs (point ranges soff/toff) with nthreads threads. */
+int pvo_icp_batch(int npairs, const float* src, const uint32_t* soff, const float* tgt, const uint32_t* toff,
+                  const pvo_icp_params* p, float* T, float* fit, int* iters, int* conv, int nthreads);
 /* Symmetric mean squared NN distance, max of both directions. */
 float pvo_cloud_mse(const float* a, size_t na, const float* b, size_t nb);
 

@@ -270,3 +270,54 @@ float pvo_cloud_mse(const float* a, size_t na, const float* b, size_t nb) {
     m2 /= (double)nb;
     return (float)(m1 > m2 ? m1 : m2);
 }
+
+/* ---- many pairs on a thread pool (PatchesRegistration::Task's queue,
+ * src/registration/patches_registration.cc:42-126) ---- */
+#include <pthread.h>
+
+typedef struct {
+    int npairs;
+    const float* src;
+    const uint32_t* soff;
+    const float* tgt;
+    const uint32_t* toff;
+    const pvo_icp_params* p;
+    float* T;
+    float* fit;
+    int* iters;
+    int* conv;
+    pthread_mutex_t mu;
+    int next;
+} icp_job_t;
+
+static void* icp_worker(void* arg) {
+    icp_job_t* j = (icp_job_t*)arg;
+    for (;;) {
+        pthread_mutex_lock(&j->mu);
+        int i = j->next++;
+        pthread_mutex_unlock(&j->mu);
+        if (i >= j->npairs) break;
+        const uint32_t a = j->soff[i], b = j->soff[i + 1], c = j->toff[i], d = j->toff[i + 1];
+        pvo_icp_align(j->src + 3ull * a, b - a, j->tgt + 3ull * c, d - c, NULL, j->p, j->T + 16 * i, j->fit + i,
+                      j->iters + i, j->conv + i);
+    }
+    return NULL;
+}
+
+int pvo_icp_batch(int npairs, const float* src, const uint32_t* soff, const float* tgt, const uint32_t* toff,
+                  const pvo_icp_params* p, float* T, float* fit, int* iters, int* conv, int nthreads) {
+    icp_job_t j = {npairs, src, soff, tgt, toff, p, T, fit, iters, conv};
+    pthread_mutex_init(&j.mu, NULL);
+    j.next = 0;
+    if (nthreads < 1) nthreads = 1;
+    pthread_t* th = (pthread_t*)malloc((size_t)nthreads * sizeof(pthread_t));
+    int started = 0;
+    for (int i = 0; i < nthreads; ++i)
+        if (pthread_create(&th[i], NULL, icp_worker, &j) == 0) started++;
+        else break;
+    if (!started) icp_worker(&j);
+    for (int i = 0; i < started; ++i) pthread_join(th[i], NULL);
+    free(th);
+    pthread_mutex_destroy(&j.mu);
+    return PVO_OK;
+}

@@ -18,12 +18,31 @@ cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payloa
                         cudaStream_t s);
 cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
                         int32_t* rstatus, cudaStream_t s);
-cudaError_t launch_raht(const SliceWork* work, int first, int count, const StateView& st, const float* coef, float* fallback,
-                        const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz, uint8_t* rgb, float* p24,
-                        int32_t* status, int wcap, cudaStream_t s);
+cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int count, const StateView& st, const float* coef,
+                              float* fallback, const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz,
+                              uint8_t* rgb, float* p24, int32_t* status, int wcap, cudaStream_t s);
+cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, int ngroups, const int32_t* items,
+                              const StateView& st, const float* coef, const int32_t* tstatus, const int32_t* rstatus,
+                              int32_t* fstatus, float* xyz, uint8_t* rgb, float* p24, int32_t* status, float* scratch,
+                              uint64_t scratch_floats, int nctas, int* counter, cudaStream_t s);
+
+// persistent CTAs of the group kernel per SM, and the SM count (queried once)
+constexpr int kGroupCtasPerSm = 2;
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 132;
+    }
+    return n;
+}
+
+// slices of one slot decoded by one warp when at least this many share it
+constexpr int kMinGroup = 4;
 
 // level-signal capacity (nodes) of the shared-memory path of k_raht
-constexpr int kRahtWcap = 2048;
+constexpr int kRahtWcap = 1024;
 
 namespace {
 inline uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
@@ -68,9 +87,19 @@ struct pvvc_plan {
     int32_t nslices = 0, nintra = 0, max_slot = -1;
     uint64_t total_points = 0;
     uint64_t ws_coef = 0, ws_fb = 0, ws_tstatus = 0, ws_rstatus = 0, ws_fstatus = 0, ws_bytes = 0;
+    uint64_t ws_grp = 0, ws_counter = 0, grp_floats = 0;  // group-kernel level buffers, queue counters
+    int32_t grp_ctas = 0;
+    uint64_t coef_floats = 0;
     std::vector<pvvc::SliceWork> work;
     std::vector<int32_t> order;
-    pvvc::DevBuf d_work, d_order;
+    // inverse-RAHT schedule: phase A needs only this batch's trees; phase B
+    // also needs phase A's intra colours.  Groups go to the warp kernel,
+    // lists to the per-slice kernel.
+    std::vector<pvvc::GroupDesc> groups;  // [A groups | B groups]
+    int32_t ngroups_a = 0, ngroups_b = 0;
+    std::vector<int32_t> idx;             // [group items | slice list A | slice list B]
+    int32_t nlist_a = 0, nlist_b = 0, list_a_off = 0, list_b_off = 0;
+    pvvc::DevBuf d_work, d_order, d_groups, d_idx;
 };
 
 struct pvvc_state {
@@ -104,7 +133,13 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
         std::sort(s.begin(), s.end());
         if (std::adjacent_find(s.begin(), s.end()) != s.end()) return PVVC_ERR_ARG;
     }
-    auto by_size = [&](int32_t a, int32_t b) { return d->size[a] != d->size[b] ? d->size[a] > d->size[b] : a < b; };
+    // largest first; equal sizes grouped by slot, so that the frames of one
+    // patch run next to each other and share its tree tables in L2
+    auto by_size = [&](int32_t a, int32_t b) {
+        if (d->size[a] != d->size[b]) return d->size[a] > d->size[b];
+        if (d->slot[a] != d->slot[b]) return d->slot[a] < d->slot[b];
+        return a < b;
+    };
     std::stable_sort(intra.begin(), intra.end(), by_size);
     std::stable_sort(pred.begin(), pred.end(), by_size);
     p->nslices = n;
@@ -140,10 +175,62 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
     for (int i : intra) fill(q++, i);
     for (int i : pred) fill(q++, i);
     p->total_points = pts;
+    p->coef_floats = coef;
+    // inverse-RAHT schedule: slices grouped by slot (largest slots first)
+    {
+        std::vector<std::vector<int32_t>> per;  // queue indices per slot, in queue order
+        std::vector<int32_t> slot_of;
+        std::vector<int32_t> where(max_slot + 1, -1);
+        for (int q2 = 0; q2 < n; ++q2) {
+            const int32_t sl = p->work[q2].slot;
+            if (where[sl] < 0) {
+                where[sl] = (int32_t)per.size();
+                per.emplace_back();
+                slot_of.push_back(sl);
+            }
+            per[where[sl]].push_back(q2);
+        }
+        std::vector<int32_t> ord(per.size());
+        std::iota(ord.begin(), ord.end(), 0);
+        std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return p->work[per[a][0]].n > p->work[per[b][0]].n; });
+        std::vector<GroupDesc> ga, gb;
+        std::vector<int32_t> items, la, lb;
+        for (int32_t si : ord) {
+            const auto& L = per[si];
+            const bool has_intra = !(p->work[L[0]].type & PVVC_TYPE_PREDICT);
+            for (size_t c0 = 0; c0 < L.size(); c0 += 32) {
+                const int cnt = (int)std::min<size_t>(32, L.size() - c0);
+                const bool first = c0 == 0;
+                const bool phase_b = has_intra && !first;
+                if ((first && has_intra) || cnt >= kMinGroup) {
+                    GroupDesc g{slot_of[si], (int32_t)items.size(), cnt, (first && has_intra) ? 1 : 0};
+                    items.insert(items.end(), L.begin() + c0, L.begin() + c0 + cnt);
+                    (phase_b ? gb : ga).push_back(g);
+                } else {
+                    auto& dst = phase_b ? lb : la;
+                    dst.insert(dst.end(), L.begin() + c0, L.begin() + c0 + cnt);
+                }
+            }
+        }
+        p->groups = ga;
+        p->groups.insert(p->groups.end(), gb.begin(), gb.end());
+        p->ngroups_a = (int32_t)ga.size();
+        p->ngroups_b = (int32_t)gb.size();
+        p->idx = items;
+        p->list_a_off = (int32_t)p->idx.size();
+        p->idx.insert(p->idx.end(), la.begin(), la.end());
+        p->list_b_off = (int32_t)p->idx.size();
+        p->idx.insert(p->idx.end(), lb.begin(), lb.end());
+        p->nlist_a = (int32_t)la.size();
+        p->nlist_b = (int32_t)lb.size();
+    }
     // RLGR order: all slices by size, so that a warp decodes similar lengths
     p->order.resize(n);
     std::iota(p->order.begin(), p->order.end(), 0);
-    std::stable_sort(p->order.begin(), p->order.end(), [&](int32_t a, int32_t b) { return p->work[a].n > p->work[b].n; });
+    std::stable_sort(p->order.begin(), p->order.end(), [&](int32_t a, int32_t b) {
+        if (p->work[a].n != p->work[b].n) return p->work[a].n > p->work[b].n;
+        return p->work[a].slot < p->work[b].slot;
+    });
     // workspace layout
     uint64_t off = 0;
     p->ws_coef = off;
@@ -156,6 +243,18 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
     off = align_up(off + 4ull * n, 256);
     p->ws_fstatus = off;
     off = align_up(off + 4ull * n, 256);
+    // group kernel: per persistent CTA two level buffers of [width][32 lanes][3]
+    // floats; an internal level of a valid tree is never wider than its leaves
+    {
+        uint32_t maxn = 0;
+        for (const auto& g : p->groups) maxn = std::max(maxn, p->work[p->idx[g.first]].n);
+        p->grp_ctas = std::min<int32_t>((int32_t)p->groups.size(), kGroupCtasPerSm * sm_count());
+        p->grp_floats = 2ull * std::max<uint32_t>(maxn, 1) * 96;
+        p->ws_grp = off;
+        off = align_up(off + 4ull * p->grp_floats * std::max(p->grp_ctas, 1), 256);
+        p->ws_counter = off;
+        off = align_up(off + 16, 256);
+    }
     p->ws_bytes = std::max<uint64_t>(off, 256);
     // upload
     if (n > 0) {
@@ -164,6 +263,14 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
         if (cudaMemcpy(p->d_work.p, p->work.data(), sizeof(SliceWork) * n, cudaMemcpyHostToDevice) != cudaSuccess)
             return PVVC_ERR_CUDA;
         if (cudaMemcpy(p->d_order.p, p->order.data(), 4ull * n, cudaMemcpyHostToDevice) != cudaSuccess) return PVVC_ERR_CUDA;
+        const size_t gbytes = sizeof(GroupDesc) * std::max<size_t>(p->groups.size(), 1);
+        if (p->d_groups.ensure(gbytes) != cudaSuccess || p->d_idx.ensure(4ull * std::max<size_t>(p->idx.size(), 1)) != cudaSuccess)
+            return PVVC_ERR_NOMEM;
+        if (!p->groups.empty() &&
+            cudaMemcpy(p->d_groups.p, p->groups.data(), sizeof(GroupDesc) * p->groups.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        if (!p->idx.empty() && cudaMemcpy(p->d_idx.p, p->idx.data(), 4ull * p->idx.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+            return PVVC_ERR_CUDA;
     }
     return PVVC_OK;
 }
@@ -188,12 +295,25 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     };
     if (!mark(0)) return PVVC_ERR_CUDA;
     if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) return PVVC_ERR_CUDA;
+    // zero symbols are not written by the decoder: clear the planes first
+    if (cudaMemsetAsync(coef, 0, 4ull * p->coef_floats, s) != cudaSuccess) return PVVC_ERR_CUDA;
     if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, s) != cudaSuccess || !mark(2)) return PVVC_ERR_CUDA;
-    if (launch_raht(dw, 0, p->nintra, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap, s) != cudaSuccess ||
+    float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
+    int* cnt = reinterpret_cast<int*>(w + p->ws_counter);
+    const GroupDesc* dg = static_cast<const GroupDesc*>(p->d_groups.p);
+    const int32_t* di = static_cast<const int32_t*>(p->d_idx.p);
+    // phase A: groups holding their slot's intra slice, slots without an intra slice here
+    if (launch_raht_group(dw, dg, p->ngroups_a, di, st->v, coef, ts, rs, fs, xyz, rgb, p24, status, gsc, p->grp_floats,
+                          p->grp_ctas, cnt, s) != cudaSuccess ||
+        launch_raht_slice(dw, di + p->list_a_off, p->nlist_a, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap, s) !=
+            cudaSuccess ||
         !mark(3))
         return PVVC_ERR_CUDA;
-    if (launch_raht(dw, p->nintra, p->nslices - p->nintra, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap,
-                    s) != cudaSuccess ||
+    // phase B: predictive slices whose intra colours phase A produced
+    if (launch_raht_group(dw, dg + p->ngroups_a, p->ngroups_b, di, st->v, coef, ts, rs, fs, xyz, rgb, p24, status, gsc,
+                          p->grp_floats, p->grp_ctas, cnt + 1, s) != cudaSuccess ||
+        launch_raht_slice(dw, di + p->list_b_off, p->nlist_b, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap, s) !=
+            cudaSuccess ||
         !mark(4))
         return PVVC_ERR_CUDA;
     return PVVC_OK;
@@ -370,7 +490,6 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (bytes && cudaMemcpyAsync(st->payload.p, hp, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return PVVC_ERR_CUDA;
     std::vector<uint8_t> seen(std::max(st->v.nslots, 1), 0);
-    size_t fstart = 0;
     k = 0;
     std::vector<int32_t> bounds;  // slice index where each batch starts
     bounds.push_back(0);
@@ -387,7 +506,6 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
             if (fr.index[i] >= 0 && fr.index[i] < st->v.nslots) seen[fr.index[i]] = 1;
     }
     bounds.push_back(nsl);
-    (void)fstart;
     for (size_t b = 0; b + 1 < bounds.size() && rc == PVVC_OK; ++b) {
         first = bounds[b];
         const int32_t cnt = bounds[b + 1] - first;

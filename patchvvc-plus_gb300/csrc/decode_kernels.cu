@@ -268,140 +268,171 @@ __global__ void __launch_bounds__(T) k_tree(const SliceWork* __restrict__ work, 
 }
 
 // ---------------------------------------------------------------------------
-// k_rlgr: bit reader over 32-bit big-endian words
+// k_rlgr
+//
+// Bit reader: the unconsumed bits are the low 32-o bits of `hi` followed by
+// `lo`; `nx` is loaded one word ahead so a refill never waits on memory.
+// peek() returns the next 32 bits with one funnel shift.  Words past the
+// payload read as zero.
 struct BitReader {
-    const uint32_t* wp;   // next word
-    const uint32_t* wend; // one past the last word holding payload bytes
-    uint64_t win;         // next bits, MSB-aligned; bits past `nb` are zero
-    int nb;               // valid bits in win
-    uint32_t used_hi;     // consumed bits beyond the payload (overrun detector)
-    int64_t left;         // payload bits not yet consumed
+    const uint32_t* p;     // next word to load into nx
+    const uint32_t* end;   // one past the last word holding payload bytes
+    uint32_t hi, lo, nx;
+    uint32_t o;            // bits of hi already consumed (0..31)
 
-    __device__ __forceinline__ void refill() {
-        while (nb <= 32) {
-            const uint32_t v = wp < wend ? __byte_perm(__ldg(wp), 0, 0x0123) : 0u;
-            ++wp;
-            win |= (uint64_t)v << (32 - nb);
-            nb += 32;
-        }
-    }
-    __device__ __forceinline__ void consume(int k) {
-        win = k >= 64 ? 0ull : (win << k);
-        nb -= k;
-        left -= k;
-    }
-    __device__ __forceinline__ uint32_t peek(int k) const { return k ? (uint32_t)(win >> (64 - k)) : 0u; }
-    __device__ __forceinline__ int ones() const { return __clzll(~win); }
-};
-
-constexpr int kRlL = 4, kRlU0 = 3, kRlD0 = 1, kRlU1 = 2, kRlD1 = 1;
-
-// GRRead (entropy_codec.cc:196-205): q ones then a zero then k bits; 32 ones
-// escape to a raw 32-bit value.
-__device__ __forceinline__ uint64_t gr_read(BitReader& br, int k) {
-    br.refill();
-    const int q = br.ones();
-    if (q >= 32) {
-        br.consume(32);
-        br.refill();
-        const uint64_t v = br.peek(32);
-        br.consume(32);
+    __device__ __forceinline__ uint32_t load() {
+        const uint32_t v = p < end ? __byte_perm(__ldg(p), 0, 0x0123) : 0u;
+        ++p;
         return v;
     }
-    br.consume(q + 1);
-    br.refill();
-    const uint64_t r = br.peek(k);
-    br.consume(k);
-    return ((uint64_t)q << k) + r;
-}
+    __device__ __forceinline__ void init(const uint32_t* first_word, const uint32_t* last, uint32_t skip_bits) {
+        p = first_word;
+        end = last;
+        hi = load();
+        lo = load();
+        nx = load();
+        o = skip_bits;
+    }
+    __device__ __forceinline__ uint32_t peek() const { return __funnelshift_l(lo, hi, o); }
+    __device__ __forceinline__ void consume(uint32_t k) {  // k <= 32
+        o += k;
+        if (o >= 32) {
+            o -= 32;
+            hi = lo;
+            lo = nx;
+            nx = load();
+        }
+    }
+};
 
+constexpr uint32_t kRlU0 = 3, kRlU1 = 2, kRlD0 = 1, kRlD1 = 1, kRlMaxRP = 32 * 4;
+
+// k_rlgr: one thread per slice.  The coefficient planes are zeroed before the
+// launch, so a run of zeros only advances the output position; symbol n of a
+// plane goes to coefficient N-1-j (the stream is reversed).
 __global__ void __launch_bounds__(128) k_rlgr(const SliceWork* __restrict__ work, const int32_t* __restrict__ order,
                                               int nslices, const uint8_t* __restrict__ payload, float* __restrict__ coef,
                                               int32_t* __restrict__ rstatus) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nslices) return;
     const int item = order[t];
-    const SliceWork& w = work[item];
-    const uint32_t N = w.n;
-    const uint64_t total = 3ull * N;
-    const long long qp = w.qp;
-
+    const SliceWork& wk = work[item];
+    const uint32_t N = wk.n;
+    const uint32_t total = 3u * N;
+    const int32_t qp = wk.qp;
+    if (total == 0) {
+        rstatus[item] = PVVC_OK;
+        return;
+    }
+    const uint64_t off = wk.col_off;
+    const uint32_t* w0 = reinterpret_cast<const uint32_t*>(payload + (off & ~3ull));
+    const uint32_t* wend = reinterpret_cast<const uint32_t*>(payload + ((off + wk.csz + 3) & ~3ull));
     BitReader br;
-    const uint64_t start = w.col_off;
-    const uint32_t* base = reinterpret_cast<const uint32_t*>(payload + (start & ~3ull));
-    br.wp = base;
-    br.wend = reinterpret_cast<const uint32_t*>(payload + ((start + w.csz + 3) & ~3ull));
-    br.win = 0;
-    br.nb = 0;
-    br.left = 8ll * w.csz;
-    br.refill();
-    const int skip = (int)(start & 3) * 8;
-    br.win <<= skip;
-    br.nb -= skip;
-    br.refill();
+    br.init(w0, wend, (uint32_t)(off & 3) * 8);
+    float* const base = coef + wk.coef_off;
 
-    float* plane = coef + w.coef_off;  // Y, then U, then V (N floats each)
-    uint32_t j = 0;                    // position within the current plane
-    uint64_t n = 0;
-    int err = 0;
-    // symbol `n` goes to coefficient N-1-j of the current plane (the stream is reversed)
-    auto emit = [&](float v) {
-        plane[N - 1 - j] = v;
+    uint32_t kP = 0, kRP = 8;
+    uint32_t n = 0;       // symbols decoded
+    uint32_t pl = 0;      // plane of symbol n
+    uint32_t j = 0;       // position of symbol n within its plane
+    int err = PVVC_OK;
+    while (n < total) {
+        uint32_t k = kP >> 2;
+        bool after_run = false;
+        if (k) {
+            // run mode (entropy_codec.cc:226-257): every leading '1' stands for
+            // 2^k zeros and raises kP by U1 (k grows every second one); then a
+            // '0' and k bits complete the run
+            uint32_t m = 0, c;
+            int guard = 0;
+            do {
+                c = __clz(~br.peek());  // leading ones, 32 when all are ones
+                for (uint32_t i = 0; i < c; ++i) {
+                    m += 1u << (k & 31);
+                    kP += kRlU1;
+                    k = kP >> 2;
+                }
+                br.consume(c);
+            } while (c == 32 && ++guard < 64);
+            br.consume(1);
+            if (k > 31) {
+                err = PVVC_ERR_OVERRUN;
+                break;
+            }
+            m += br.peek() >> (32 - k);
+            br.consume(k);
+            const uint32_t z = m < total - n ? m : total - n;
+            n += z;
+            j += z;
+            while (j >= N && pl < 3) {  // the run may cross plane boundaries
+                j -= N;
+                ++pl;
+            }
+            if (n >= total) break;
+            after_run = true;
+        }
+        // Golomb-Rice symbol (GRRead, entropy_codec.cc:196-205)
+        const uint32_t kR = kRP >> 2;
+        const uint32_t v = br.peek();
+        const uint32_t q = __clz(~v);
+        uint32_t lo32, hi32 = 0;  // u = hi32:lo32
+        uint32_t pq;              // u >> kR, which drives kRP
+        if (q < 32) {
+            uint32_t r;
+            if (q + 1 + kR <= 32) {
+                r = kR ? (v << (q + 1)) >> (32 - kR) : 0u;
+                br.consume(q + 1 + kR);
+            } else {
+                br.consume(q + 1);
+                r = kR == 32 ? br.peek() : (br.peek() >> (32 - kR));
+                br.consume(kR);
+            }
+            // (q << kR) | r, q < 32 and kR <= 32
+            if (kR < 32) {
+                lo32 = (q << kR) | r;
+                hi32 = kR ? (q >> (32 - kR)) : 0u;
+            } else {
+                lo32 = r;
+                hi32 = q;
+            }
+            pq = q;
+        } else {  // 32 ones: a raw 32-bit value follows
+            br.consume(32);
+            lo32 = br.peek();
+            br.consume(32);
+            const uint32_t t2 = kR >= 32 ? 0u : (lo32 >> kR);
+            pq = t2 > kRlMaxRP ? kRlMaxRP : t2;
+        }
+        // adaptation (entropy_codec.cc:245-281)
+        kRP = pq ? min(kRP + pq - 1, kRlMaxRP) : (kRP < 2 ? 0u : kRP - 2);
+        const bool uz = (lo32 | hi32) == 0;
+        if (after_run) {
+            kP = kP < kRlD1 ? 0u : kP - kRlD1;
+        } else {
+            kP = uz ? kP + kRlU0 : (kP < kRlD0 ? 0u : kP - kRlD0);
+        }
+        // Unsign2Sign(u) or Unsign2Sign(u + 1) after a run, times qp
+        float val;
+        if (hi32 == 0 && lo32 < (1u << 23)) {
+            const int32_t zz = (int32_t)lo32 + (after_run ? 1 : 0);
+            const int32_t sym = (zz & 1) ? -(zz >> 1) - 1 : (zz >> 1);
+            val = __int2float_rn(sym * qp);  // |sym*qp| < 2^31: exact product, same rounding as int64
+        } else {
+            const uint64_t zz = (((uint64_t)hi32 << 32) | lo32) + (after_run ? 1u : 0u);
+            const long long sym = (zz & 1) ? -(long long)(zz >> 1) - 1 : (long long)(zz >> 1);
+            val = __ll2float_rn(sym * (long long)qp);
+        }
+        if (val != 0.0f) base[pl * N + (N - 1 - j)] = val;  // zero symbols keep the cleared value
+        ++n;
         if (++j == N) {
             j = 0;
-            plane += N;
+            ++pl;
         }
-        ++n;
-    };
-
-    uint32_t kP = 0, kRP = 2 * kRlL;
-    while (n < total) {
-        uint32_t k = kP / kRlL;
-        const int kR = (int)(kRP / kRlL);
-        uint64_t u;
-        if (k) {
-            // run mode: each leading '1' is a full run of 2^k zeros (k grows as it goes)
-            uint64_t m = 0;
-            for (;;) {
-                br.refill();
-                const int q = min(br.ones(), br.nb);
-                for (int i = 0; i < q; ++i) {
-                    m += 1ull << k;
-                    kP += kRlU1;
-                    k = kP / kRlL;
-                }
-                br.consume(q);
-                if (q < 32 || br.left < -64) break;
-            }
-            br.consume(1);
-            br.refill();
-            if (k > 32) { err = PVVC_ERR_OVERRUN; break; }
-            m += br.peek((int)k);
-            br.consume((int)k);
-            if (br.left < 0) { err = PVVC_ERR_OVERRUN; break; }
-            const uint64_t z = m < total - n ? m : total - n;
-            for (uint64_t i = 0; i < z; ++i) emit(0.0f);
-            if (n >= total) break;
-            u = gr_read(br, kR);
-            if (br.left < 0) { err = PVVC_ERR_OVERRUN; break; }
-            const uint64_t uu = u + 1;  // Unsign2Sign(u_data + 1)
-            const long long s = (uu & 1) ? -(long long)(uu >> 1) - 1 : (long long)(uu >> 1);
-            emit(__ll2float_rn(s * qp));
-            const uint64_t p = u >> kR;
-            if (p) kRP = (uint32_t)(kRP + p - 1 > 32ull * kRlL ? 32ull * kRlL : kRP + p - 1);
-            else kRP = kRP < 2 ? 0 : kRP - 2;
-            kP = kP < (uint32_t)kRlD1 ? 0 : kP - kRlD1;
-        } else {
-            u = gr_read(br, kR);
-            if (br.left < 0) { err = PVVC_ERR_OVERRUN; break; }
-            const long long s = (u & 1) ? -(long long)(u >> 1) - 1 : (long long)(u >> 1);
-            emit(__ll2float_rn(s * qp));
-            const uint64_t p = u >> kR;
-            if (p) kRP = (uint32_t)(kRP + p - 1 > 32ull * kRlL ? 32ull * kRlL : kRP + p - 1);
-            else kRP = kRP < 2 ? 0 : kRP - 2;
-            if (u) kP = kP < (uint32_t)kRlD0 ? 0 : kP - kRlD0;
-            else kP += kRlU0;
-        }
+    }
+    // bits consumed vs the payload (the reference reads past it, which is undefined)
+    if (!err) {
+        const int64_t consumed = ((int64_t)(br.p - w0) - 3) * 32 + (int64_t)br.o - (int64_t)(off & 3) * 8;
+        if (consumed > 8ll * wk.csz) err = PVVC_ERR_OVERRUN;
     }
     rstatus[item] = err;
 }
@@ -466,32 +497,86 @@ __device__ __forceinline__ void emit_leaf(const SliceWork& w, const StateView& s
     }
 }
 
+// Inverse hierarchical transform of one internal node (octree_base.cc:84-100):
+// the node's DC `g` and its coded coefficients -> the 8 child slots (absent
+// children's slots hold values nobody reads).
+__device__ __forceinline__ void inverse_node(const StateView& st, size_t node, const float* __restrict__ cy,
+                                             const float* __restrict__ cu, const float* __restrict__ cv, float gy, float gu,
+                                             float gv, float (&oy)[8], float (&ou)[8], float (&ov)[8]) {
+    const uint32_t m = st.mask[node];
+    uint32_t ci = st.coff[node];
+    const float2* ab = st.ab + node * 7;
+    float sy[8], su[8], sv[8];  // slots 1..7 (index 0 unused)
+    sy[1] = gy;
+    su[1] = gu;
+    sv[1] = gv;
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+        const float2 t = ab[i - 1];
+        float hy = 0.f, hu = 0.f, hv = 0.f;
+        if (m & (1u << i)) {
+            hy = cy[ci];
+            hu = cu[ci];
+            hv = cv[ci];
+            ++ci;
+        }
+        const float ay = sy[i], au = su[i], av = sv[i];
+        const float nbv = -t.y;
+        // [G;H] = [[a,-b],[b,a]] [g;h]   (InvertHaarTransform, octree_base.cc:186-206)
+        const float Gy = __fadd_rn(__fmul_rn(ay, t.x), __fmul_rn(hy, nbv));
+        const float Gu = __fadd_rn(__fmul_rn(au, t.x), __fmul_rn(hu, nbv));
+        const float Gv = __fadd_rn(__fmul_rn(av, t.x), __fmul_rn(hv, nbv));
+        const float Hy = __fadd_rn(__fmul_rn(ay, t.y), __fmul_rn(hy, t.x));
+        const float Hu = __fadd_rn(__fmul_rn(au, t.y), __fmul_rn(hu, t.x));
+        const float Hv = __fadd_rn(__fmul_rn(av, t.y), __fmul_rn(hv, t.x));
+        if (pair0(i) < 8) {
+            sy[pair0(i)] = Gy; su[pair0(i)] = Gu; sv[pair0(i)] = Gv;
+            sy[pair1(i)] = Hy; su[pair1(i)] = Hu; sv[pair1(i)] = Hv;
+        } else {
+            oy[pair0(i) - 8] = Gy; ou[pair0(i) - 8] = Gu; ov[pair0(i) - 8] = Gv;
+            oy[pair1(i) - 8] = Hy; ou[pair1(i) - 8] = Hu; ov[pair1(i) - 8] = Hv;
+        }
+    }
+}
+
+// Status of one slice before its inverse RAHT.  Priority: slice type, then
+// the tree (intra) or the reference (predictive), then the colour stream.
+__device__ __forceinline__ int slice_status(const SliceWork& w, int item, const StateView& st, const int32_t* tstatus,
+                                            const int32_t* rstatus) {
+    const bool predict = (w.type & PVVC_TYPE_PREDICT) != 0;
+    int err = PVVC_OK;
+    if (!(w.type & PVVC_TYPE_VALID)) err = PVVC_ERR_BAD_SLICE;
+    else if (!predict) err = tstatus[item];
+    if (!err) {
+        const SlotInfo* si = st.info + w.slot;
+        if (!si->valid) err = PVVC_ERR_NO_REFERENCE;
+        else if ((uint32_t)si->leaves != w.n) err = PVVC_ERR_SIZE;
+    }
+    if (!err) err = rstatus[item];
+    return err;
+}
+
+// k_raht_slice: one CTA per slice, level-synchronous over all internal levels
+// with the level signal in shared memory (global fallback for wide levels).
+// Used for slices that share their tree with few others in the batch.
 template <int T>
-__global__ void __launch_bounds__(T) k_raht(const SliceWork* __restrict__ work, int first_item, StateView st,
-                                            const float* __restrict__ coef, float* __restrict__ fallback,
-                                            const int32_t* __restrict__ tstatus, const int32_t* __restrict__ rstatus,
-                                            int32_t* __restrict__ fstatus, OutPtrs o, int wcap) {
+__global__ void __launch_bounds__(T) k_raht_slice(const SliceWork* __restrict__ work, const int32_t* __restrict__ list,
+                                                  StateView st, const float* __restrict__ coef, float* __restrict__ fallback,
+                                                  const int32_t* __restrict__ tstatus, const int32_t* __restrict__ rstatus,
+                                                  int32_t* __restrict__ fstatus, OutPtrs o, int wcap) {
     extern __shared__ float s_g[];  // [2][wcap][3]
     __shared__ SlotInfo s_info;
     __shared__ int s_err;
-    const int item = first_item + blockIdx.x;
+    const int item = list[blockIdx.x];
     const SliceWork& w = work[item];
     const int tid = threadIdx.x;
     const bool predict = (w.type & PVVC_TYPE_PREDICT) != 0;
-
     if (tid == 0) {
-        // status priority: slice type, then the tree (intra) or the reference
-        // (predictive), then the colour stream
-        int err = PVVC_OK;
-        if (!(w.type & PVVC_TYPE_VALID)) err = PVVC_ERR_BAD_SLICE;
-        else if (!predict) err = tstatus[item];
+        int err = slice_status(w, item, st, tstatus, rstatus);
         if (!err) {
             s_info = st.info[w.slot];
-            if (!s_info.valid) err = PVVC_ERR_NO_REFERENCE;
-            else if ((uint32_t)s_info.leaves != w.n) err = PVVC_ERR_SIZE;
-            else if (s_info.max_width > wcap && (w.fb_off == ~0ull || s_info.max_width > (int)w.n)) err = PVVC_ERR_TREE;
+            if (s_info.max_width > wcap && (w.fb_off == ~0ull || s_info.max_width > (int)w.n)) err = PVVC_ERR_TREE;
         }
-        if (!err) err = rstatus[item];
         // an intra slice that fails leaves its slot without a reference
         if (err && !predict && (w.type & PVVC_TYPE_VALID)) st.info[w.slot].valid = 0;
         s_err = err;
@@ -500,7 +585,6 @@ __global__ void __launch_bounds__(T) k_raht(const SliceWork* __restrict__ work, 
     }
     __syncthreads();
     if (s_err) return;
-
     const int H = s_info.height;
     const size_t nb = (size_t)w.slot * st.max_nodes;
     const size_t lb = (size_t)w.slot * st.max_leaves;
@@ -508,61 +592,32 @@ __global__ void __launch_bounds__(T) k_raht(const SliceWork* __restrict__ work, 
     const float* cy = coef + w.coef_off;
     const float* cu = cy + N;
     const float* cv = cu + N;
-
     if (H == 1) {
         if (tid == 0) emit_leaf(w, st, lb, 0, cy[0], cu[0], cv[0], predict, o);
         return;
     }
     float *gA, *gB;
-    int cap;
     if (s_info.max_width <= wcap) {
         gA = s_g;
         gB = s_g + 3 * wcap;
-        cap = wcap;
     } else {
         gA = fallback + w.fb_off;
         gB = gA + 3ull * N;
-        cap = (int)N;
     }
-    (void)cap;
     if (tid == 0) {
         gA[0] = cy[0];
         gA[1] = cu[0];
         gA[2] = cv[0];
     }
     __syncthreads();
-
     for (int l = 0; l < H - 1; ++l) {
         const int a = s_info.level_start[l], b = s_info.level_start[l + 1];
         const bool last = (l == H - 2);
         for (int j = tid; j < b - a; j += T) {
             const size_t node = nb + a + j;
-            const uint32_t byte = st.occ[node], m = st.mask[node], cb = st.cbase[node];
-            uint32_t ci = st.coff[node];
-            float sy[16], su[16], sv[16];
-            sy[1] = gA[3 * j];
-            su[1] = gA[3 * j + 1];
-            sv[1] = gA[3 * j + 2];
-#pragma unroll
-            for (int i = 1; i < 8; ++i) {
-                const float2 t = st.ab[node * 7 + (i - 1)];
-                float hy = 0.f, hu = 0.f, hv = 0.f;
-                if (m & (1u << i)) {
-                    hy = cy[ci];
-                    hu = cu[ci];
-                    hv = cv[ci];
-                    ++ci;
-                }
-                const float gy = sy[i], gu = su[i], gv = sv[i];
-                const float nbv = -t.y;
-                // [G;H] = [[a,-b],[b,a]] [g;h]   (InvertHaarTransform)
-                sy[pair0(i)] = __fadd_rn(__fmul_rn(gy, t.x), __fmul_rn(hy, nbv));
-                su[pair0(i)] = __fadd_rn(__fmul_rn(gu, t.x), __fmul_rn(hu, nbv));
-                sv[pair0(i)] = __fadd_rn(__fmul_rn(gv, t.x), __fmul_rn(hv, nbv));
-                sy[pair1(i)] = __fadd_rn(__fmul_rn(gy, t.y), __fmul_rn(hy, t.x));
-                su[pair1(i)] = __fadd_rn(__fmul_rn(gu, t.y), __fmul_rn(hu, t.x));
-                sv[pair1(i)] = __fadd_rn(__fmul_rn(gv, t.y), __fmul_rn(hv, t.x));
-            }
+            const uint32_t byte = st.occ[node], cb = st.cbase[node];
+            float oy[8], ou[8], ov[8];
+            inverse_node(st, node, cy, cu, cv, gA[3 * j], gA[3 * j + 1], gA[3 * j + 2], oy, ou, ov);
             uint32_t r = 0;
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
@@ -570,11 +625,11 @@ __global__ void __launch_bounds__(T) k_raht(const SliceWork* __restrict__ work, 
                 const uint32_t child = cb + r;
                 ++r;
                 if (!last) {
-                    gB[3 * child] = sy[8 + c];
-                    gB[3 * child + 1] = su[8 + c];
-                    gB[3 * child + 2] = sv[8 + c];
+                    gB[3 * child] = oy[c];
+                    gB[3 * child + 1] = ou[c];
+                    gB[3 * child + 2] = ov[c];
                 } else {
-                    emit_leaf(w, st, lb, child, sy[8 + c], su[8 + c], sv[8 + c], predict, o);
+                    emit_leaf(w, st, lb, child, oy[c], ou[c], ov[c], predict, o);
                 }
             }
         }
@@ -582,6 +637,344 @@ __global__ void __launch_bounds__(T) k_raht(const SliceWork* __restrict__ work, 
         float* t = gA;
         gA = gB;
         gB = t;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_raht_group: one warp per group of slices that share a slot (the frames of
+// one patch in a GoP).  All lanes walk the same tree depth first in lockstep
+// (node records are warp-wide broadcast loads, control flow is uniform); lane
+// f owns frame f's coefficients, signal and output.  The intra slice, when
+// the group has one, is lane 0, and its leaf colours reach the predictive
+// lanes by shuffle (the reference add of invert_raht_octree.cc:304-308).
+
+__device__ __forceinline__ void group_emit(const SliceWork& w, bool act, bool intra_lane, bool ref_lane0, const StateView& st,
+                                           size_t lb, uint32_t leaf, float y, float u, float v, const OutPtrs& o) {
+    float ry, ru, rv;
+    if (ref_lane0) {  // lane 0 holds the intra colours of this leaf
+        ry = __shfl_sync(0xffffffffu, y, 0);
+        ru = __shfl_sync(0xffffffffu, u, 0);
+        rv = __shfl_sync(0xffffffffu, v, 0);
+    } else {
+        const float* r = st.ref + (lb + leaf) * 3;
+        ry = r[0];
+        ru = r[1];
+        rv = r[2];
+    }
+    if (!act) return;
+    if (intra_lane) {
+        float* r = st.ref + (lb + leaf) * 3;
+        r[0] = y;
+        r[1] = u;
+        r[2] = v;
+    } else {
+        y = __fadd_rn(y, ry);
+        u = __fadd_rn(u, ru);
+        v = __fadd_rn(v, rv);
+    }
+    const float* p = st.xyz + (lb + leaf) * 3;
+    const float x0 = p[0], y0 = p[1], z0 = p[2];
+    const float* m = w.mv;
+    const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
+    const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
+    const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
+    const float du = __fsub_rn(u, 128.0f), dv = __fsub_rn(v, 128.0f);
+    const float R = __fadd_rn(y, __fmul_rn(1.4020f, dv));
+    const float G = __fsub_rn(__fsub_rn(y, __fmul_rn(0.3441f, du)), __fmul_rn(0.7141f, dv));
+    const float B = __fadd_rn(y, __fmul_rn(1.7720f, du));
+    const uint64_t oi = w.out_off + leaf;
+    if (o.xyz) {
+        o.xyz[oi * 3 + 0] = X;
+        o.xyz[oi * 3 + 1] = Y;
+        o.xyz[oi * 3 + 2] = Z;
+    }
+    if (o.rgb) {
+        o.rgb[oi * 3 + 0] = to_u8(R);
+        o.rgb[oi * 3 + 1] = to_u8(G);
+        o.rgb[oi * 3 + 2] = to_u8(B);
+    }
+    if (o.p24) {
+        float* q = o.p24 + oi * 6;
+        const bool white = w.n < 10;
+        q[0] = X;
+        q[1] = Y;
+        q[2] = Z;
+        q[3] = white ? 1.0f : __fdiv_rn(R, 255.0f);
+        q[4] = white ? 1.0f : __fdiv_rn(G, 255.0f);
+        q[5] = white ? 1.0f : __fdiv_rn(B, 255.0f);
+    }
+}
+
+// inverse_node for a lane that may be inactive (no coefficient loads then)
+__device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool act, const float* cy, const float* cu,
+                                          const float* cv, float gy, float gu, float gv, float (&oy)[8], float (&ou)[8],
+                                          float (&ov)[8]) {
+    const uint32_t m = __ldg(st.mask + node);
+    uint32_t ci = __ldg(st.coff + node);
+    const float2* ab = st.ab + node * 7;
+    float sy[8], su[8], sv[8];
+    sy[1] = gy;
+    su[1] = gu;
+    sv[1] = gv;
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+        const float2 t = __ldg(ab + (i - 1));
+        float hy = 0.f, hu = 0.f, hv = 0.f;
+        if (m & (1u << i)) {
+            if (act) {
+                hy = __ldg(cy + ci);
+                hu = __ldg(cu + ci);
+                hv = __ldg(cv + ci);
+            }
+            ++ci;
+        }
+        const float ay = sy[i], au = su[i], av = sv[i];
+        const float nbv = -t.y;
+        const float Gy = __fadd_rn(__fmul_rn(ay, t.x), __fmul_rn(hy, nbv));
+        const float Gu = __fadd_rn(__fmul_rn(au, t.x), __fmul_rn(hu, nbv));
+        const float Gv = __fadd_rn(__fmul_rn(av, t.x), __fmul_rn(hv, nbv));
+        const float Hy = __fadd_rn(__fmul_rn(ay, t.y), __fmul_rn(hy, t.x));
+        const float Hu = __fadd_rn(__fmul_rn(au, t.y), __fmul_rn(hu, t.x));
+        const float Hv = __fadd_rn(__fmul_rn(av, t.y), __fmul_rn(hv, t.x));
+        if (pair0(i) < 8) {
+            sy[pair0(i)] = Gy; su[pair0(i)] = Gu; sv[pair0(i)] = Gv;
+            sy[pair1(i)] = Hy; su[pair1(i)] = Hu; sv[pair1(i)] = Hv;
+        } else {
+            oy[pair0(i) - 8] = Gy; ou[pair0(i) - 8] = Gu; ov[pair0(i) - 8] = Gv;
+            oy[pair1(i) - 8] = Hy; ou[pair1(i) - 8] = Hu; ov[pair1(i) - 8] = Hv;
+        }
+    }
+}
+
+
+// k_raht_group: persistent CTAs; each takes the next group of slices that
+// share a slot (the frames of one patch) from a queue.  Its 8 warps split the
+// nodes of each level; lane f of every warp owns frame f (same control flow
+// in all lanes, node records are broadcast loads).  The level signal lives in
+// the CTA's own scratch region as [node][lane][yuv], so warp accesses are
+// contiguous.  The intra slice, when the group has one, is lane 0 and hands
+// its leaf colours to the predictive lanes by shuffle.  The last level runs
+// in chunks of 8 nodes whose leaves are consecutive: each chunk's finished
+// points are staged in shared memory and written per frame as contiguous,
+// coalesced runs.
+constexpr int kGrpWarps = 8;
+constexpr int kStageLeaves = 8 * kGrpWarps;  // leaves of 8 nodes at most
+
+struct GroupStage {
+    float x[32][kStageLeaves], y[32][kStageLeaves], z[32][kStageLeaves];
+    uint32_t rgb[32][kStageLeaves];
+    float fr[32][kStageLeaves], fg[32][kStageLeaves], fb[32][kStageLeaves];  // points24 colours
+};
+
+__global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* __restrict__ work,
+                                                               const GroupDesc* __restrict__ groups, int ngroups,
+                                                               const int32_t* __restrict__ items, StateView st,
+                                                               const float* __restrict__ coef,
+                                                               const int32_t* __restrict__ tstatus,
+                                                               const int32_t* __restrict__ rstatus,
+                                                               int32_t* __restrict__ fstatus, OutPtrs o,
+                                                               float* __restrict__ scratch, uint64_t scratch_floats,
+                                                               int* __restrict__ counter) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    GroupStage& sg = *reinterpret_cast<GroupStage*>(s_raw);
+    __shared__ int s_g, s_H, s_ls[kMaxLevels + 1];
+    __shared__ uint64_t s_out[32];
+    __shared__ int s_act[32], s_white[32];
+    __shared__ uint32_t s_base, s_end;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    float* const bufA = scratch + (uint64_t)blockIdx.x * scratch_floats;
+    float* const bufB = bufA + scratch_floats / 2;
+    for (;;) {
+        if (tid == 0) s_g = atomicAdd(counter, 1);
+        __syncthreads();
+        const int gi = s_g;
+        if (gi >= ngroups) break;
+        const GroupDesc G = groups[gi];
+        const bool have = lane < G.count;
+        const int item = have ? items[G.first + lane] : 0;
+        const SliceWork& w = work[item];
+        const bool intra_lane = have && G.intra && lane == 0;
+        int err = have ? slice_status(w, item, st, tstatus, rstatus) : PVVC_OK;
+        const int ierr = G.intra ? __shfl_sync(0xffffffffu, err, 0) : PVVC_OK;
+        if (ierr && !intra_lane && have && !err) err = PVVC_ERR_NO_REFERENCE;
+        const bool act = have && !err;
+        if (wid == 0) {
+            if (ierr && lane == 0) st.info[G.slot].valid = 0;  // a failed intra slice empties the slot
+            if (have) {
+                fstatus[item] = err;
+                if (o.status) o.status[w.orig] = err;
+            }
+            s_act[lane] = act;
+            s_out[lane] = act ? w.out_off : 0;
+            s_white[lane] = act && w.n < 10;
+        }
+        const bool any = __any_sync(0xffffffffu, act);  // the same in every warp
+        const bool ref_lane0 = G.intra && !ierr;
+        if (tid == 0) {
+            const SlotInfo* si = st.info + G.slot;
+            s_H = si->height;
+            for (int l = 0; l < kMaxLevels + 1; ++l) s_ls[l] = si->level_start[l];
+        }
+        __syncthreads();
+        if (any) {
+            const int H = s_H;
+            const size_t nb = (size_t)G.slot * st.max_nodes;
+            const size_t lb = (size_t)G.slot * st.max_leaves;
+            const uint32_t N = act ? w.n : 0;
+            const float* cy = coef + (act ? w.coef_off : 0);
+            const float* cu = cy + N;
+            const float* cv = cu + N;
+            const float* m = w.mv;
+            // one finished leaf of this lane's frame into the stage
+            auto finish = [&](uint32_t leaf, uint32_t slot_local, float y, float u, float v) {
+                float ry, ru, rv;
+                if (ref_lane0) {
+                    ry = __shfl_sync(0xffffffffu, y, 0);
+                    ru = __shfl_sync(0xffffffffu, u, 0);
+                    rv = __shfl_sync(0xffffffffu, v, 0);
+                } else {
+                    const float* r = st.ref + (lb + leaf) * 3;
+                    ry = __ldg(r);
+                    ru = __ldg(r + 1);
+                    rv = __ldg(r + 2);
+                }
+                if (!act) return;
+                if (intra_lane) {
+                    float* r = st.ref + (lb + leaf) * 3;
+                    r[0] = y;
+                    r[1] = u;
+                    r[2] = v;
+                } else {
+                    y = __fadd_rn(y, ry);
+                    u = __fadd_rn(u, ru);
+                    v = __fadd_rn(v, rv);
+                }
+                const float* p = st.xyz + (lb + leaf) * 3;
+                const float x0 = __ldg(p), y0 = __ldg(p + 1), z0 = __ldg(p + 2);
+                sg.x[lane][slot_local] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
+                sg.y[lane][slot_local] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
+                sg.z[lane][slot_local] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
+                const float du = __fsub_rn(u, 128.0f), dv = __fsub_rn(v, 128.0f);
+                const float R = __fadd_rn(y, __fmul_rn(1.4020f, dv));
+                const float Gc = __fsub_rn(__fsub_rn(y, __fmul_rn(0.3441f, du)), __fmul_rn(0.7141f, dv));
+                const float B = __fadd_rn(y, __fmul_rn(1.7720f, du));
+                sg.rgb[lane][slot_local] = (uint32_t)to_u8(R) | ((uint32_t)to_u8(Gc) << 8) | ((uint32_t)to_u8(B) << 16);
+                if (o.p24) {
+                    sg.fr[lane][slot_local] = __fdiv_rn(R, 255.0f);
+                    sg.fg[lane][slot_local] = __fdiv_rn(Gc, 255.0f);
+                    sg.fb[lane][slot_local] = __fdiv_rn(B, 255.0f);
+                }
+            };
+            // write the staged leaves [s_base, s_end) of every active frame
+            auto flush = [&]() {
+                const uint32_t base = s_base, cnt = s_end - s_base;
+                for (uint32_t t = tid; t < 32 * cnt; t += 32 * kGrpWarps) {
+                    const uint32_t f = t / cnt, i = t - f * cnt;
+                    if (!s_act[f]) continue;
+                    const uint64_t oi = s_out[f] + base + i;
+                    if (o.xyz) {
+                        o.xyz[oi * 3 + 0] = sg.x[f][i];
+                        o.xyz[oi * 3 + 1] = sg.y[f][i];
+                        o.xyz[oi * 3 + 2] = sg.z[f][i];
+                    }
+                    const uint32_t c = sg.rgb[f][i];
+                    if (o.rgb) {
+                        o.rgb[oi * 3 + 0] = (uint8_t)c;
+                        o.rgb[oi * 3 + 1] = (uint8_t)(c >> 8);
+                        o.rgb[oi * 3 + 2] = (uint8_t)(c >> 16);
+                    }
+                    if (o.p24) {
+                        float* q = o.p24 + oi * 6;
+                        const bool white = s_white[f];
+                        q[0] = sg.x[f][i];
+                        q[1] = sg.y[f][i];
+                        q[2] = sg.z[f][i];
+                        q[3] = white ? 1.0f : sg.fr[f][i];
+                        q[4] = white ? 1.0f : sg.fg[f][i];
+                        q[5] = white ? 1.0f : sg.fb[f][i];
+                    }
+                }
+            };
+            if (H == 1) {
+                if (wid == 0) {
+                    const float gy = act ? cy[0] : 0.f, gu = act ? cu[0] : 0.f, gv = act ? cv[0] : 0.f;
+                    finish(0, 0, gy, gu, gv);
+                }
+                if (tid == 0) {
+                    s_base = 0;
+                    s_end = 1;
+                }
+                __syncthreads();
+                flush();
+            } else {
+                float* gA = bufA;
+                float* gB = bufB;
+                if (wid == 0) {
+                    gA[lane * 3 + 0] = act ? cy[0] : 0.f;
+                    gA[lane * 3 + 1] = act ? cu[0] : 0.f;
+                    gA[lane * 3 + 2] = act ? cv[0] : 0.f;
+                }
+                __syncthreads();
+                for (int l = 0; l < H - 2; ++l) {  // internal levels above the last
+                    const int a = s_ls[l], b = s_ls[l + 1];
+                    for (int j = wid; j < b - a; j += kGrpWarps) {
+                        const size_t node = nb + a + j;
+                        const uint32_t byte = __ldg(st.occ + node), cb = __ldg(st.cbase + node);
+                        const float* g3 = gA + ((size_t)j * 32 + lane) * 3;
+                        float oy[8], ou[8], ov[8];
+                        lane_node(st, node, act, cy, cu, cv, g3[0], g3[1], g3[2], oy, ou, ov);
+                        uint32_t r = 0;
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            if (!(byte & (0x80u >> c))) continue;
+                            float* go = gB + ((size_t)(cb + r) * 32 + lane) * 3;
+                            ++r;
+                            go[0] = oy[c];
+                            go[1] = ou[c];
+                            go[2] = ov[c];
+                        }
+                    }
+                    __syncthreads();
+                    float* t = gA;
+                    gA = gB;
+                    gB = t;
+                }
+                // last internal level: chunks of 8 consecutive nodes
+                const int a = s_ls[H - 2], b = s_ls[H - 1];
+                for (int j0 = 0; j0 < b - a; j0 += kGrpWarps) {
+                    const int j = j0 + wid;
+                    const bool mine = j < b - a;
+                    uint32_t byte = 0, cb = 0;
+                    if (mine) {
+                        const size_t node = nb + a + j;
+                        byte = __ldg(st.occ + node);
+                        cb = __ldg(st.cbase + node);
+                    }
+                    if (lane == 0 && wid == 0) s_base = cb;
+                    const int lastw = min(kGrpWarps, b - a - j0) - 1;
+                    if (lane == 0 && wid == lastw) s_end = cb + __popc(byte);
+                    __syncthreads();
+                    if (mine) {
+                        const size_t node = nb + a + j;
+                        const float* g3 = gA + ((size_t)j * 32 + lane) * 3;
+                        float oy[8], ou[8], ov[8];
+                        lane_node(st, node, act, cy, cu, cv, g3[0], g3[1], g3[2], oy, ou, ov);
+                        const uint32_t base = s_base;
+                        uint32_t r = 0;
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            if (!(byte & (0x80u >> c))) continue;
+                            finish(cb + r, cb + r - base, oy[c], ou[c], ov[c]);
+                            ++r;
+                        }
+                    }
+                    __syncthreads();
+                    flush();
+                    __syncthreads();
+                }
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -604,18 +997,37 @@ cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices
     return cudaGetLastError();
 }
 
-cudaError_t launch_raht(const SliceWork* work, int first, int count, const StateView& st, const float* coef, float* fallback,
-                        const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz, uint8_t* rgb, float* p24,
-                        int32_t* status, int wcap, cudaStream_t s) {
+cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int count, const StateView& st, const float* coef,
+                              float* fallback, const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz,
+                              uint8_t* rgb, float* p24, int32_t* status, int wcap, cudaStream_t s) {
     if (count <= 0) return cudaSuccess;
     const size_t smem = 2ull * wcap * 3 * sizeof(float);
     static bool attr_set = false;
     if (!attr_set) {
-        cudaFuncSetAttribute(k_raht<kRahtThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_raht_slice<kRahtThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         attr_set = true;
     }
     OutPtrs o{xyz, rgb, p24, status};
-    k_raht<kRahtThreads><<<count, kRahtThreads, smem, s>>>(work, first, st, coef, fallback, tstatus, rstatus, fstatus, o, wcap);
+    k_raht_slice<kRahtThreads><<<count, kRahtThreads, smem, s>>>(work, list, st, coef, fallback, tstatus, rstatus, fstatus, o,
+                                                                 wcap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, int ngroups, const int32_t* items,
+                              const StateView& st, const float* coef, const int32_t* tstatus, const int32_t* rstatus,
+                              int32_t* fstatus, float* xyz, uint8_t* rgb, float* p24, int32_t* status, float* scratch,
+                              uint64_t scratch_floats, int nctas, int* counter, cudaStream_t s) {
+    if (ngroups <= 0) return cudaSuccess;
+    if (cudaMemsetAsync(counter, 0, sizeof(int), s) != cudaSuccess) return cudaGetLastError();
+    OutPtrs o{xyz, rgb, p24, status};
+    const int grid = ngroups < nctas ? ngroups : nctas;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_raht_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupStage));
+        attr_set = true;
+    }
+    k_raht_group<<<grid, 32 * kGrpWarps, sizeof(GroupStage), s>>>(work, groups, ngroups, items, st, coef, tstatus, rstatus,
+                                                                  fstatus, o, scratch, scratch_floats, counter);
     return cudaGetLastError();
 }
 

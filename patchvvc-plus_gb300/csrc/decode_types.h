@@ -48,4 +48,13 @@ struct StateView {
     int32_t nslots, max_leaves, max_nodes;
 };
 
+// A group of slices of one slot inverse-transformed by one warp (one lane
+// per slice).  When the group holds the slot's intra slice it is lane 0.
+struct GroupDesc {
+    int32_t slot;
+    int32_t first;  // into the group item list
+    int32_t count;  // <= 32
+    int32_t intra;
+};
+
 }  // namespace pvvc
