@@ -95,7 +95,10 @@ int pvvc_plan_query(const pvvc_plan* plan, uint64_t* total_points, uint64_t* wor
  * (src/cuda/render/CUDA2OpenGL.cu:37-74, include/cuda/render.cuh:42-57) and
  * the CPU path InvertRAHTOctree::SetSlice/GetPatch + the transform loop
  * (src/octree/invert_raht_octree.cc:22-120, pvvc_decompression.cc:141-150).
- *   payload      device bytes the plan's offsets index (raw, not zstd)
+ *   payload      device bytes the plan's offsets index (raw, not zstd); the
+ *                base must be 16-byte aligned and the buffer readable up to the
+ *                16-byte boundary after its last payload byte (the colour
+ *                stream is read in 16-byte blocks)
  *   xyz          device float[3*points] transformed coordinates (or NULL)
  *   rgb          device uint8[3*points] colours rounded as the CPU decoder
  *                rounds them, clamped to [0,255] (or NULL)

@@ -279,7 +279,7 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
                int32_t* status, void* ws, uint64_t ws_bytes, cudaStream_t s, void* const* events = nullptr) {
     if (!p || !st) return PVVC_ERR_ARG;
     if (p->nslices == 0) return PVVC_OK;
-    if (!payload || (reinterpret_cast<uintptr_t>(payload) & 3u)) return PVVC_ERR_ARG;
+    if (!payload || (reinterpret_cast<uintptr_t>(payload) & 15u)) return PVVC_ERR_ARG;
     if (!ws || ws_bytes < p->ws_bytes || (reinterpret_cast<uintptr_t>(ws) & 255u)) return PVVC_ERR_CAPACITY;
     if (p->max_slot >= st->v.nslots) return PVVC_ERR_ARG;
     uint8_t* w = static_cast<uint8_t*>(ws);
@@ -452,7 +452,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     }
     if (npoints_out) *npoints_out = pts;
     if (pts > cap_points || (status_host && status_cap < nsl)) return PVVC_ERR_CAPACITY;
-    if (st->h_payload.ensure(std::max<uint64_t>(bytes, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (st->h_payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     uint8_t* hp = static_cast<uint8_t*>(st->h_payload.p);
     std::vector<int32_t> slot(nsl);
     std::vector<uint8_t> type(nsl), qp(nsl);
@@ -484,7 +484,8 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     pvvc_batch_desc d{};
     int32_t first = 0;
     int rc = PVVC_OK;
-    if (st->payload.ensure(std::max<uint64_t>(bytes, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    // the decoder reads whole 16-byte blocks: pad past the last payload byte
+    if (st->payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
@@ -577,7 +578,7 @@ extern "C" int pvvc_launch_cudaProcess(int grid, int block, float* out_points24,
         if (h_csz[i] && h_col[i]) base = std::min(base, reinterpret_cast<uintptr_t>(h_col[i]));
     }
     if (base == UINTPTR_MAX) return PVVC_ERR_ARG;
-    base &= ~uintptr_t(3);
+    base &= ~uintptr_t(15);
     std::vector<int32_t> slot(n);
     std::vector<uint64_t> goff(n), coff(n), oo(n);
     for (int i = 0; i < n; ++i) {

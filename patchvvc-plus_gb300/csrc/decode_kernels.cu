@@ -275,41 +275,77 @@ __global__ void __launch_bounds__(T) k_tree(const SliceWork* __restrict__ work, 
 // peek() returns the next 32 bits with one funnel shift.  Words past the
 // payload read as zero.
 struct BitReader {
-    const uint32_t* p;     // next word to load into nx
-    const uint32_t* end;   // one past the last word holding payload bytes
-    uint32_t hi, lo, nx;
-    uint32_t o;            // bits of hi already consumed (0..31)
+    // Payload words W[0..] (big-endian), read as 16-byte blocks: `cur` holds the
+    // block words are taken from, `nxt` the following block, loaded when `cur`
+    // became current -- four words (about thirty codes) before it is needed,
+    // so taking a word never waits on memory.  Blocks past the payload read
+    // as zero.  The window is hi:lo with `o` bits of hi consumed.
+    const uint4* p;      // next block to load
+    const uint4* end;    // one past the last block holding payload bytes
+    uint4 cur, nxt;
+    uint32_t k;          // index in cur of the next word to enter the window
+    uint32_t hi, lo;
+    uint32_t o;
+    uint32_t taken;      // words that have entered the window
 
-    __device__ __forceinline__ uint32_t load() {
-        const uint32_t v = p < end ? __byte_perm(__ldg(p), 0, 0x0123) : 0u;
+    __device__ __forceinline__ uint4 load() {
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (p < end) v = __ldg(p);
         ++p;
         return v;
     }
-    __device__ __forceinline__ void init(const uint32_t* first_word, const uint32_t* last, uint32_t skip_bits) {
-        p = first_word;
-        end = last;
-        hi = load();
-        lo = load();
-        nx = load();
-        o = skip_bits;
+    __device__ __forceinline__ uint32_t word(uint32_t i) const {
+        const uint32_t v = i == 0 ? cur.x : i == 1 ? cur.y : i == 2 ? cur.z : cur.w;
+        return __byte_perm(v, 0, 0x0123);
+    }
+    __device__ __forceinline__ uint32_t take() {  // next word of the stream
+        const uint32_t v = word(k);
+        ++taken;
+        if (++k == 4) {
+            k = 0;
+            cur = nxt;
+            nxt = load();
+        }
+        return v;
+    }
+    __device__ __forceinline__ void init(const uint8_t* payload, uint64_t off, uint32_t nbytes) {
+        p = reinterpret_cast<const uint4*>(payload + (off & ~15ull));
+        end = reinterpret_cast<const uint4*>(payload + ((off + nbytes + 15) & ~15ull));
+        cur = load();
+        nxt = load();
+        k = 0;
+        taken = 0;
+        hi = take();
+        lo = take();
+        o = (uint32_t)(off & 15) * 8;
+        while (o >= 32) {
+            o -= 32;
+            hi = lo;
+            lo = take();
+        }
     }
     __device__ __forceinline__ uint32_t peek() const { return __funnelshift_l(lo, hi, o); }
-    __device__ __forceinline__ void consume(uint32_t k) {  // k <= 32
-        o += k;
+    __device__ __forceinline__ void consume(uint32_t n) {  // n <= 32
+        o += n;
         if (o >= 32) {
             o -= 32;
             hi = lo;
-            lo = nx;
-            nx = load();
+            lo = take();
         }
+    }
+    // payload bits consumed (words before hi, plus o, minus the leading skip)
+    __device__ __forceinline__ int64_t consumed(uint64_t off) const {
+        return ((int64_t)taken - 2) * 32 + (int64_t)o - (int64_t)(off & 15) * 8;
     }
 };
 
 constexpr uint32_t kRlU0 = 3, kRlU1 = 2, kRlD0 = 1, kRlD1 = 1, kRlMaxRP = 32 * 4;
 
 // k_rlgr: one thread per slice.  The coefficient planes are zeroed before the
-// launch, so a run of zeros only advances the output position; symbol n of a
-// plane goes to coefficient N-1-j (the stream is reversed).
+// launch, so a run of zeros only moves the output position; symbol j of a
+// plane goes to coefficient N-1-j (the stream is reversed).  The loop keeps
+// 32-bit state only: `dst` walks down the current plane, `rem` counts the
+// plane's symbols still to come, `left` all symbols still to come.
 __global__ void __launch_bounds__(128) k_rlgr(const SliceWork* __restrict__ work, const int32_t* __restrict__ order,
                                               int nslices, const uint8_t* __restrict__ payload, float* __restrict__ coef,
                                               int32_t* __restrict__ rstatus) {
@@ -318,32 +354,26 @@ __global__ void __launch_bounds__(128) k_rlgr(const SliceWork* __restrict__ work
     const int item = order[t];
     const SliceWork& wk = work[item];
     const uint32_t N = wk.n;
-    const uint32_t total = 3u * N;
     const int32_t qp = wk.qp;
-    if (total == 0) {
+    if (N == 0) {
         rstatus[item] = PVVC_OK;
         return;
     }
     const uint64_t off = wk.col_off;
-    const uint32_t* w0 = reinterpret_cast<const uint32_t*>(payload + (off & ~3ull));
-    const uint32_t* wend = reinterpret_cast<const uint32_t*>(payload + ((off + wk.csz + 3) & ~3ull));
     BitReader br;
-    br.init(w0, wend, (uint32_t)(off & 3) * 8);
-    float* const base = coef + wk.coef_off;
-
+    br.init(payload, off, wk.csz);
+    float* dst = coef + wk.coef_off + N - 1;  // coefficient of the next symbol
+    uint32_t rem = N;                         // symbols left in the current plane
+    uint32_t left = 3u * N;                   // symbols left in the slice
     uint32_t kP = 0, kRP = 8;
-    uint32_t n = 0;       // symbols decoded
-    uint32_t pl = 0;      // plane of symbol n
-    uint32_t j = 0;       // position of symbol n within its plane
     int err = PVVC_OK;
-    while (n < total) {
-        uint32_t k = kP >> 2;
-        bool after_run = false;
-        if (k) {
+    for (;;) {
+        uint32_t after_run = 0;
+        if (kP >= 4) {
             // run mode (entropy_codec.cc:226-257): every leading '1' stands for
             // 2^k zeros and raises kP by U1 (k grows every second one); then a
             // '0' and k bits complete the run
-            uint32_t m = 0, c;
+            uint32_t k = kP >> 2, m = 0, c;
             int guard = 0;
             do {
                 c = __clz(~br.peek());  // leading ones, 32 when all are ones
@@ -361,78 +391,71 @@ __global__ void __launch_bounds__(128) k_rlgr(const SliceWork* __restrict__ work
             }
             m += br.peek() >> (32 - k);
             br.consume(k);
-            const uint32_t z = m < total - n ? m : total - n;
-            n += z;
-            j += z;
-            while (j >= N && pl < 3) {  // the run may cross plane boundaries
-                j -= N;
-                ++pl;
+            // skip m zeros (they may cross plane boundaries)
+            uint32_t z = m < left ? m : left;
+            left -= z;
+            while (z >= rem && rem) {
+                z -= rem;
+                dst += 2 * N - rem;  // to the top of the next plane
+                rem = N;
             }
-            if (n >= total) break;
-            after_run = true;
+            dst -= z;
+            rem -= z;
+            if (left == 0) break;
+            after_run = 1;
         }
         // Golomb-Rice symbol (GRRead, entropy_codec.cc:196-205)
         const uint32_t kR = kRP >> 2;
         const uint32_t v = br.peek();
         const uint32_t q = __clz(~v);
-        uint32_t lo32, hi32 = 0;  // u = hi32:lo32
-        uint32_t pq;              // u >> kR, which drives kRP
-        if (q < 32) {
-            uint32_t r;
-            if (q + 1 + kR <= 32) {
-                r = kR ? (v << (q + 1)) >> (32 - kR) : 0u;
-                br.consume(q + 1 + kR);
-            } else {
-                br.consume(q + 1);
-                r = kR == 32 ? br.peek() : (br.peek() >> (32 - kR));
-                br.consume(kR);
-            }
-            // (q << kR) | r, q < 32 and kR <= 32
-            if (kR < 32) {
-                lo32 = (q << kR) | r;
-                hi32 = kR ? (q >> (32 - kR)) : 0u;
-            } else {
-                lo32 = r;
-                hi32 = q;
-            }
+        uint32_t u, pq;
+        bool wide = false;  // u does not fit 32 bits
+        uint64_t uw = 0;
+        if (q + 1 + kR <= 32) {  // the common case: one peek holds the whole code
+            u = (q << kR) | (kR ? (v << (q + 1)) >> (32 - kR) : 0u);
+            br.consume(q + 1 + kR);
+            pq = q;
+        } else if (q < 32) {
+            br.consume(q + 1);
+            const uint32_t r = kR == 32 ? br.peek() : (br.peek() >> (32 - kR));
+            br.consume(kR);
+            uw = ((uint64_t)q << kR) | r;
+            wide = (uw >> 32) != 0;
+            u = (uint32_t)uw;
             pq = q;
         } else {  // 32 ones: a raw 32-bit value follows
             br.consume(32);
-            lo32 = br.peek();
+            u = br.peek();
             br.consume(32);
-            const uint32_t t2 = kR >= 32 ? 0u : (lo32 >> kR);
+            const uint32_t t2 = kR >= 32 ? 0u : (u >> kR);
             pq = t2 > kRlMaxRP ? kRlMaxRP : t2;
         }
         // adaptation (entropy_codec.cc:245-281)
         kRP = pq ? min(kRP + pq - 1, kRlMaxRP) : (kRP < 2 ? 0u : kRP - 2);
-        const bool uz = (lo32 | hi32) == 0;
-        if (after_run) {
-            kP = kP < kRlD1 ? 0u : kP - kRlD1;
+        if (after_run) kP = kP ? kP - kRlD1 : 0u;
+        else kP = (u | (uint32_t)wide) ? (kP ? kP - kRlD0 : 0u) : kP + kRlU0;
+        // Unsign2Sign(u + after_run) * qp, stored unless zero
+        if (!wide && u < (1u << 23)) {
+            const uint32_t zz = u + after_run;
+            const int32_t sym = (int32_t)(zz >> 1) ^ -(int32_t)(zz & 1);
+            if (sym) *dst = __int2float_rn(sym * qp);
         } else {
-            kP = uz ? kP + kRlU0 : (kP < kRlD0 ? 0u : kP - kRlD0);
+            const uint64_t zz = (wide ? uw : (uint64_t)u) + after_run;
+            const long long sym = (long long)(zz >> 1) ^ -(long long)(zz & 1);
+            *dst = __ll2float_rn(sym * (long long)qp);
         }
-        // Unsign2Sign(u) or Unsign2Sign(u + 1) after a run, times qp
-        float val;
-        if (hi32 == 0 && lo32 < (1u << 23)) {
-            const int32_t zz = (int32_t)lo32 + (after_run ? 1 : 0);
-            const int32_t sym = (zz & 1) ? -(zz >> 1) - 1 : (zz >> 1);
-            val = __int2float_rn(sym * qp);  // |sym*qp| < 2^31: exact product, same rounding as int64
+        --left;
+        if (--rem == 0) {
+            dst += 2 * N - 1;
+            rem = N;
         } else {
-            const uint64_t zz = (((uint64_t)hi32 << 32) | lo32) + (after_run ? 1u : 0u);
-            const long long sym = (zz & 1) ? -(long long)(zz >> 1) - 1 : (long long)(zz >> 1);
-            val = __ll2float_rn(sym * (long long)qp);
+            --dst;
         }
-        if (val != 0.0f) base[pl * N + (N - 1 - j)] = val;  // zero symbols keep the cleared value
-        ++n;
-        if (++j == N) {
-            j = 0;
-            ++pl;
-        }
+        if (left == 0) break;
     }
     // bits consumed vs the payload (the reference reads past it, which is undefined)
     if (!err) {
-        const int64_t consumed = ((int64_t)(br.p - w0) - 3) * 32 + (int64_t)br.o - (int64_t)(off & 3) * 8;
-        if (consumed > 8ll * wk.csz) err = PVVC_ERR_OVERRUN;
+        if (br.consumed(off) > 8ll * wk.csz) err = PVVC_ERR_OVERRUN;
     }
     rstatus[item] = err;
 }

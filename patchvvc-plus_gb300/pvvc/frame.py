@@ -129,7 +129,7 @@ def pack_frames(frames: list[Frame], slot_base: int = 0) -> Batch:
     slot of a slice is slot_base + its patch index."""
     nsl = sum(f.n for f in frames)
     tot = sum(_align(len(g)) + _align(len(c)) for f in frames for g, c in zip(f.geometry, f.color))
-    payload = np.zeros(max(tot, 4), np.uint8)
+    payload = np.zeros(tot + 16, np.uint8)  # the decoder reads whole 16-byte blocks
     slot = np.empty(nsl, np.int32); typ = np.empty(nsl, np.uint8); size = np.empty(nsl, np.uint32)
     qp = np.empty(nsl, np.uint8); mv = np.empty((nsl, 16), np.float32)
     goff = np.zeros(nsl, np.uint64); gsz = np.zeros(nsl, np.uint32)
