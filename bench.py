@@ -270,7 +270,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         kt += np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(4)])
     kt /= 3
-    names = ["k_tree", "k_rlgr", "k_raht(intra)", "k_raht(predictive)"]
+    names = ["k_tree", "memset+k_rlgr", "k_raht phase A", "k_raht phase B"]
 
     out = None
     if rank == 0:
@@ -297,7 +297,7 @@ def run_ours(args):
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
-               "clocks": clk.summary(), "gpu_launches": 4 * args.steps, "points_per_step": P * world, "icp": icp}
+               "clocks": clk.summary(), "gpu_launches": 3 * args.steps, "points_per_step": P * world, "icp": icp}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()

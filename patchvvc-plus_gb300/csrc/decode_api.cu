@@ -27,7 +27,7 @@ cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, in
                               uint64_t scratch_floats, int nctas, int* counter, cudaStream_t s);
 
 // persistent CTAs of the group kernel per SM, and the SM count (queried once)
-constexpr int kGroupCtasPerSm = 2;
+constexpr int kGroupCtasPerSm = 3;
 int sm_count() {
     static int n = 0;
     if (!n) {
@@ -175,7 +175,6 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
     for (int i : intra) fill(q++, i);
     for (int i : pred) fill(q++, i);
     p->total_points = pts;
-    p->coef_floats = coef;
     // inverse-RAHT schedule: slices grouped by slot (largest slots first)
     {
         std::vector<std::vector<int32_t>> per;  // queue indices per slot, in queue order
@@ -223,6 +222,28 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
         p->idx.insert(p->idx.end(), lb.begin(), lb.end());
         p->nlist_a = (int32_t)la.size();
         p->nlist_b = (int32_t)lb.size();
+        // coefficient regions: a group shares one frame-interleaved region
+        // (stride 32), every other slice owns contiguous planes
+        uint64_t c = 0;
+        for (const auto& g : p->groups) {
+            const uint32_t gn = p->work[p->idx[g.first]].n;
+            for (int l = 0; l < g.count; ++l) {
+                SliceWork& w = p->work[p->idx[g.first + l]];
+                w.coef_off = c;
+                w.coef_stride = 32;
+                w.coef_lane = (uint32_t)l;
+            }
+            c += 3ull * gn * 32;
+        }
+        for (int li = p->list_a_off; li < (int)p->idx.size(); ++li) {
+            SliceWork& w = p->work[p->idx[li]];
+            w.coef_off = c;
+            w.coef_stride = 1;
+            w.coef_lane = 0;
+            c += 3ull * w.n;
+        }
+        coef = c;
+        p->coef_floats = coef;
     }
     // RLGR order: all slices by size, so that a warp decodes similar lengths
     p->order.resize(n);

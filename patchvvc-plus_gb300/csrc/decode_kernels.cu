@@ -362,7 +362,8 @@ __global__ void __launch_bounds__(128) k_rlgr(const SliceWork* __restrict__ work
     const uint64_t off = wk.col_off;
     BitReader br;
     br.init(payload, off, wk.csz);
-    float* dst = coef + wk.coef_off + N - 1;  // coefficient of the next symbol
+    const uint32_t cs = wk.coef_stride;
+    float* dst = coef + wk.coef_off + (uint64_t)(N - 1) * cs + wk.coef_lane;  // coefficient of the next symbol
     uint32_t rem = N;                         // symbols left in the current plane
     uint32_t left = 3u * N;                   // symbols left in the slice
     uint32_t kP = 0, kRP = 8;
@@ -396,10 +397,10 @@ __global__ void __launch_bounds__(128) k_rlgr(const SliceWork* __restrict__ work
             left -= z;
             while (z >= rem && rem) {
                 z -= rem;
-                dst += 2 * N - rem;  // to the top of the next plane
+                dst += (int64_t)(2 * N - rem) * cs;  // to the top of the next plane
                 rem = N;
             }
-            dst -= z;
+            dst -= (int64_t)z * cs;
             rem -= z;
             if (left == 0) break;
             after_run = 1;
@@ -446,10 +447,10 @@ __global__ void __launch_bounds__(128) k_rlgr(const SliceWork* __restrict__ work
         }
         --left;
         if (--rem == 0) {
-            dst += 2 * N - 1;
+            dst += (int64_t)(2 * N - 1) * cs;
             rem = N;
         } else {
-            --dst;
+            dst -= cs;
         }
         if (left == 0) break;
     }
@@ -729,6 +730,7 @@ __device__ __forceinline__ void group_emit(const SliceWork& w, bool act, bool in
 }
 
 // inverse_node for a lane that may be inactive (no coefficient loads then)
+template <int S>  // coefficient stride (32 in frame-interleaved group regions)
 __device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool act, const float* cy, const float* cu,
                                           const float* cv, float gy, float gu, float gv, float (&oy)[8], float (&ou)[8],
                                           float (&ov)[8]) {
@@ -745,9 +747,9 @@ __device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool
         float hy = 0.f, hu = 0.f, hv = 0.f;
         if (m & (1u << i)) {
             if (act) {
-                hy = __ldg(cy + ci);
-                hu = __ldg(cu + ci);
-                hv = __ldg(cv + ci);
+                hy = __ldg(cy + (size_t)ci * S);
+                hu = __ldg(cu + (size_t)ci * S);
+                hv = __ldg(cv + (size_t)ci * S);
             }
             ++ci;
         }
@@ -844,9 +846,10 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
             const size_t nb = (size_t)G.slot * st.max_nodes;
             const size_t lb = (size_t)G.slot * st.max_leaves;
             const uint32_t N = act ? w.n : 0;
-            const float* cy = coef + (act ? w.coef_off : 0);
-            const float* cu = cy + N;
-            const float* cv = cu + N;
+            // frame-interleaved region: coefficient i of plane p at (p*N + i)*32 + lane
+            const float* cy = coef + (act ? w.coef_off + lane : 0);
+            const float* cu = cy + (size_t)N * 32;
+            const float* cv = cu + (size_t)N * 32;
             const float* m = w.mv;
             // one finished leaf of this lane's frame into the stage
             auto finish = [&](uint32_t leaf, uint32_t slot_local, float y, float u, float v) {
@@ -945,7 +948,7 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
                         const uint32_t byte = __ldg(st.occ + node), cb = __ldg(st.cbase + node);
                         const float* g3 = gA + ((size_t)j * 32 + lane) * 3;
                         float oy[8], ou[8], ov[8];
-                        lane_node(st, node, act, cy, cu, cv, g3[0], g3[1], g3[2], oy, ou, ov);
+                        lane_node<32>(st, node, act, cy, cu, cv, g3[0], g3[1], g3[2], oy, ou, ov);
                         uint32_t r = 0;
 #pragma unroll
                         for (int c = 0; c < 8; ++c) {
@@ -981,7 +984,7 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
                         const size_t node = nb + a + j;
                         const float* g3 = gA + ((size_t)j * 32 + lane) * 3;
                         float oy[8], ou[8], ov[8];
-                        lane_node(st, node, act, cy, cu, cv, g3[0], g3[1], g3[2], oy, ou, ov);
+                        lane_node<32>(st, node, act, cy, cu, cv, g3[0], g3[1], g3[2], oy, ou, ov);
                         const uint32_t base = s_base;
                         uint32_t r = 0;
 #pragma unroll

@@ -20,6 +20,10 @@ struct SliceWork {
     int32_t slot;       // state slot
     int32_t orig;       // index in the caller's arrays (status)
     uint8_t type, qp, pad0, pad1;
+    // coefficient (plane p, index i) lives at coef_off + (p*n + i)*coef_stride + coef_lane:
+    // slices decoded by one warp share a frame-interleaved region (stride 32,
+    // lane = position in the group), the others own contiguous planes
+    uint32_t coef_stride, coef_lane;
     float mv[12];       // first three rows of the row-major 4x4
 };
 
