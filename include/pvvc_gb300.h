@@ -89,6 +89,38 @@ int pvvc_plan_destroy(pvvc_plan* plan);
 /* total output points, device workspace bytes pvvc_decode needs */
 int pvvc_plan_query(const pvvc_plan* plan, uint64_t* total_points, uint64_t* workspace_bytes);
 
+/* Launch shapes of a plan.  A zero field takes the built-in default.  No
+ * reference counterpart: the reference launches one thread per slice
+ * (src/cuda/render/render.cc:269-301, block = 1). */
+typedef struct {
+    int32_t group_ctas_per_sm; /* persistent CTAs of the grouped inverse-RAHT kernel per SM: 1..3 (default 3)   */
+    int32_t min_group;         /* a slot's predictive slices share one warp when at least this many: 1..32 (4) */
+    int32_t rlgr_block;        /* threads per CTA of the RLGR kernel: 32, 64, 128 or 256 (default 128)         */
+} pvvc_tune;
+int pvvc_plan_create_tuned(const pvvc_batch_desc* desc, const pvvc_tune* tune, pvvc_plan** out);
+
+/* What a plan launches: counts of its work items and of the kernels one
+ * pvvc_decode of it runs (every kernel with an empty grid is skipped). */
+typedef struct {
+    int32_t nslices, nintra;
+    int32_t groups_a, groups_b;   /* warp groups of the two inverse-RAHT phases    */
+    int32_t singles_a, singles_b; /* slices inverse-transformed by a CTA of their own */
+    int32_t kernels;              /* kernel launches per decode                    */
+    int32_t group_ctas;           /* grid of the grouped inverse-RAHT kernel        */
+    pvvc_tune tune;               /* the shapes in force (defaults resolved)         */
+} pvvc_plan_info;
+int pvvc_plan_info_get(const pvvc_plan* plan, pvvc_plan_info* info);
+
+/* Autotuner: plans `desc` under a set of candidate launch shapes (a
+ * coordinate search over the three pvvc_tune fields, starting at the
+ * defaults), decodes the batch `reps` times under each with CUDA events on
+ * `stream`, and returns the fastest shapes and their mean device time.  The
+ * decodes run for real: afterwards `st` holds what one pvvc_decode of the
+ * batch leaves.  It allocates its own workspace and outputs, and
+ * synchronises `stream`.  `payload` as for pvvc_decode. */
+int pvvc_plan_autotune(const pvvc_batch_desc* desc, pvvc_state* st, const uint8_t* payload, int32_t reps, void* stream,
+                       pvvc_tune* best, float* best_ms);
+
 /* Decode one planned batch: RLGR -> dequantise -> (intra: occupancy tree
  * expansion) -> inverse RAHT -> (+ reference colours) -> YUV->RGB -> rigid
  * transform.  Replaces launch_cudaProcess / processCUDA
@@ -118,6 +150,19 @@ int pvvc_decode(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, f
 int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
                          float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, void* stream,
                          void* const* events);
+
+/* One planned decode captured in a CUDA graph: the arguments of pvvc_decode
+ * are bound at creation, and each pvvc_graph_launch replays the whole decode
+ * (its memsets and kernels) as one graph launch on `stream`.  The plan, the
+ * state and every buffer must outlive the graph; the payload buffer's
+ * CONTENTS may change between launches as long as its layout is the plan's
+ * (e.g. the next GoP of a stream with identical slice sizes).  Creation
+ * captures on a private stream and does not touch the caller's streams. */
+typedef struct pvvc_graph pvvc_graph;
+int pvvc_graph_create(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
+                      float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, pvvc_graph** out);
+int pvvc_graph_launch(pvvc_graph* graph, void* stream);
+int pvvc_graph_destroy(pvvc_graph* graph);
 
 /* ---- end-to-end host call ------------------------------------------------
  * Decode whole .frame files held in HOST memory (the bytes of one or more
@@ -215,6 +260,77 @@ int pvvc_icp_batch_noalloc(int32_t npairs, const float* src_xyz, const uint32_t*
 int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
                          const uint32_t* tgt_off, const float* T, float* mse_out, void* workspace,
                          uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream);
+
+/* ---- playback server -----------------------------------------------------
+ * Decodes .frame requests of many concurrent playback streams with
+ * continuous batching.  It replaces the reference client's single decode
+ * thread (src/cuda/common/manager.cc:230-270: one stream, one frame per
+ * launch_cudaProcess, synchronised after each).  A worker thread takes every
+ * request that has arrived, across streams, packs it into one batch (frames
+ * of one stream in submission order; a stream's next intra frame waits for
+ * the next batch), uploads it on a copy stream while the previous batch
+ * decodes, and enqueues one planned decode per batch on a compute stream;
+ * a completion thread stamps each frame when its batch's event fires.
+ * Per-patch state (trees, reference colours) and decoded frames stay in HBM.
+ *
+ * Memory: at creation the server reserves, within hbm_budget_bytes, the
+ * output ring, `inflight` batch workspaces, and a pool of patch-state slots
+ * with the rest.  A stream is admitted (pvvc_server_open_stream) only when a
+ * contiguous range of `nslots` free slots exists: PVVC_ERR_CAPACITY
+ * otherwise, and closing a stream frees its range.  Timestamps are
+ * microseconds on the server's steady clock. */
+typedef struct {
+    uint64_t hbm_budget_bytes;   /* device memory the server may reserve in total                 */
+    int32_t max_leaves;          /* points per patch slot (default 8192)                          */
+    int32_t max_nodes;           /* internal octree nodes per slot (default 2 * max_leaves)         */
+    uint64_t max_batch_points;   /* points of one batch (default 32M)                             */
+    uint64_t ring_points;        /* decoded points held until released (default 256M)             */
+    int32_t inflight;            /* batches queued on the GPU at once: 1..4 (default 2)           */
+    int32_t max_batch_frames;    /* frames of one batch (default 4096)                            */
+    pvvc_tune tune;              /* launch shapes of every batch                                  */
+} pvvc_server_config;
+
+typedef struct {
+    uint64_t tag;          /* the caller's tag of the request                          */
+    uint64_t handle;       /* pass to pvvc_server_release / pvvc_server_read           */
+    int32_t stream_id;
+    int32_t status;        /* PVVC_OK or the status of the frame's first failed slice  */
+    uint64_t npoints;
+    const float* xyz;      /* device float[3*npoints]: valid until released           */
+    const uint8_t* rgb;    /* device uint8[3*npoints]                                   */
+    double submit_us;      /* request accepted                                          */
+    double launch_us;      /* its batch enqueued on the GPU                             */
+    double done_us;        /* its batch finished on the GPU                             */
+    int32_t batch_id;
+    int32_t batch_frames;  /* frames in that batch                                      */
+} pvvc_completion;
+
+typedef struct {
+    uint64_t batches, frames, points, slices;
+    uint64_t slots_total, slots_free, streams_open;
+    uint64_t reserved_bytes;    /* device memory the server holds                       */
+    double gpu_busy_us;         /* sum of batch device times (CUDA events)              */
+} pvvc_server_stats;
+
+typedef struct pvvc_server pvvc_server;
+int pvvc_server_create(const pvvc_server_config* cfg, pvvc_server** out);
+/* Waits for the batches already on the GPU, drops frames still queued, frees everything. */
+int pvvc_server_destroy(pvvc_server* s);
+int pvvc_server_open_stream(pvvc_server* s, int32_t nslots, int32_t* stream_id);
+/* Frees the stream's slots once its submitted frames have completed. */
+int pvvc_server_close_stream(pvvc_server* s, int32_t stream_id);
+/* Queue one .frame of a stream (host bytes that the caller keeps unchanged
+ * until the frame's completion is polled).  The frame header is parsed here;
+ * a malformed frame or a patch index >= the stream's nslots is refused with
+ * PVVC_ERR_FORMAT / PVVC_ERR_ARG and not queued. */
+int pvvc_server_submit(pvvc_server* s, int32_t stream_id, const uint8_t* frame_bytes, uint64_t len, uint64_t tag);
+/* Up to `cap` completions in completion order, waiting up to wait_us for the first. */
+int pvvc_server_poll(pvvc_server* s, pvvc_completion* out, int32_t cap, int32_t* n, int32_t wait_us);
+/* Copy a completed frame to host memory (synchronous). */
+int pvvc_server_read(pvvc_server* s, uint64_t handle, float* xyz_host, uint8_t* rgb_host);
+/* Return a completed frame's output space to the ring. */
+int pvvc_server_release(pvvc_server* s, uint64_t handle);
+int pvvc_server_stats_get(pvvc_server* s, pvvc_server_stats* out);
 
 #ifdef __cplusplus
 }

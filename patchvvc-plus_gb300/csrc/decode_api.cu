@@ -10,111 +10,28 @@
 #include <vector>
 
 #include "../host/bitstream.h"
-#include "decode_types.h"
-#include "pvvc_gb300.h"
+#include "decode_internal.h"
 
 namespace pvvc {
-cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payload, const StateView& st, int32_t* tstatus,
-                        cudaStream_t s);
-cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
-                        int32_t* rstatus, cudaStream_t s);
-cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int count, const StateView& st, const float* coef,
-                              float* fallback, const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz,
-                              uint8_t* rgb, float* p24, int32_t* status, int wcap, cudaStream_t s);
-cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, int ngroups, const int32_t* items,
-                              const StateView& st, const float* coef, const int32_t* tstatus, const int32_t* rstatus,
-                              int32_t* fstatus, float* xyz, uint8_t* rgb, float* p24, int32_t* status, float* scratch,
-                              uint64_t scratch_floats, int nctas, int* counter, cudaStream_t s);
 
-// persistent CTAs of the group kernel per SM, and the SM count (queried once)
-constexpr int kGroupCtasPerSm = 3;
-int sm_count() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 132;
+// zero fields -> defaults; out-of-range fields -> PVVC_ERR_ARG
+int resolve_tune(const pvvc_tune* in, pvvc_tune* out) {
+    pvvc_tune t{kGroupCtasPerSm, kMinGroup, kRlgrBlock};
+    if (in) {
+        if (in->group_ctas_per_sm) t.group_ctas_per_sm = in->group_ctas_per_sm;
+        if (in->min_group) t.min_group = in->min_group;
+        if (in->rlgr_block) t.rlgr_block = in->rlgr_block;
     }
-    return n;
+    if (t.group_ctas_per_sm < 1 || t.group_ctas_per_sm > 3 || t.min_group < 1 || t.min_group > 32) return PVVC_ERR_ARG;
+    if (t.rlgr_block != 32 && t.rlgr_block != 64 && t.rlgr_block != 128 && t.rlgr_block != 256) return PVVC_ERR_ARG;
+    *out = t;
+    return PVVC_OK;
 }
 
-// slices of one slot decoded by one warp when at least this many share it
-constexpr int kMinGroup = 4;
-
-// level-signal capacity (nodes) of the shared-memory path of k_raht
-constexpr int kRahtWcap = 1024;
-
-namespace {
-inline uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
-
-// grow-only device buffer
-struct DevBuf {
-    void* p = nullptr;
-    size_t cap = 0;
-    ~DevBuf() {
-        if (p) cudaFree(p);
-    }
-    cudaError_t ensure(size_t n) {
-        if (n <= cap) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e == cudaSuccess) cap = n;
-        return e;
-    }
-};
-struct HostBuf {  // pinned, grow-only
-    void* p = nullptr;
-    size_t cap = 0;
-    ~HostBuf() {
-        if (p) cudaFreeHost(p);
-    }
-    cudaError_t ensure(size_t n) {
-        if (n <= cap) return cudaSuccess;
-        if (p) cudaFreeHost(p);
-        p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMallocHost(&p, n);
-        if (e == cudaSuccess) cap = n;
-        return e;
-    }
-};
-}  // namespace
-}  // namespace pvvc
-
-struct pvvc_plan {
-    int32_t nslices = 0, nintra = 0, max_slot = -1;
-    uint64_t total_points = 0;
-    uint64_t ws_coef = 0, ws_fb = 0, ws_tstatus = 0, ws_rstatus = 0, ws_fstatus = 0, ws_bytes = 0;
-    uint64_t ws_grp = 0, ws_counter = 0, grp_floats = 0;  // group-kernel level buffers, queue counters
-    int32_t grp_ctas = 0;
-    uint64_t coef_floats = 0;
-    std::vector<pvvc::SliceWork> work;
-    std::vector<int32_t> order;
-    // inverse-RAHT schedule: phase A needs only this batch's trees; phase B
-    // also needs phase A's intra colours.  Groups go to the warp kernel,
-    // lists to the per-slice kernel.
-    std::vector<pvvc::GroupDesc> groups;  // [A groups | B groups]
-    int32_t ngroups_a = 0, ngroups_b = 0;
-    std::vector<int32_t> idx;             // [group items | slice list A | slice list B]
-    int32_t nlist_a = 0, nlist_b = 0, list_a_off = 0, list_b_off = 0;
-    pvvc::DevBuf d_work, d_order, d_groups, d_idx;
-};
-
-struct pvvc_state {
-    pvvc::StateView v{};
-    // buffers of the end-to-end host call, kept across calls
-    pvvc::DevBuf payload, xyz, rgb, ws, status;
-    pvvc::HostBuf h_payload;
-    pvvc_plan plan;
-};
-
-namespace pvvc {
-namespace {
-
-int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
+int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload) {
     if (!d || d->nslices < 0) return PVVC_ERR_ARG;
+    if (resolve_tune(tune, &p->tune)) return PVVC_ERR_ARG;
+    if (prepare_kernels() != cudaSuccess) return PVVC_ERR_CUDA;
     const int n = d->nslices;
     if (n > 0 && (!d->slot || !d->type || !d->size || !d->qp || !d->mv || !d->geo_off || !d->geo_size || !d->col_off ||
                   !d->col_size || !d->out_off))
@@ -201,7 +118,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
                 const int cnt = (int)std::min<size_t>(32, L.size() - c0);
                 const bool first = c0 == 0;
                 const bool phase_b = has_intra && !first;
-                if ((first && has_intra) || cnt >= kMinGroup) {
+                if ((first && has_intra) || cnt >= p->tune.min_group) {
                     GroupDesc g{slot_of[si], (int32_t)items.size(), cnt, (first && has_intra) ? 1 : 0};
                     items.insert(items.end(), L.begin() + c0, L.begin() + c0 + cnt);
                     (phase_b ? gb : ga).push_back(g);
@@ -269,7 +186,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
     {
         uint32_t maxn = 0;
         for (const auto& g : p->groups) maxn = std::max(maxn, p->work[p->idx[g.first]].n);
-        p->grp_ctas = std::min<int32_t>((int32_t)p->groups.size(), kGroupCtasPerSm * sm_count());
+        p->grp_ctas = std::min<int32_t>((int32_t)p->groups.size(), p->tune.group_ctas_per_sm * sm_count());
         p->grp_floats = 2ull * std::max<uint32_t>(maxn, 1) * 96;
         p->ws_grp = off;
         off = align_up(off + 4ull * p->grp_floats * std::max(p->grp_ctas, 1), 256);
@@ -277,27 +194,31 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p) {
         off = align_up(off + 16, 256);
     }
     p->ws_bytes = std::max<uint64_t>(off, 256);
-    // upload
+    // upload: synchronous from the plan's vectors, or (upload != nullptr)
+    // stream-ordered from pinned mirrors that stay untouched until the plan is
+    // rebuilt (the caller orders that after the copies)
     if (n > 0) {
-        if (p->d_work.ensure(sizeof(SliceWork) * n) != cudaSuccess) return PVVC_ERR_NOMEM;
-        if (p->d_order.ensure(4ull * n) != cudaSuccess) return PVVC_ERR_NOMEM;
-        if (cudaMemcpy(p->d_work.p, p->work.data(), sizeof(SliceWork) * n, cudaMemcpyHostToDevice) != cudaSuccess)
-            return PVVC_ERR_CUDA;
-        if (cudaMemcpy(p->d_order.p, p->order.data(), 4ull * n, cudaMemcpyHostToDevice) != cudaSuccess) return PVVC_ERR_CUDA;
-        const size_t gbytes = sizeof(GroupDesc) * std::max<size_t>(p->groups.size(), 1);
-        if (p->d_groups.ensure(gbytes) != cudaSuccess || p->d_idx.ensure(4ull * std::max<size_t>(p->idx.size(), 1)) != cudaSuccess)
+        const size_t wb = sizeof(SliceWork) * n, ob = 4ull * n;
+        const size_t gb = sizeof(GroupDesc) * p->groups.size(), ib = 4ull * p->idx.size();
+        if (p->d_work.ensure(wb) != cudaSuccess || p->d_order.ensure(ob) != cudaSuccess ||
+            p->d_groups.ensure(std::max<size_t>(gb, 16)) != cudaSuccess || p->d_idx.ensure(std::max<size_t>(ib, 16)) != cudaSuccess)
             return PVVC_ERR_NOMEM;
-        if (!p->groups.empty() &&
-            cudaMemcpy(p->d_groups.p, p->groups.data(), sizeof(GroupDesc) * p->groups.size(), cudaMemcpyHostToDevice) != cudaSuccess)
-            return PVVC_ERR_CUDA;
-        if (!p->idx.empty() && cudaMemcpy(p->d_idx.p, p->idx.data(), 4ull * p->idx.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        auto put = [&](DevBuf& d, HostBuf& h, const void* src, size_t bytes) -> bool {
+            if (!bytes) return true;
+            if (!upload) return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+            if (h.ensure(bytes) != cudaSuccess) return false;
+            std::memcpy(h.p, src, bytes);
+            return cudaMemcpyAsync(d.p, h.p, bytes, cudaMemcpyHostToDevice, upload) == cudaSuccess;
+        };
+        if (!put(p->d_work, p->h_work, p->work.data(), wb) || !put(p->d_order, p->h_order, p->order.data(), ob) ||
+            !put(p->d_groups, p->h_groups, p->groups.data(), gb) || !put(p->d_idx, p->h_idx, p->idx.data(), ib))
             return PVVC_ERR_CUDA;
     }
     return PVVC_OK;
 }
 
 int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb, float* p24,
-               int32_t* status, void* ws, uint64_t ws_bytes, cudaStream_t s, void* const* events = nullptr) {
+               int32_t* status, void* ws, uint64_t ws_bytes, cudaStream_t s, void* const* events) {
     if (!p || !st) return PVVC_ERR_ARG;
     if (p->nslices == 0) return PVVC_OK;
     if (!payload || (reinterpret_cast<uintptr_t>(payload) & 15u)) return PVVC_ERR_ARG;
@@ -318,7 +239,8 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) return PVVC_ERR_CUDA;
     // zero symbols are not written by the decoder: clear the planes first
     if (cudaMemsetAsync(coef, 0, 4ull * p->coef_floats, s) != cudaSuccess) return PVVC_ERR_CUDA;
-    if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, s) != cudaSuccess || !mark(2)) return PVVC_ERR_CUDA;
+    if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, p->tune.rlgr_block, s) != cudaSuccess || !mark(2))
+        return PVVC_ERR_CUDA;
     float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
     int* cnt = reinterpret_cast<int*>(w + p->ws_counter);
     const GroupDesc* dg = static_cast<const GroupDesc*>(p->d_groups.p);
@@ -340,7 +262,6 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     return PVVC_OK;
 }
 
-}  // namespace
 }  // namespace pvvc
 
 using namespace pvvc;
@@ -412,13 +333,156 @@ extern "C" int pvvc_state_reset(pvvc_state* st, void* stream) {
                                                                                                                 : PVVC_ERR_CUDA;
 }
 
-extern "C" int pvvc_plan_create(const pvvc_batch_desc* desc, pvvc_plan** out) {
+extern "C" int pvvc_plan_create_tuned(const pvvc_batch_desc* desc, const pvvc_tune* tune, pvvc_plan** out) {
     if (!out) return PVVC_ERR_ARG;
     *out = nullptr;
     auto p = std::make_unique<pvvc_plan>();
-    int s = build_plan(desc, p.get());
+    int s = build_plan(desc, p.get(), tune, nullptr);
     if (s) return s;
     *out = p.release();
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_plan_create(const pvvc_batch_desc* desc, pvvc_plan** out) {
+    return pvvc_plan_create_tuned(desc, nullptr, out);
+}
+
+extern "C" int pvvc_plan_info_get(const pvvc_plan* p, pvvc_plan_info* info) {
+    if (!p || !info) return PVVC_ERR_ARG;
+    std::memset(info, 0, sizeof(*info));
+    info->nslices = p->nslices;
+    info->nintra = p->nintra;
+    info->groups_a = p->ngroups_a;
+    info->groups_b = p->ngroups_b;
+    info->singles_a = p->nlist_a;
+    info->singles_b = p->nlist_b;
+    info->group_ctas = p->grp_ctas;
+    info->tune = p->tune;
+    if (p->nslices > 0)
+        info->kernels = (p->nintra > 0) + 1 + (p->ngroups_a > 0) + (p->nlist_a > 0) + (p->ngroups_b > 0) + (p->nlist_b > 0);
+    return PVVC_OK;
+}
+
+namespace {
+// device time of `reps` decodes of `p` (ms each), or a negative value on error
+float time_plan(pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb, int32_t* status,
+                DevBuf& ws, int reps, cudaStream_t s) {
+    if (ws.ensure(p->ws_bytes) != cudaSuccess) return -1.f;
+    // one untimed decode (first touch of the workspace, L2 state)
+    if (run_decode(p, st, payload, xyz, rgb, nullptr, status, ws.p, ws.cap, s, nullptr)) return -1.f;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return -1.f;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return -1.f;
+    }
+    float ms = -1.f;
+    bool ok = cudaEventRecord(e0, s) == cudaSuccess;
+    for (int r = 0; ok && r < reps; ++r) ok = run_decode(p, st, payload, xyz, rgb, nullptr, status, ws.p, ws.cap, s, nullptr) == PVVC_OK;
+    if (ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
+        ms /= reps;
+    else
+        ms = -1.f;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms;
+}
+}  // namespace
+
+extern "C" int pvvc_plan_autotune(const pvvc_batch_desc* desc, pvvc_state* st, const uint8_t* payload, int32_t reps,
+                                  void* stream, pvvc_tune* best, float* best_ms) {
+    if (!desc || !st || !best || reps <= 0) return PVVC_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    pvvc_plan probe;
+    int rc = build_plan(desc, &probe, nullptr, nullptr);
+    if (rc) return rc;
+    DevBuf xyz, rgb, status, ws;
+    if (xyz.ensure(std::max<uint64_t>(12 * probe.total_points, 4)) != cudaSuccess ||
+        rgb.ensure(std::max<uint64_t>(3 * probe.total_points, 4)) != cudaSuccess ||
+        status.ensure(std::max<uint64_t>(4ull * probe.nslices, 4)) != cudaSuccess)
+        return PVVC_ERR_NOMEM;
+    float* dx = static_cast<float*>(xyz.p);
+    uint8_t* dr = static_cast<uint8_t*>(rgb.p);
+    int32_t* ds = static_cast<int32_t*>(status.p);
+    pvvc_tune cur = probe.tune;
+    float cur_ms = time_plan(&probe, st, payload, dx, dr, ds, ws, reps, s);
+    if (cur_ms < 0) return PVVC_ERR_CUDA;
+    // coordinate search: each field in turn over its candidates, twice
+    const int32_t ctas[] = {1, 2, 3};
+    const int32_t groups[] = {2, 4, 8, 16};
+    const int32_t blocks[] = {32, 64, 128, 256};
+    for (int pass = 0; pass < 2; ++pass) {
+        bool moved = false;
+        for (int field = 0; field < 3; ++field) {
+            const int32_t* cand = field == 0 ? ctas : field == 1 ? groups : blocks;
+            const int nc = field == 0 ? 3 : 4;
+            for (int c = 0; c < nc; ++c) {
+                pvvc_tune t = cur;
+                int32_t* f = field == 0 ? &t.group_ctas_per_sm : field == 1 ? &t.min_group : &t.rlgr_block;
+                if (*f == cand[c]) continue;
+                *f = cand[c];
+                pvvc_plan pl;
+                if ((rc = build_plan(desc, &pl, &t, nullptr))) return rc;
+                const float ms = time_plan(&pl, st, payload, dx, dr, ds, ws, reps, s);
+                if (ms < 0) return PVVC_ERR_CUDA;
+                if (ms < cur_ms * 0.99f) {
+                    cur = t;
+                    cur_ms = ms;
+                    moved = true;
+                }
+            }
+        }
+        if (!moved) break;
+    }
+    *best = cur;
+    if (best_ms) *best_ms = cur_ms;
+    return PVVC_OK;
+}
+
+struct pvvc_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int pvvc_graph_create(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
+                                 float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, pvvc_graph** out) {
+    if (!out || !plan || !st) return PVVC_ERR_ARG;
+    *out = nullptr;
+    if (prepare_kernels() != cudaSuccess) return PVVC_ERR_CUDA;
+    cudaStream_t cs;
+    if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return PVVC_ERR_CUDA;
+    auto g = std::make_unique<pvvc_graph>();
+    int rc = PVVC_OK;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        rc = PVVC_ERR_CUDA;
+    } else {
+        rc = run_decode(plan, st, payload, xyz, rgb, points24, status, workspace, workspace_bytes, cs, nullptr);
+        cudaGraph_t gr = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(cs, &gr);  // ends the capture on every path
+        g->graph = gr;
+        if (rc == PVVC_OK && (e != cudaSuccess || !gr)) rc = PVVC_ERR_CUDA;
+    }
+    if (rc == PVVC_OK && cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess) rc = PVVC_ERR_CUDA;
+    cudaStreamDestroy(cs);
+    if (rc) {
+        pvvc_graph_destroy(g.release());
+        return rc;
+    }
+    *out = g.release();
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_graph_launch(pvvc_graph* g, void* stream) {
+    if (!g || !g->exec) return PVVC_ERR_ARG;
+    return cudaGraphLaunch(g->exec, (cudaStream_t)stream) == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
+}
+
+extern "C" int pvvc_graph_destroy(pvvc_graph* g) {
+    if (!g) return PVVC_ERR_ARG;
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    if (g->graph) cudaGraphDestroy(g->graph);
+    delete g;
     return PVVC_OK;
 }
 
@@ -437,7 +501,8 @@ extern "C" int pvvc_plan_query(const pvvc_plan* p, uint64_t* total_points, uint6
 
 extern "C" int pvvc_decode(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
                            float* points24, int32_t* status, void* workspace, uint64_t workspace_bytes, void* stream) {
-    return run_decode(plan, st, payload, xyz, rgb, points24, status, workspace, workspace_bytes, (cudaStream_t)stream);
+    return run_decode(plan, st, payload, xyz, rgb, points24, status, workspace, workspace_bytes, (cudaStream_t)stream,
+                      nullptr);
 }
 
 extern "C" int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb,
@@ -543,12 +608,12 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         d.col_off = coff.data() + first;
         d.col_size = csz.data() + first;
         d.out_off = oo.data() + first;
-        rc = build_plan(&d, &st->plan);
+        rc = build_plan(&d, &st->plan, nullptr, nullptr);
         if (rc) break;
         if (st->ws.ensure(st->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
         rc = run_decode(&st->plan, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
                         static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
-                        st->ws.cap, s);
+                        st->ws.cap, s, nullptr);
         // the plan's host arrays are rebuilt by the next batch: finish this one first
         if (rc == PVVC_OK && bounds.size() > 2 && cudaStreamSynchronize(s) != cudaSuccess) rc = PVVC_ERR_CUDA;
     }
@@ -610,11 +675,11 @@ extern "C" int pvvc_launch_cudaProcess(int grid, int block, float* out_points24,
     }
     pvvc_batch_desc d{n, slot.data(), h_type.data(), h_size.data(), h_qp.data(), h_m.data(), goff.data(), h_gsz.data(),
                       coff.data(), h_csz.data(), oo.data()};
-    int rc = build_plan(&d, &decoders->plan);
+    int rc = build_plan(&d, &decoders->plan, nullptr, nullptr);
     if (rc) return rc;
     if (decoders->ws.ensure(decoders->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
     rc = run_decode(&decoders->plan, decoders, reinterpret_cast<const uint8_t*>(base), nullptr, nullptr, out_points24, nullptr,
-                    decoders->ws.p, decoders->ws.cap, s);
+                    decoders->ws.p, decoders->ws.cap, s, nullptr);
     if (rc) return rc;
     return cudaStreamSynchronize(s) == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }

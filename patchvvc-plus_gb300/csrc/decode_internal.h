@@ -1,0 +1,123 @@
+// decode_internal.h -- host-side internals of the decode path shared by the
+// C ABI (decode_api.cu) and the serving runtime (serve.cu): plan and state
+// objects, grow-only buffers, the planner and the stream-ordered decode.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "decode_types.h"
+#include "pvvc_gb300.h"
+
+namespace pvvc {
+cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payload, const StateView& st, int32_t* tstatus,
+                        cudaStream_t s);
+cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
+                        int32_t* rstatus, int block, cudaStream_t s);
+cudaError_t prepare_kernels();
+cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int count, const StateView& st, const float* coef,
+                              float* fallback, const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz,
+                              uint8_t* rgb, float* p24, int32_t* status, int wcap, cudaStream_t s);
+cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, int ngroups, const int32_t* items,
+                              const StateView& st, const float* coef, const int32_t* tstatus, const int32_t* rstatus,
+                              int32_t* fstatus, float* xyz, uint8_t* rgb, float* p24, int32_t* status, float* scratch,
+                              uint64_t scratch_floats, int nctas, int* counter, cudaStream_t s);
+
+// default launch shapes: persistent CTAs of the group kernel per SM (its
+// ~57 KB of staging allows three), the group threshold, the RLGR block
+constexpr int kGroupCtasPerSm = 3;
+constexpr int kMinGroup = 4;
+constexpr int kRlgrBlock = 128;
+
+// the SM count (queried once)
+inline int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 132;
+    }
+    return n;
+}
+
+// level-signal capacity (nodes) of the shared-memory path of k_raht
+constexpr int kRahtWcap = 1024;
+
+inline uint64_t align_up(uint64_t v, uint64_t a) { return (v + a - 1) / a * a; }
+
+// grow-only device buffer
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) cap = n;
+        return e;
+    }
+};
+struct HostBuf {  // pinned, grow-only
+    void* p = nullptr;
+    size_t cap = 0;
+    ~HostBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    cudaError_t ensure(size_t n) {
+        if (n <= cap) return cudaSuccess;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMallocHost(&p, n);
+        if (e == cudaSuccess) cap = n;
+        return e;
+    }
+};
+}  // namespace pvvc
+
+struct pvvc_plan {
+    pvvc_tune tune{};  // resolved launch shapes
+    int32_t nslices = 0, nintra = 0, max_slot = -1;
+    uint64_t total_points = 0;
+    uint64_t ws_coef = 0, ws_fb = 0, ws_tstatus = 0, ws_rstatus = 0, ws_fstatus = 0, ws_bytes = 0;
+    uint64_t ws_grp = 0, ws_counter = 0, grp_floats = 0;  // group-kernel level buffers, queue counters
+    int32_t grp_ctas = 0;
+    uint64_t coef_floats = 0;
+    std::vector<pvvc::SliceWork> work;
+    std::vector<int32_t> order;
+    // inverse-RAHT schedule: phase A needs only this batch's trees; phase B
+    // also needs phase A's intra colours.  Groups go to the warp kernel,
+    // lists to the per-slice kernel.
+    std::vector<pvvc::GroupDesc> groups;  // [A groups | B groups]
+    int32_t ngroups_a = 0, ngroups_b = 0;
+    std::vector<int32_t> idx;             // [group items | slice list A | slice list B]
+    int32_t nlist_a = 0, nlist_b = 0, list_a_off = 0, list_b_off = 0;
+    pvvc::DevBuf d_work, d_order, d_groups, d_idx;
+    pvvc::HostBuf h_work, h_order, h_groups, h_idx;  // pinned mirrors of stream-ordered uploads
+};
+
+struct pvvc_state {
+    pvvc::StateView v{};
+    // buffers of the end-to-end host call, kept across calls
+    pvvc::DevBuf payload, xyz, rgb, ws, status;
+    pvvc::HostBuf h_payload;
+    pvvc_plan plan;
+};
+
+namespace pvvc {
+// zero tune fields -> defaults; out-of-range fields -> PVVC_ERR_ARG
+int resolve_tune(const pvvc_tune* in, pvvc_tune* out);
+// Sort a batch into the work queue and upload it: synchronously, or with
+// `upload` set, stream-ordered on that stream from pinned mirrors.
+int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload);
+// Enqueue one planned decode on `s` (events: optional stage markers).
+int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb, float* p24,
+               int32_t* status, void* ws, uint64_t ws_bytes, cudaStream_t s, void* const* events);
+}  // namespace pvvc

@@ -21,6 +21,8 @@
 // the reference's order, so nothing is contracted into an FMA.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include <cstdint>
 
 #include "decode_types.h"
@@ -346,7 +348,8 @@ constexpr uint32_t kRlU0 = 3, kRlU1 = 2, kRlD0 = 1, kRlD1 = 1, kRlMaxRP = 32 * 4
 // plane goes to coefficient N-1-j (the stream is reversed).  The loop keeps
 // 32-bit state only: `dst` walks down the current plane, `rem` counts the
 // plane's symbols still to come, `left` all symbols still to come.
-__global__ void __launch_bounds__(128) k_rlgr(const SliceWork* __restrict__ work, const int32_t* __restrict__ order,
+template <int T>
+__global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, const int32_t* __restrict__ order,
                                               int nslices, const uint8_t* __restrict__ payload, float* __restrict__ coef,
                                               int32_t* __restrict__ rstatus) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1009,6 +1012,24 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
 constexpr int kTreeThreads = 256;
 constexpr int kRahtThreads = 128;
 
+// Dynamic shared-memory limits of the inverse-RAHT kernels, set once per
+// device before any launch (and so before any stream capture: the launchers
+// themselves make only capturable calls).
+cudaError_t prepare_kernels() {
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> g(mu);
+    if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+    e = cudaFuncSetAttribute(k_raht_slice<kRahtThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_raht_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupStage));
+    if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+    return e;
+}
+
 cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payload, const StateView& st, int32_t* tstatus,
                         cudaStream_t s) {
     if (nintra <= 0) return cudaSuccess;
@@ -1017,9 +1038,16 @@ cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payloa
 }
 
 cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
-                        int32_t* rstatus, cudaStream_t s) {
+                        int32_t* rstatus, int block, cudaStream_t s) {
     if (nslices <= 0) return cudaSuccess;
-    k_rlgr<<<(nslices + 127) / 128, 128, 0, s>>>(work, order, nslices, payload, coef, rstatus);
+    const int grid = (nslices + block - 1) / block;
+    switch (block) {
+        case 32: k_rlgr<32><<<grid, 32, 0, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 64: k_rlgr<64><<<grid, 64, 0, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 128: k_rlgr<128><<<grid, 128, 0, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 256: k_rlgr<256><<<grid, 256, 0, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 
@@ -1028,11 +1056,6 @@ cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int co
                               uint8_t* rgb, float* p24, int32_t* status, int wcap, cudaStream_t s) {
     if (count <= 0) return cudaSuccess;
     const size_t smem = 2ull * wcap * 3 * sizeof(float);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_raht_slice<kRahtThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        attr_set = true;
-    }
     OutPtrs o{xyz, rgb, p24, status};
     k_raht_slice<kRahtThreads><<<count, kRahtThreads, smem, s>>>(work, list, st, coef, fallback, tstatus, rstatus, fstatus, o,
                                                                  wcap);
@@ -1047,11 +1070,6 @@ cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, in
     if (cudaMemsetAsync(counter, 0, sizeof(int), s) != cudaSuccess) return cudaGetLastError();
     OutPtrs o{xyz, rgb, p24, status};
     const int grid = ngroups < nctas ? ngroups : nctas;
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_raht_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupStage));
-        attr_set = true;
-    }
     k_raht_group<<<grid, 32 * kGrpWarps, sizeof(GroupStage), s>>>(work, groups, ngroups, items, st, coef, tstatus, rstatus,
                                                                   fstatus, o, scratch, scratch_floats, counter);
     return cudaGetLastError();

@@ -29,6 +29,34 @@ class BatchDesc(C.Structure):
                 ("geo_off", u64p), ("geo_size", u32p), ("col_off", u64p), ("col_size", u32p), ("out_off", u64p)]
 
 
+class Tune(C.Structure):
+    _fields_ = [("group_ctas_per_sm", C.c_int32), ("min_group", C.c_int32), ("rlgr_block", C.c_int32)]
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("nslices", C.c_int32), ("nintra", C.c_int32), ("groups_a", C.c_int32), ("groups_b", C.c_int32),
+                ("singles_a", C.c_int32), ("singles_b", C.c_int32), ("kernels", C.c_int32), ("group_ctas", C.c_int32),
+                ("tune", Tune)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_leaves", C.c_int32), ("max_nodes", C.c_int32),
+                ("max_batch_points", C.c_uint64), ("ring_points", C.c_uint64), ("inflight", C.c_int32),
+                ("max_batch_frames", C.c_int32), ("tune", Tune)]
+
+
+class Completion(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("handle", C.c_uint64), ("stream_id", C.c_int32), ("status", C.c_int32),
+                ("npoints", C.c_uint64), ("xyz", C.c_void_p), ("rgb", C.c_void_p), ("submit_us", C.c_double),
+                ("launch_us", C.c_double), ("done_us", C.c_double), ("batch_id", C.c_int32), ("batch_frames", C.c_int32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("batches", C.c_uint64), ("frames", C.c_uint64), ("points", C.c_uint64), ("slices", C.c_uint64),
+                ("slots_total", C.c_uint64), ("slots_free", C.c_uint64), ("streams_open", C.c_uint64),
+                ("reserved_bytes", C.c_uint64), ("gpu_busy_us", C.c_double)]
+
+
 class IcpParams(C.Structure):
     _fields_ = [("max_corr_dist", C.c_float), ("max_iter", C.c_int32), ("fitness_eps", C.c_float),
                 ("transform_eps", C.c_float), ("mse_abs_eps", C.c_float)]
@@ -51,6 +79,12 @@ SIGNATURES = [
     ("pvvc_plan_create", C.c_int, [C.POINTER(BatchDesc), C.POINTER(vp)]),
     ("pvvc_plan_destroy", C.c_int, [vp]),
     ("pvvc_plan_query", C.c_int, [vp, u64p, u64p]),
+    ("pvvc_plan_create_tuned", C.c_int, [C.POINTER(BatchDesc), C.POINTER(Tune), C.POINTER(vp)]),
+    ("pvvc_plan_info_get", C.c_int, [vp, C.POINTER(PlanInfo)]),
+    ("pvvc_plan_autotune", C.c_int, [C.POINTER(BatchDesc), vp, vp, C.c_int32, vp, C.POINTER(Tune), f32p]),
+    ("pvvc_graph_create", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.POINTER(vp)]),
+    ("pvvc_graph_launch", C.c_int, [vp, vp]),
+    ("pvvc_graph_destroy", C.c_int, [vp]),
     ("pvvc_decode", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, vp]),
     ("pvvc_decode_profiled", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, vp, C.POINTER(vp)]),
     ("pvvc_decode_frames_host", C.c_int, [vp, C.c_int32, C.POINTER(u8p), u64p, f32p, u8p, C.c_uint64, u64p, i32p,
@@ -67,6 +101,15 @@ SIGNATURES = [
     ("pvvc_icp_batch_noalloc", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, C.POINTER(IcpParams), vp, vp, vp, vp,
                                          C.c_uint64, vp]),
     ("pvvc_cloud_mse_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
+    ("pvvc_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(vp)]),
+    ("pvvc_server_destroy", C.c_int, [vp]),
+    ("pvvc_server_open_stream", C.c_int, [vp, C.c_int32, i32p]),
+    ("pvvc_server_close_stream", C.c_int, [vp, C.c_int32]),
+    ("pvvc_server_submit", C.c_int, [vp, C.c_int32, vp, C.c_uint64, C.c_uint64]),
+    ("pvvc_server_poll", C.c_int, [vp, C.POINTER(Completion), C.c_int32, i32p, C.c_int32]),
+    ("pvvc_server_read", C.c_int, [vp, C.c_uint64, f32p, u8p]),
+    ("pvvc_server_release", C.c_int, [vp, C.c_uint64]),
+    ("pvvc_server_stats_get", C.c_int, [vp, C.POINTER(ServerStats)]),
     # synthetic sequences (not part of the drop-in boundary)
     ("pvvc_synth_create", C.c_int, [C.POINTER(SynthConfig), C.POINTER(vp)]),
     ("pvvc_synth_destroy", None, [vp]),

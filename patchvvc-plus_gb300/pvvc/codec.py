@@ -115,24 +115,64 @@ class Decoder:
         return xyz[:P], rgb[:P], st[:nsl]
 
 
-class Plan:
-    """A device work queue for one packed Batch (pvvc_plan)."""
+def _desc(b: Batch):
+    keep = [np.ascontiguousarray(x) for x in (b.slot, b.type, b.size, b.qp, b.mv, b.geo_off, b.geo_size, b.col_off,
+                                              b.col_size, b.out_off)]
+    k = keep
+    d = L.BatchDesc(b.nslices, _p(k[0], L.i32p), _p(k[1], L.u8p), _p(k[2], L.u32p), _p(k[3], L.u8p), _p(k[4], L.f32p),
+                    _p(k[5], L.u64p), _p(k[6], L.u32p), _p(k[7], L.u64p), _p(k[8], L.u32p), _p(k[9], L.u64p))
+    return d, keep
 
-    def __init__(self, b: Batch):
+
+def _tune(t) -> L.Tune:
+    if t is None:
+        return L.Tune(0, 0, 0)
+    if isinstance(t, L.Tune):
+        return t
+    if isinstance(t, dict):
+        return L.Tune(int(t.get("group_ctas_per_sm", 0)), int(t.get("min_group", 0)), int(t.get("rlgr_block", 0)))
+    return L.Tune(*[int(x) for x in t])
+
+
+def tune_dict(t: L.Tune) -> dict:
+    return {"group_ctas_per_sm": int(t.group_ctas_per_sm), "min_group": int(t.min_group), "rlgr_block": int(t.rlgr_block)}
+
+
+def autotune(b: Batch, dec: "Decoder", payload_ptr: int, reps: int = 3, stream: int = 0) -> tuple[dict, float]:
+    """pvvc_plan_autotune: the fastest launch shapes for this batch and their
+    mean device time (ms).  Decodes the batch for real into `dec`."""
+    d, keep = _desc(b)
+    best = L.Tune(0, 0, 0)
+    ms = C.c_float(0)
+    L.check(L.lib().pvvc_plan_autotune(C.byref(d), dec.h, payload_ptr, reps, stream, C.byref(best), C.byref(ms)),
+            "pvvc_plan_autotune")
+    del keep
+    return tune_dict(best), float(ms.value)
+
+
+class Plan:
+    """A device work queue for one packed Batch (pvvc_plan), with optional
+    launch shapes (a pvvc_tune as dict / tuple; None = defaults)."""
+
+    def __init__(self, b: Batch, tune=None):
         self.batch = b
-        self._keep = [np.ascontiguousarray(x) for x in (b.slot, b.type, b.size, b.qp, b.mv, b.geo_off, b.geo_size,
-                                                         b.col_off, b.col_size, b.out_off)]
-        k = self._keep
-        d = L.BatchDesc(b.nslices, _p(k[0], L.i32p), _p(k[1], L.u8p), _p(k[2], L.u32p), _p(k[3], L.u8p), _p(k[4], L.f32p),
-                        _p(k[5], L.u64p), _p(k[6], L.u32p), _p(k[7], L.u64p), _p(k[8], L.u32p), _p(k[9], L.u64p))
+        d, self._keep = _desc(b)
         h = L.vp()
-        L.check(L.lib().pvvc_plan_create(C.byref(d), C.byref(h)), "pvvc_plan_create")
+        t = _tune(tune)
+        L.check(L.lib().pvvc_plan_create_tuned(C.byref(d), C.byref(t), C.byref(h)), "pvvc_plan_create")
         self.h = h
         tp = C.c_uint64(0)
         wb = C.c_uint64(0)
         L.check(L.lib().pvvc_plan_query(h, C.byref(tp), C.byref(wb)), "pvvc_plan_query")
         self.total_points = int(tp.value)
         self.workspace_bytes = int(wb.value)
+
+    def info(self) -> dict:
+        i = L.PlanInfo()
+        L.check(L.lib().pvvc_plan_info_get(self.h, C.byref(i)), "pvvc_plan_info_get")
+        out = {k: int(getattr(i, k)) for k, _ in L.PlanInfo._fields_ if k != "tune"}
+        out["tune"] = tune_dict(i.tune)
+        return out
 
     def close(self):
         if self.h:
@@ -150,3 +190,35 @@ class Plan:
         """pvvc_decode with raw device pointers (0 = not wanted)."""
         L.check(L.lib().pvvc_decode(self.h, dec.h, payload_ptr, xyz_ptr or None, rgb_ptr or None, points24_ptr or None,
                                     status_ptr or None, workspace_ptr, workspace_bytes, stream), "pvvc_decode")
+
+    def graph(self, dec: Decoder, payload_ptr: int, xyz_ptr: int, rgb_ptr: int, points24_ptr: int, status_ptr: int,
+              workspace_ptr: int, workspace_bytes: int) -> "Graph":
+        """The decode of this plan with these buffers, captured in a CUDA graph."""
+        return Graph(self, dec, payload_ptr, xyz_ptr, rgb_ptr, points24_ptr, status_ptr, workspace_ptr, workspace_bytes)
+
+
+class Graph:
+    """pvvc_graph: one planned decode replayed by a single graph launch."""
+
+    def __init__(self, plan: Plan, dec: Decoder, payload_ptr, xyz_ptr, rgb_ptr, points24_ptr, status_ptr, workspace_ptr,
+                 workspace_bytes):
+        self._refs = (plan, dec)  # the graph bakes in their device buffers
+        h = L.vp()
+        L.check(L.lib().pvvc_graph_create(plan.h, dec.h, payload_ptr, xyz_ptr or None, rgb_ptr or None,
+                                          points24_ptr or None, status_ptr or None, workspace_ptr, workspace_bytes,
+                                          C.byref(h)), "pvvc_graph_create")
+        self.h = h
+
+    def launch(self, stream: int = 0) -> None:
+        L.check(L.lib().pvvc_graph_launch(self.h, stream), "pvvc_graph_launch")
+
+    def close(self):
+        if self.h:
+            L.lib().pvvc_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

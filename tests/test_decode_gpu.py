@@ -24,9 +24,9 @@ def _dev(torch, a: np.ndarray):
     return torch.from_numpy(np.ascontiguousarray(a)).to("cuda")
 
 
-def decode_batch(torch, pvvc, dec, batch, points24=False):
+def decode_batch(torch, pvvc, dec, batch, points24=False, tune=None):
     """Plan + pvvc_decode through the C ABI with torch-allocated buffers."""
-    plan = pvvc.Plan(batch)
+    plan = pvvc.Plan(batch, tune=tune)
     P = max(plan.total_points, 1)
     pay = _dev(torch, batch.payload)
     xyz = torch.zeros((P, 3), dtype=torch.float32, device="cuda")
