@@ -431,8 +431,11 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
             br.consume(32);
             u = br.peek();
             br.consume(32);
+            // p may be far above the kRP cap; any p > kRlMaxRP saturates
+            // kRP + p - 1 at the cap (kRP >= 0), so clamp p to kRlMaxRP + 1,
+            // not kRlMaxRP (that would leave kRP one short when kRP = 0)
             const uint32_t t2 = kR >= 32 ? 0u : (u >> kR);
-            pq = t2 > kRlMaxRP ? kRlMaxRP : t2;
+            pq = t2 > kRlMaxRP ? kRlMaxRP + 1 : t2;
         }
         // adaptation (entropy_codec.cc:245-281)
         kRP = pq ? min(kRP + pq - 1, kRlMaxRP) : (kRP < 2 ? 0u : kRP - 2);

@@ -182,7 +182,14 @@ def playback(server: Server, streams: list[list[bytes]], duration_s: float, fps:
     lat = lat_ms[steady] if steady.any() else lat_ms
     span_us = a[:, 4].max() - a[:, 2].min() if len(a) else 1.0
     st = server.stats()
-    return {"streams": len(streams), "requests": total, "completed": len(got), "errors": int((a[:, 0] != 0).sum()),
+    bad = [(g[0], g[1], g[3], g[9]) for g in got if g[3] != 0]
+    hist = {}
+    for _, _, code, _ in bad:
+        hist[int(code)] = hist.get(int(code), 0) + 1
+    diag = {"error_status": hist,
+            "error_samples": [{"stream": int(i), "frame": int(k % len(streams[i])), "k": int(k), "status": int(code),
+                               "batch_frames": int(bf)} for i, k, code, bf in bad[:12]]}
+    return {**diag, "streams": len(streams), "requests": total, "completed": len(got), "errors": int((a[:, 0] != 0).sum()),
             "p50_ms": float(np.percentile(lat, 50)), "p95_ms": float(np.percentile(lat, 95)),
             "p99_ms": float(np.percentile(lat, 99)), "max_ms": float(lat.max()), "mean_ms": float(lat.mean()),
             "points": int(a[:, 1].sum()), "mpts_per_s": float(a[:, 1].sum() / (span_us / 1e6) / 1e6),

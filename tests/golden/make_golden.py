@@ -100,6 +100,21 @@ def make_rlgr(ref: Reference, rng):
             s[:: 7] = 0
         vecs.append(s.astype(np.int64))
         kinds.append(k)
+    # kind 7: a Golomb-Rice escape (>= 32 leading ones) taken while k_RP = 0
+    # and k_P < 4, so that p = u >> k_R is far above the k_RP cap and the next
+    # symbol is read with k_R = 32.  From the initial state (k_P = 0,
+    # k_RP = 8) the head -1 -1 -1 0 drives k_RP 8 -> 6 -> 4 -> 2 -> 0 and k_P
+    # to 3 (entropy_codec.cc:262-281); |escape| >= 65 makes p >= 129.  Lengths
+    # are multiples of 3 (Y|U|V planes).  Own generator, so that the vectors
+    # above and the GoP below are unchanged.
+    r7 = np.random.default_rng(77)
+    for t in range(6):
+        head = [-1, -1, -1, 0, int(r7.integers(65, 2 ** 20)) * (1 if t % 2 else -1), int(r7.integers(-60, 61))]
+        n = 3 * int(r7.integers(4, 900))
+        tail = np.where(r7.random(n) < 0.5, 0, r7.integers(-80, 81, n))
+        s = np.concatenate([head, tail])[:n]
+        vecs.append(s.astype(np.int64))
+        kinds.append(7)
     enc = [ref.rlgr_encode(v) for v in vecs]
     dec = [ref.rlgr_decode(e, v.size) for e, v in zip(enc, vecs)]
     off = np.cumsum([0] + [len(e) for e in enc])

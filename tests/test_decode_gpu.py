@@ -4,11 +4,12 @@ equal the reference's wherever its uint8 cast is defined (see
 conftest.rgb_matches), which makes them bit-identical in practice."""
 import ctypes
 import ctypes.util
+import os
 
 import numpy as np
 import pytest
 
-from conftest import golden_expected, golden_frames, rgb_matches
+from conftest import GOLDEN, golden_expected, golden_frames, rgb_matches
 
 pytestmark = pytest.mark.gpu
 
@@ -221,3 +222,35 @@ def test_decode_is_deterministic(pvvc_lib, torch):
     b = decode_batch(torch, pvvc_lib, dec, batch)
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+def test_rlgr_golden_vectors_through_gpu_decode(pvvc_lib, oracle, torch):
+    """Every reference-encoded RLGR vector of the fixtures (runs, escapes,
+    the lossy >32-bit escape, and escapes taken at k_RP = 0, after which the
+    next symbol is read with k_R = 32) decoded as the colour payload of an
+    intra slice: status 0, and geometry and colours equal to the oracle's."""
+    z = np.load(os.path.join(GOLDEN, "rlgr.npz"))
+    so, bo = z["sym_off"], z["byte_off"]
+    g = np.stack(np.meshgrid(np.arange(16), np.arange(16), np.arange(16), indexing="ij"), -1).reshape(-1, 3)
+    sizes, geos, cols = [], [], []
+    for i in range(len(so) - 1):
+        sym = z["symbols"][so[i]:so[i + 1]]
+        n = max(1, -(-sym.size // 3))
+        if sym.size == 3 * n:
+            col = z["bytes"][bo[i]:bo[i + 1]].tobytes()           # the reference's own bytes
+        else:
+            col = oracle.rlgr_encode(np.concatenate([sym, np.zeros(3 * n - sym.size, np.int64)]))
+        xyz = (g[:n] * 2 + 3).astype(np.float32)
+        geo, nl, _, _ = oracle.encode_patch(xyz, [np.zeros((n, 3), np.float32)], [8])
+        assert nl == n
+        sizes.append(n); geos.append(geo); cols.append(col)
+    m = len(sizes)
+    fr = pvvc_lib.Frame(0, np.arange(m, dtype=np.int32), np.full(m, 1, np.uint8), np.array(sizes, np.uint32),
+                        np.full(m, 8, np.uint8), np.tile(np.eye(4, dtype=np.float32).reshape(16), (m, 1)), geos, cols)
+    dec = pvvc_lib.Decoder(nslots=64, max_leaves=4096)
+    xyz, rgb, st = decode_batch(torch, pvvc_lib, dec, pvvc_lib.pack_frames([fr]))
+    assert (st == 0).all(), st
+    (oxyz, orgb, ost, oyuv), = oracle_decode(oracle, pvvc_lib, [pvvc_lib.write_frame(fr)], m)
+    assert (ost == 0).all()
+    assert np.array_equal(xyz.view(np.uint32), oxyz.view(np.uint32))
+    assert rgb_matches(rgb, orgb, oyuv).all()

@@ -24,7 +24,7 @@ def test_oracle_rlgr_matches_reference_bytes(oracle):
         if kind != 6:  # below 2^32 the code is lossless
             assert np.array_equal(dec, sym)
         n += 1
-    assert n == 28
+    assert n == 34
 
 
 def test_oracle_rlgr_truncated_stream_reports_overrun(oracle):
