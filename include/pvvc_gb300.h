@@ -261,6 +261,69 @@ int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const uint32_t* s
                          const uint32_t* tgt_off, const float* T, float* mse_out, void* workspace,
                          uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream);
 
+/* ---- BF16 tensor-core GEMM ------------------------------------------------
+ * The building block of the registration network's training and inference
+ * kernels (no reference counterpart: the reference registers with PCL ICP
+ * from the identity).  C[M,N] = epilogue(A[M,K] . B[N,K]^T): A and B bf16
+ * row-major with K contiguous (lda, ldb in elements, multiples of 8; K a
+ * multiple of 64; N a multiple of 64; pointers 16-byte aligned), FP32
+ * accumulation in tensor memory (tcgen05.mma).  Epilogues:
+ *   PVVC_GEMM_BIAS_RELU_BF16  C bf16 = max(acc + bias, 0)   (bias may be NULL)
+ *   PVVC_GEMM_F32             C f32  = acc + bias            (bias may be NULL)
+ *   PVVC_GEMM_F32_ACCUM       C f32 += acc, K split `splits` ways (partials
+ *                             added atomically; the only epilogue with splits > 1)
+ *   PVVC_GEMM_MASK_BF16       C bf16 = acc where aux[M,N] (bf16) > 0, else 0
+ * Stream-ordered.  A kernel whose bounded internal wait gave up sets a device
+ * error code that pvvc_device_error_take returns (and clears); 0 = none. */
+#define PVVC_GEMM_BIAS_RELU_BF16 0
+#define PVVC_GEMM_F32 1
+#define PVVC_GEMM_F32_ACCUM 2
+#define PVVC_GEMM_MASK_BF16 3
+int pvvc_gemm_bf16(int32_t M, int32_t N, int32_t K, const void* A, int64_t lda, const void* B, int64_t ldb, void* C,
+                   int64_t ldc, const float* bias, const void* aux, int64_t ldaux, int32_t epilogue, int32_t splits,
+                   void* stream);
+int pvvc_device_error_take(int32_t* code);
+
+/* ---- learned ICP initialisation -------------------------------------------
+ * A PointNet-style network proposes each pair's initial transform for
+ * pvvc_icp_batch (`init`).  No reference counterpart: the reference starts
+ * every registration from the identity (src/registration/icp.cc:21-102).
+ * Inputs: 256 points sampled (with replacement, seeded) from each cloud,
+ * centred on their sample mean and scaled by the source sample's RMS radius;
+ * shared MLP 3-64-128-256 per point, max-pool per cloud, MLP 512-256-128-6 ->
+ * (omega, delta): R = exp(omega), t = c_t - R c_s + s * delta.  BF16 weights
+ * and activations, FP32 accumulation (tcgen05).  Training targets come from
+ * converged ICP: omega* = log R*, delta* from t*.  Parameters are one fp32
+ * vector of pvvc_regnet_param_count() floats (get/set for checkpoints). */
+typedef struct pvvc_regnet pvvc_regnet;
+typedef struct {
+    float lr, beta1, beta2, eps, weight_decay; /* AdamW (decoupled decay on weight matrices) */
+    float lambda_w;                            /* loss weight of the rotation part           */
+} pvvc_adamw;
+int pvvc_regnet_param_count(void);
+int pvvc_regnet_create(uint64_t seed, pvvc_regnet** out);
+int pvvc_regnet_destroy(pvvc_regnet* net);
+int pvvc_regnet_get_params(pvvc_regnet* net, float* host, int64_t count);
+/* also resets the AdamW moments and step */
+int pvvc_regnet_set_params(pvvc_regnet* net, const float* host, int64_t count);
+/* One training step on the pairs pair_ids[0..npairs) of a device dataset
+ * (clouds as for pvvc_icp_batch; T_label [*,16] row-major converged ICP
+ * transforms, omega_label [*,3] their axis-angle): sample, forward, loss,
+ * backward, AdamW.  loss_out: device float (or NULL).  Stream-ordered. */
+int pvvc_regnet_train_step(pvvc_regnet* net, int32_t npairs, const int32_t* pair_ids, const float* src,
+                           const uint32_t* src_off, const float* tgt, const uint32_t* tgt_off, const float* T_label,
+                           const float* omega_label, uint64_t seed, const pvvc_adamw* opt, float* loss_out, void* stream);
+/* Gradient of the loss for given normalised inputs x0 [npairs*2*256*3] (pair
+ * b's source rows then target rows) and targets y [npairs*6]: grad_out
+ * [param_count] (device), loss_out (device float).  No update. */
+int pvvc_regnet_grad(pvvc_regnet* net, int32_t npairs, const float* x0, const float* y, float lambda_w, float* grad_out,
+                     float* loss_out, void* stream);
+/* Proposed transforms T_out [npairs*16] (row-major) for every pair. */
+int pvvc_propose(pvvc_regnet* net, int32_t npairs, const float* src, const uint32_t* src_off, const float* tgt,
+                 const uint32_t* tgt_off, uint64_t seed, float* T_out, void* stream);
+/* The last forward's raw outputs (omega, delta) [npairs*6] (device). */
+int pvvc_regnet_outputs(pvvc_regnet* net, int32_t npairs, float* out6, void* stream);
+
 /* ---- playback server -----------------------------------------------------
  * Decodes .frame requests of many concurrent playback streams with
  * continuous batching.  It replaces the reference client's single decode
