@@ -343,11 +343,36 @@ struct BitReader {
 
 constexpr uint32_t kRlU0 = 3, kRlU1 = 2, kRlD0 = 1, kRlD1 = 1, kRlMaxRP = 32 * 4;
 
+// Zero-run length of `c` leading ones read in run mode from state kP
+// (entropy_codec.cc:228-233): the i-th one stands for 2^((kP + 2i) >> 2)
+// zeros, kP growing by U1 = 2 per one, so the exponents go in pairs.  With
+// S(n) = sum_{i<n} 2^(i>>1) = 2 (2^(n>>1) - 1) + (n & 1) 2^(n>>1):
+//   kP & 3 in {0,1}:  sum = 2^(kP>>2) S(c)
+//   kP & 3 in {2,3}:  sum = 2^(kP>>2) (S(c+1) - 1)
+// c <= 32 and kP >> 2 <= 31 keep the result below 2^49.
+__device__ __forceinline__ uint64_t run_ones_length(uint32_t kP, uint32_t c) {
+    const uint32_t hi = (kP >> 1) & 1u;  // exponent pairs start one late
+    const uint32_t n = c + hi;
+    const uint64_t h = 1ull << (n >> 1);
+    const uint64_t S = 2 * (h - 1) + (n & 1u) * h - hi;
+    return S << (kP >> 2);
+}
+
 // k_rlgr: one thread per slice.  The coefficient planes are zeroed before the
 // launch, so a run of zeros only moves the output position; symbol j of a
 // plane goes to coefficient N-1-j (the stream is reversed).  The loop keeps
 // 32-bit state only: `dst` walks down the current plane, `rem` counts the
 // plane's symbols still to come, `left` all symbols still to come.
+//
+// One iteration = an optional zero run (run mode, kP >= 4) followed by one
+// Golomb-Rice symbol, or a run that ends the slice.  The common case is one
+// straight line that every lane of a warp executes in step, whatever mode
+// its slice is in: the run's leading ones are counted with one clz and summed
+// in closed form (run_ones_length), the run's terminator and k bits and the
+// symbol's code are each taken from one 32-bit peek.  Rare cases leave the
+// line: 31+ leading ones or a run code longer than 32 bits, a Golomb-Rice
+// code longer than 32 bits (wide remainders, the 32-ones escape), symbols of
+// 2^23 or more, and runs that reach the end of a plane.
 template <int T>
 __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, const int32_t* __restrict__ order,
                                               int nslices, const uint8_t* __restrict__ payload, float* __restrict__ coef,
@@ -365,26 +390,35 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
     const uint64_t off = wk.col_off;
     BitReader br;
     br.init(payload, off, wk.csz);
-    const uint32_t cs = wk.coef_stride;
+    const int64_t cs = wk.coef_stride;
+    const int64_t wrap = (int64_t)(2 * N - 1) * cs;  // last coefficient of a plane -> top of the next
     float* dst = coef + wk.coef_off + (uint64_t)(N - 1) * cs + wk.coef_lane;  // coefficient of the next symbol
     uint32_t rem = N;                         // symbols left in the current plane
     uint32_t left = 3u * N;                   // symbols left in the slice
     uint32_t kP = 0, kRP = 8;
     int err = PVVC_OK;
     for (;;) {
-        uint32_t after_run = 0;
-        if (kP >= 4) {
-            // run mode (entropy_codec.cc:226-257): every leading '1' stands for
-            // 2^k zeros and raises kP by U1 (k grows every second one); then a
-            // '0' and k bits complete the run
-            uint32_t k = kP >> 2, m = 0, c;
+        // ---- zero run (entropy_codec.cc:226-241) ----
+        const bool run = kP >= 4;
+        uint32_t v = br.peek();
+        uint32_t c = run ? __clz(~v) : 0u;       // leading ones
+        uint32_t kP2 = kP + 2 * c;               // kP after the ones
+        uint32_t k = run ? (kP2 >> 2) : 0u;      // bits of the run's remainder
+        uint64_t m = 0;
+        if (run && c + 1 + k <= 32) {
+            m = run_ones_length(kP, c) + (uint32_t)((uint64_t)((v << c) << 1) >> (32 - k));
+            br.consume(c + 1 + k);
+        } else if (run) {  // 31+ ones, or the remainder runs past this peek
+            m = 0;
+            k = kP >> 2;
+            kP2 = kP;
             int guard = 0;
             do {
-                c = __clz(~br.peek());  // leading ones, 32 when all are ones
+                c = __clz(~br.peek());
                 for (uint32_t i = 0; i < c; ++i) {
-                    m += 1u << (k & 31);
-                    kP += kRlU1;
-                    k = kP >> 2;
+                    m += 1ull << (k & 31);
+                    kP2 += kRlU1;
+                    k = kP2 >> 2;
                 }
                 br.consume(c);
             } while (c == 32 && ++guard < 64);
@@ -395,69 +429,75 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
             }
             m += br.peek() >> (32 - k);
             br.consume(k);
-            // skip m zeros (they may cross plane boundaries)
-            uint32_t z = m < left ? m : left;
-            left -= z;
-            while (z >= rem && rem) {
-                z -= rem;
-                dst += (int64_t)(2 * N - rem) * cs;  // to the top of the next plane
-                rem = N;
-            }
-            dst -= (int64_t)z * cs;
-            rem -= z;
-            if (left == 0) break;
-            after_run = 1;
         }
-        // Golomb-Rice symbol (GRRead, entropy_codec.cc:196-205)
+        if (run) {
+            // skip m zeros (they may cross plane boundaries)
+            uint32_t z = m < left ? (uint32_t)m : left;
+            left -= z;
+            if (z < rem) {
+                dst -= (int64_t)z * cs;
+                rem -= z;
+            } else {
+                while (z >= rem && rem) {
+                    z -= rem;
+                    dst += (int64_t)(2 * N - rem) * cs;  // to the top of the next plane
+                    rem = N;
+                }
+                dst -= (int64_t)z * cs;
+                rem -= z;
+            }
+            if (left == 0) break;
+        }
+        // ---- Golomb-Rice symbol (GRRead, entropy_codec.cc:196-205) ----
         const uint32_t kR = kRP >> 2;
-        const uint32_t v = br.peek();
+        v = br.peek();
         const uint32_t q = __clz(~v);
         uint32_t u, pq;
-        bool wide = false;  // u does not fit 32 bits
-        uint64_t uw = 0;
-        if (q + 1 + kR <= 32) {  // the common case: one peek holds the whole code
-            u = (q << kR) | (kR ? (v << (q + 1)) >> (32 - kR) : 0u);
+        uint64_t uw;
+        bool wide;  // u does not fit the fast symbol path
+        if (q + 1 + kR <= 32) {  // the whole code is in this peek
+            u = (q << kR) | (uint32_t)((uint64_t)((v << q) << 1) >> (32 - kR));
             br.consume(q + 1 + kR);
             pq = q;
+            uw = u;
+            wide = u >= (1u << 23);
         } else if (q < 32) {
             br.consume(q + 1);
             const uint32_t r = kR == 32 ? br.peek() : (br.peek() >> (32 - kR));
             br.consume(kR);
             uw = ((uint64_t)q << kR) | r;
-            wide = (uw >> 32) != 0;
-            u = (uint32_t)uw;
+            u = (uint32_t)uw | (uint32_t)(uw >> 32);  // nonzero iff uw is
             pq = q;
+            wide = true;
         } else {  // 32 ones: a raw 32-bit value follows
             br.consume(32);
             u = br.peek();
             br.consume(32);
+            uw = u;
             // p may be far above the kRP cap; any p > kRlMaxRP saturates
             // kRP + p - 1 at the cap (kRP >= 0), so clamp p to kRlMaxRP + 1,
             // not kRlMaxRP (that would leave kRP one short when kRP = 0)
             const uint32_t t2 = kR >= 32 ? 0u : (u >> kR);
             pq = t2 > kRlMaxRP ? kRlMaxRP + 1 : t2;
+            wide = true;
         }
         // adaptation (entropy_codec.cc:245-281)
         kRP = pq ? min(kRP + pq - 1, kRlMaxRP) : (kRP < 2 ? 0u : kRP - 2);
-        if (after_run) kP = kP ? kP - kRlD1 : 0u;
-        else kP = (u | (uint32_t)wide) ? (kP ? kP - kRlD0 : 0u) : kP + kRlU0;
+        kP = (run || u) ? (kP2 ? kP2 - kRlD1 : 0u) : kP2 + kRlU0;  // D0 = D1 = 1
         // Unsign2Sign(u + after_run) * qp, stored unless zero
-        if (!wide && u < (1u << 23)) {
-            const uint32_t zz = u + after_run;
+        if (!wide) {
+            const uint32_t zz = u + (uint32_t)run;
             const int32_t sym = (int32_t)(zz >> 1) ^ -(int32_t)(zz & 1);
             if (sym) *dst = __int2float_rn(sym * qp);
         } else {
-            const uint64_t zz = (wide ? uw : (uint64_t)u) + after_run;
+            const uint64_t zz = uw + (uint64_t)run;
             const long long sym = (long long)(zz >> 1) ^ -(long long)(zz & 1);
             *dst = __ll2float_rn(sym * (long long)qp);
         }
         --left;
-        if (--rem == 0) {
-            dst += (int64_t)(2 * N - 1) * cs;
-            rem = N;
-        } else {
-            dst -= cs;
-        }
+        const bool end_of_plane = --rem == 0;
+        dst += end_of_plane ? wrap : -cs;
+        rem = end_of_plane ? N : rem;
         if (left == 0) break;
     }
     // bits consumed vs the payload (the reference reads past it, which is undefined)
@@ -791,10 +831,13 @@ __device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool
 constexpr int kGrpWarps = 8;
 constexpr int kStageLeaves = 8 * kGrpWarps;  // leaves of 8 nodes at most
 
+// Rows are one word longer than kStageLeaves so that the 32 lanes, which
+// store to the same column of their own rows, hit 32 different banks.
+constexpr int kStageRow = kStageLeaves + 1;
 struct GroupStage {
-    float x[32][kStageLeaves], y[32][kStageLeaves], z[32][kStageLeaves];
-    uint32_t rgb[32][kStageLeaves];
-    float fr[32][kStageLeaves], fg[32][kStageLeaves], fb[32][kStageLeaves];  // points24 colours
+    float x[32][kStageRow], y[32][kStageRow], z[32][kStageRow];
+    uint32_t rgb[32][kStageRow];
+    float fr[32][kStageRow], fg[32][kStageRow], fb[32][kStageRow];  // points24 colours
 };
 
 __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* __restrict__ work,
