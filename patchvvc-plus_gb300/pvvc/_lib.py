@@ -30,7 +30,8 @@ class BatchDesc(C.Structure):
 
 
 class Tune(C.Structure):
-    _fields_ = [("group_ctas_per_sm", C.c_int32), ("min_group", C.c_int32), ("rlgr_block", C.c_int32)]
+    _fields_ = [("group_ctas_per_sm", C.c_int32), ("min_group", C.c_int32), ("rlgr_block", C.c_int32),
+                ("rlgr_long_ctas", C.c_int32)]
 
 
 class PlanInfo(C.Structure):
@@ -104,6 +105,15 @@ SIGNATURES = [
     ("pvvc_gemm_bf16", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp, vp,
                                  C.c_int64, C.c_int32, C.c_int32, vp]),
     ("pvvc_device_error_take", C.c_int, [i32p]),
+    ("pvvc_regnet_param_count", C.c_int, []),
+    ("pvvc_regnet_create", C.c_int, [C.c_uint64, C.POINTER(vp)]),
+    ("pvvc_regnet_destroy", C.c_int, [vp]),
+    ("pvvc_regnet_get_params", C.c_int, [vp, f32p, C.c_int64]),
+    ("pvvc_regnet_set_params", C.c_int, [vp, f32p, C.c_int64]),
+    ("pvvc_regnet_train_step", C.c_int, [vp, C.c_int32, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, vp, vp, vp]),
+    ("pvvc_regnet_grad", C.c_int, [vp, C.c_int32, vp, vp, C.c_float, vp, vp, vp]),
+    ("pvvc_propose", C.c_int, [vp, C.c_int32, vp, vp, vp, vp, C.c_uint64, vp, vp]),
+    ("pvvc_regnet_outputs", C.c_int, [vp, C.c_int32, vp, vp]),
     ("pvvc_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(vp)]),
     ("pvvc_server_destroy", C.c_int, [vp]),
     ("pvvc_server_open_stream", C.c_int, [vp, C.c_int32, i32p]),
