@@ -57,7 +57,12 @@ def parse_args():
     ap.add_argument("--frames", type=int, default=300)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--tune", default="", help="fixed launch shapes 'group_ctas,min_group,rlgr_block,long_ctas' "
+                                               "instead of the autotuner")
     ap.add_argument("--icp-pairs", type=int, default=4096, help="batched ICP workload size (0: skip)")
+    ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned-ICP comparison")
+    ap.add_argument("--learned-train-pairs", type=int, default=32768, help="pairs to train on when no weights are committed")
+    ap.add_argument("--learned-train-epochs", type=int, default=8)
     ap.add_argument("--serve-streams", type=int, default=64, help="playback streams of the serving run (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="real-time length of the serving run")
     return ap.parse_args()
@@ -72,6 +77,19 @@ def make_workload(args, rank):
     frames = s.frames()
     log(f"[rank {rank}] generated + encoded {len(frames)} frames in {time.time() - t0:.1f}s")
     return s, frames
+
+
+def traffic_per_step():
+    """DRAM bytes (read + write) of one decode pass of this workload from the
+    committed ncu capture summary, or None when it is absent."""
+    path = os.path.join(ROOT, "profiles", "decode_seq300_dram.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_step:"):
+                return int(line.split(":")[1].strip())
+    except OSError:
+        pass
+    return None
 
 
 def algorithmic_bytes(parsed):
@@ -221,8 +239,12 @@ def run_ours(args):
     pay = torch.from_numpy(batch.payload).to(dev)
     stream = torch.cuda.current_stream(dev)
     t_tune = time.time()
-    tune, tune_ms = pvvc.autotune(batch, dec, pay.data_ptr(), reps=2, stream=stream.cuda_stream)
-    log(f"[rank {rank}] autotune {tune} ({tune_ms:.2f} ms) in {time.time() - t_tune:.1f}s")
+    if args.tune:
+        g, m, b, l = (int(x) for x in args.tune.split(","))
+        tune, tune_ms = {"group_ctas_per_sm": g, "min_group": m, "rlgr_block": b, "rlgr_long_ctas": l}, None
+    else:
+        tune, tune_ms = pvvc.autotune(batch, dec, pay.data_ptr(), reps=2, stream=stream.cuda_stream)
+    log(f"[rank {rank}] launch shapes {tune} ({tune_ms} ms) in {time.time() - t_tune:.1f}s")
     plan = pvvc.Plan(batch, tune=tune)
     info = plan.info()
     P = plan.total_points
@@ -289,25 +311,29 @@ def run_ours(args):
         except Exception:
             pass
         peak = float(peaks.get("hbm_gbs", 6800.0))
-        dev_ms = float(kt.sum())
-        achieved = alg / (dev_ms / 1e3) / 1e9
+        # the decode pass is one CUDA-graph launch: its duration is the timed region's
+        achieved = alg / (ms / 1e3) / 1e9
         dom = int(np.argmax(kt))
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "kernel": f"decode pass ({info['kernels']} kernels in one CUDA graph)",
-                "dominant_kernel": names[dom], "kernel_ms": {n: float(t) for n, t in zip(names, kt)},
+                "traffic": traffic_per_step(), "kernel": f"decode pass (one CUDA-graph launch of {info['kernels']} kernels)",
+                "dominant_kernel": names[dom],
+                "kernel_ms_stream_order": {n: float(t) for n, t in zip(names, kt)},
+                "note": "kernel_ms_stream_order: the same kernels launched in stream order with CUDA events between "
+                        "them (the graph runs the two RLGR launches side by side, so their sum exceeds the pass)",
                 "algorithmic_bytes_per_step": alg, "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}
         e2e = None
         if not args.no_e2e:
             e2e = measure_e2e(args, pvvc, frames, P, torch, stream)
         cb = cpu_baseline(frames, args.cpu_seconds)
         icp = measure_icp(args, torch, peak) if args.icp_pairs > 0 else None
+        learned = measure_learned(args, torch, pvvc) if args.icp_pairs > 0 and args.learned else None
         serving = measure_serving(args, pvvc) if args.serve_streams > 0 and args.serve_seconds > 0 else None
         out = {"metric": "decoded Mpts/s (seq300, GoP 30, ~800k pts/frame)", "value": value, "unit": "Mpts/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
                "clocks": clk.summary(), "gpu_launches": info["kernels"] * args.steps, "points_per_step": P * world,
-               "plan": info, "autotune_ms": tune_ms, "icp": icp, "serving": serving}
+               "plan": info, "autotune_ms": tune_ms, "icp": icp, "learned_icp": learned, "serving": serving}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
@@ -354,6 +380,64 @@ def measure_icp(args, torch, peak_gbs):
             "hbm_gbs_one_read": nbytes / (ms / 1e3) / 1e9, "hbm_frac_one_read": nbytes / (ms / 1e3) / 1e9 / peak_gbs,
             "cpu_baseline": {"value": ns / cdt, "unit": "patches/s", "cores": cores, "kind": "port",
                              "sample": f"first {ns} pairs, {cdt:.1f}s"}}
+
+
+def measure_learned(args, torch, pvvc):
+    """Learned ICP initialisation against plain ICP on the --icp-pairs
+    workload of measure_icp: plain = 50 ICP iterations from the identity;
+    learned = network proposal + at most 10 ICP iterations, pairs whose
+    refinement did not converge (relative dMSE >= 1e-3) re-registered by
+    plain ICP.  Both timed end to end with CUDA events (proposal, ICP, the
+    fallback's gather and ICP).  Weights: the committed network trained on
+    the GPU by pvvc.train_regnet, else a small network trained here."""
+    from pvvc.icp import IcpBatch, make_pairs
+    from pvvc.regnet import PairData, RegNet, register_learned
+    wpath = os.path.join(ROOT, "patchvvc-plus_gb300", "pvvc", "data", "regnet_seq300.npz")
+    net = RegNet(seed=1)
+    if os.path.exists(wpath):
+        z = np.load(wpath)
+        net.set_params(z["params"])
+        weights = {"source": "committed", "pairs": int(z["pairs"]), "epochs": int(z["epochs"]), "batch": int(z["batch"]),
+                   "train_seconds": float(z["train_seconds"]), "final_loss": float(np.mean(z["losses"][-20:]))}
+    else:
+        from pvvc.train_regnet import labelled_dataset, train
+        t0 = time.time()
+        data = labelled_dataset(args.learned_train_pairs, seed=101, log=log)
+        losses, secs = train(net, data, args.learned_train_epochs, 1024, 1e-3, seed=1, log=log, log_every=0)
+        weights = {"source": "trained in this run", "pairs": args.learned_train_pairs, "epochs": args.learned_train_epochs,
+                   "batch": 1024, "train_seconds": secs, "final_loss": float(np.mean(losses[-20:])),
+                   "setup_seconds": time.time() - t0}
+        del data
+    pairs = make_pairs(args.icp_pairs, seed=7)
+    b = IcpBatch(pairs)
+    kw = dict(max_corr_dist=1e6, max_iter=50, fitness_eps=0.0, transform_eps=0.0, mse_abs_eps=1e-6)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn, reps=3):
+        fn()
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, out
+
+    ms_plain, _ = timed(lambda: b.run(**kw))
+    mse_plain = b.mse.cpu().numpy().copy()
+    ms_learn, (T, mse, info) = timed(lambda: register_learned(net, b, judge="converged"))
+    ml = mse.cpu().numpy()
+    ms_prop, _ = timed(lambda: net.propose(PairData(b), seed=0))
+    n = args.icp_pairs
+    return {"npairs": n, "weights": weights,
+            "plain": {"patches_per_s": n / (ms_plain / 1e3), "ms": ms_plain, "mean_mse": float(mse_plain.mean())},
+            "learned": {"patches_per_s": n / (ms_learn / 1e3), "ms": ms_learn, "mean_mse": float(ml.mean()),
+                        "fallback_pairs": int(info["fallback"]), "propose_ms": ms_prop},
+            "speedup": ms_plain / ms_learn,
+            "mse_ratio_mean": float(ml.mean() / mse_plain.mean()),
+            "pairs_mse_le_plain": float((ml <= mse_plain * (1 + 1e-6)).mean()),
+            "pairs_mse_within_1pct": float((ml <= mse_plain * 1.01).mean()),
+            "rule": "proposal + <=10 ICP iterations (accept on relative dMSE < 1e-3), else plain ICP from identity"}
 
 
 def measure_serving(args, pvvc):

@@ -93,9 +93,11 @@ int pvvc_plan_query(const pvvc_plan* plan, uint64_t* total_points, uint64_t* wor
  * reference counterpart: the reference launches one thread per slice
  * (src/cuda/render/render.cc:269-301, block = 1). */
 typedef struct {
-    int32_t group_ctas_per_sm; /* persistent CTAs of the grouped inverse-RAHT kernel per SM: 1..3 (default 3)   */
+    int32_t group_ctas_per_sm; /* persistent CTAs of the grouped inverse-RAHT kernel per SM: 1..4 (default 3)   */
     int32_t min_group;         /* a slot's predictive slices share one warp when at least this many: 1..32 (4) */
     int32_t rlgr_block;        /* threads per CTA of the RLGR kernel: 32, 64, 128 or 256 (default 128)         */
+    int32_t rlgr_long_ctas;    /* CTAs of 128 threads that decode the longest slices alone on an SM each, side by
+                                  side with the rest: 0..152 (default 32); -1 turns the split off                 */
 } pvvc_tune;
 int pvvc_plan_create_tuned(const pvvc_batch_desc* desc, const pvvc_tune* tune, pvvc_plan** out);
 
@@ -112,9 +114,10 @@ typedef struct {
 int pvvc_plan_info_get(const pvvc_plan* plan, pvvc_plan_info* info);
 
 /* Autotuner: plans `desc` under a set of candidate launch shapes (a
- * coordinate search over the three pvvc_tune fields, starting at the
- * defaults), decodes the batch `reps` times under each with CUDA events on
- * `stream`, and returns the fastest shapes and their mean device time.  The
+ * coordinate search over the four pvvc_tune fields, starting at the
+ * defaults), captures one decode of the batch under each into a CUDA graph,
+ * replays it `reps` times on `stream` timed with CUDA events, and returns the
+ * fastest shapes and their mean device time per decode.  The
  * decodes run for real: afterwards `st` holds what one pvvc_decode of the
  * batch leaves.  It allocates its own workspace and outputs, and
  * synchronises `stream`.  `payload` as for pvvc_decode. */

@@ -16,13 +16,15 @@ namespace pvvc {
 
 // zero fields -> defaults; out-of-range fields -> PVVC_ERR_ARG
 int resolve_tune(const pvvc_tune* in, pvvc_tune* out) {
-    pvvc_tune t{kGroupCtasPerSm, kMinGroup, kRlgrBlock};
+    pvvc_tune t{kGroupCtasPerSm, kMinGroup, kRlgrBlock, kRlgrLongCtas};
     if (in) {
         if (in->group_ctas_per_sm) t.group_ctas_per_sm = in->group_ctas_per_sm;
         if (in->min_group) t.min_group = in->min_group;
         if (in->rlgr_block) t.rlgr_block = in->rlgr_block;
+        if (in->rlgr_long_ctas) t.rlgr_long_ctas = in->rlgr_long_ctas;
     }
-    if (t.group_ctas_per_sm < 1 || t.group_ctas_per_sm > 3 || t.min_group < 1 || t.min_group > 32) return PVVC_ERR_ARG;
+    if (t.group_ctas_per_sm < 1 || t.group_ctas_per_sm > 4 || t.min_group < 1 || t.min_group > 32) return PVVC_ERR_ARG;
+    if (t.rlgr_long_ctas < -1 || t.rlgr_long_ctas > 152) return PVVC_ERR_ARG;
     if (t.rlgr_block != 32 && t.rlgr_block != 64 && t.rlgr_block != 128 && t.rlgr_block != 256) return PVVC_ERR_ARG;
     *out = t;
     return PVVC_OK;
@@ -169,6 +171,13 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         if (p->work[a].n != p->work[b].n) return p->work[a].n > p->work[b].n;
         return p->work[a].slot < p->work[b].slot;
     });
+    // the head of that order goes to the long-slice launch (at most a quarter
+    // of the slices, so that small batches still spread over many SMs)
+    p->nlong = 0;
+    if (p->tune.rlgr_long_ctas > 0 && n >= 8) {
+        p->nlong = std::min<int32_t>(kRlgrLongBlock * p->tune.rlgr_long_ctas, n / 4);
+        if (p->side.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+    }
     // workspace layout
     uint64_t off = 0;
     p->ws_coef = off;
@@ -239,8 +248,20 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) return PVVC_ERR_CUDA;
     // zero symbols are not written by the decoder: clear the planes first
     if (cudaMemsetAsync(coef, 0, 4ull * p->coef_floats, s) != cudaSuccess) return PVVC_ERR_CUDA;
-    if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, p->tune.rlgr_block, s) != cudaSuccess || !mark(2))
+    if (p->nlong > 0) {
+        // the longest slices (the head of the size order) on SMs of their own,
+        // side by side with the rest
+        const SideStream& sd = p->side;
+        if (cudaEventRecord(sd.fork, s) != cudaSuccess || cudaStreamWaitEvent(sd.s, sd.fork, 0) != cudaSuccess ||
+            launch_rlgr(dw, ord, p->nlong, payload, coef, rs, kRlgrLongBlock, kRlgrLongSmem, sd.s) != cudaSuccess ||
+            cudaEventRecord(sd.join, sd.s) != cudaSuccess ||
+            launch_rlgr(dw, ord + p->nlong, p->nslices - p->nlong, payload, coef, rs, p->tune.rlgr_block, kRlgrShortSmem,
+                        s) != cudaSuccess ||
+            cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess || !mark(2))
+            return PVVC_ERR_CUDA;
+    } else if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, p->tune.rlgr_block, 0, s) != cudaSuccess || !mark(2)) {
         return PVVC_ERR_CUDA;
+    }
     float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
     int* cnt = reinterpret_cast<int*>(w + p->ws_counter);
     const GroupDesc* dg = static_cast<const GroupDesc*>(p->d_groups.p);
@@ -359,33 +380,44 @@ extern "C" int pvvc_plan_info_get(const pvvc_plan* p, pvvc_plan_info* info) {
     info->group_ctas = p->grp_ctas;
     info->tune = p->tune;
     if (p->nslices > 0)
-        info->kernels = (p->nintra > 0) + 1 + (p->ngroups_a > 0) + (p->nlist_a > 0) + (p->ngroups_b > 0) + (p->nlist_b > 0);
+        info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) + (p->ngroups_a > 0) + (p->nlist_a > 0) + (p->ngroups_b > 0) + (p->nlist_b > 0);
     return PVVC_OK;
 }
 
 namespace {
 // device time of `reps` decodes of `p` (ms each), or a negative value on error
+// Mean device time of one decode of plan p, as the decode is meant to run:
+// captured once into a CUDA graph and replayed on s (stream launches time
+// differently where a plan runs kernels side by side).
 float time_plan(pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb, int32_t* status,
                 DevBuf& ws, int reps, cudaStream_t s) {
     if (ws.ensure(p->ws_bytes) != cudaSuccess) return -1.f;
-    // one untimed decode (first touch of the workspace, L2 state)
-    if (run_decode(p, st, payload, xyz, rgb, nullptr, status, ws.p, ws.cap, s, nullptr)) return -1.f;
-    cudaEvent_t e0, e1;
-    if (cudaEventCreate(&e0) != cudaSuccess) return -1.f;
-    if (cudaEventCreate(&e1) != cudaSuccess) {
-        cudaEventDestroy(e0);
-        return -1.f;
-    }
+    cudaStream_t cs = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
     float ms = -1.f;
-    bool ok = cudaEventRecord(e0, s) == cudaSuccess;
-    for (int r = 0; ok && r < reps; ++r) ok = run_decode(p, st, payload, xyz, rgb, nullptr, status, ws.p, ws.cap, s, nullptr) == PVVC_OK;
+    bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+        const int rc = run_decode(p, st, payload, xyz, rgb, nullptr, status, ws.p, ws.cap, cs, nullptr);
+        ok = cudaStreamEndCapture(cs, &g) == cudaSuccess && rc == PVVC_OK && g;
+    }
+    ok = ok && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+    ok = ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+    ok = ok && cudaGraphLaunch(ge, s) == cudaSuccess;  // untimed: first touch of the workspace, L2 state
+    ok = ok && cudaEventRecord(e0, s) == cudaSuccess;
+    for (int r = 0; ok && r < reps; ++r) ok = cudaGraphLaunch(ge, s) == cudaSuccess;
     if (ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
         cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
         ms /= reps;
     else
         ms = -1.f;
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (ge) cudaGraphExecDestroy(ge);
+    if (g) cudaGraphDestroy(g);
+    if (cs) cudaStreamDestroy(cs);
     return ms;
 }
 }  // namespace
@@ -409,17 +441,21 @@ extern "C" int pvvc_plan_autotune(const pvvc_batch_desc* desc, pvvc_state* st, c
     float cur_ms = time_plan(&probe, st, payload, dx, dr, ds, ws, reps, s);
     if (cur_ms < 0) return PVVC_ERR_CUDA;
     // coordinate search: each field in turn over its candidates, twice
-    const int32_t ctas[] = {1, 2, 3};
+    const int32_t ctas[] = {1, 2, 3, 4};
     const int32_t groups[] = {2, 4, 8, 16};
     const int32_t blocks[] = {32, 64, 128, 256};
+    const int32_t longs[] = {-1, 16, 32, 48, 64, 96};
     for (int pass = 0; pass < 2; ++pass) {
         bool moved = false;
-        for (int field = 0; field < 3; ++field) {
-            const int32_t* cand = field == 0 ? ctas : field == 1 ? groups : blocks;
-            const int nc = field == 0 ? 3 : 4;
+        for (int field = 0; field < 4; ++field) {
+            const int32_t* cand = field == 0 ? ctas : field == 1 ? groups : field == 2 ? blocks : longs;
+            const int nc = field == 3 ? 6 : 4;
             for (int c = 0; c < nc; ++c) {
                 pvvc_tune t = cur;
-                int32_t* f = field == 0 ? &t.group_ctas_per_sm : field == 1 ? &t.min_group : &t.rlgr_block;
+                int32_t* f = field == 0 ? &t.group_ctas_per_sm
+                           : field == 1 ? &t.min_group
+                           : field == 2 ? &t.rlgr_block
+                                        : &t.rlgr_long_ctas;
                 if (*f == cand[c]) continue;
                 *f = cand[c];
                 pvvc_plan pl;

@@ -15,7 +15,7 @@ namespace pvvc {
 cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payload, const StateView& st, int32_t* tstatus,
                         cudaStream_t s);
 cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
-                        int32_t* rstatus, int block, cudaStream_t s);
+                        int32_t* rstatus, int block, int smem, cudaStream_t s);
 cudaError_t prepare_kernels();
 cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int count, const StateView& st, const float* coef,
                               float* fallback, const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz,
@@ -26,10 +26,12 @@ cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, in
                               uint64_t scratch_floats, int nctas, int* counter, cudaStream_t s);
 
 // default launch shapes: persistent CTAs of the group kernel per SM (its
-// ~57 KB of staging allows three), the group threshold, the RLGR block
+// registers allow four), the group threshold, the RLGR block, and
+// the CTAs that decode the longest slices on SMs of their own
 constexpr int kGroupCtasPerSm = 3;
 constexpr int kMinGroup = 4;
 constexpr int kRlgrBlock = 128;
+constexpr int kRlgrLongCtas = 32;
 
 // the SM count (queried once)
 inline int sm_count() {
@@ -61,6 +63,27 @@ struct DevBuf {
         cap = 0;
         cudaError_t e = cudaMalloc(&p, n);
         if (e == cudaSuccess) cap = n;
+        return e;
+    }
+};
+// a second stream and fork/join events, so that a decode can run two kernels
+// side by side (also under stream capture, where they become graph branches)
+struct SideStream {
+    cudaStream_t s = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    SideStream() = default;
+    SideStream(const SideStream&) = delete;
+    SideStream& operator=(const SideStream&) = delete;
+    ~SideStream() {
+        if (fork) cudaEventDestroy(fork);
+        if (join) cudaEventDestroy(join);
+        if (s) cudaStreamDestroy(s);
+    }
+    cudaError_t ensure() {
+        cudaError_t e = cudaSuccess;
+        if (!s) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess && !fork) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+        if (e == cudaSuccess && !join) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
         return e;
     }
 };
@@ -101,6 +124,8 @@ struct pvvc_plan {
     int32_t nlist_a = 0, nlist_b = 0, list_a_off = 0, list_b_off = 0;
     pvvc::DevBuf d_work, d_order, d_groups, d_idx;
     pvvc::HostBuf h_work, h_order, h_groups, h_idx;  // pinned mirrors of stream-ordered uploads
+    int32_t nlong = 0;       // the first nlong slices of `order` go to the long-slice RLGR launch
+    pvvc::SideStream side;   // its stream
 };
 
 struct pvvc_state {

@@ -272,21 +272,20 @@ __global__ void __launch_bounds__(T) k_tree(const SliceWork* __restrict__ work, 
 // ---------------------------------------------------------------------------
 // k_rlgr
 //
-// Bit reader: the unconsumed bits are the low 32-o bits of `hi` followed by
-// `lo`; `nx` is loaded one word ahead so a refill never waits on memory.
-// peek() returns the next 32 bits with one funnel shift.  Words past the
+// Bit window: the stream continues at bit `o` (0..31, counted from the MSB)
+// of `hi`, then `mid`, then `lo` -- 96 - o >= 65 bits in registers, so any
+// 32 bits starting up to 32 bits ahead can be peeked without a refill, and
+// one advance (at most 64 bits) per loop iteration consumes a whole zero run
+// plus a Golomb-Rice code.  Words come from 16-byte blocks: `cur` holds the
+// block words are taken from, `nxt` the following block, loaded when `cur`
+// became current, four words ahead of its first use.  Blocks past the
 // payload read as zero.
 struct BitReader {
-    // Payload words W[0..] (big-endian), read as 16-byte blocks: `cur` holds the
-    // block words are taken from, `nxt` the following block, loaded when `cur`
-    // became current -- four words (about thirty codes) before it is needed,
-    // so taking a word never waits on memory.  Blocks past the payload read
-    // as zero.  The window is hi:lo with `o` bits of hi consumed.
     const uint4* p;      // next block to load
     const uint4* end;    // one past the last block holding payload bytes
     uint4 cur, nxt;
     uint32_t k;          // index in cur of the next word to enter the window
-    uint32_t hi, lo;
+    uint32_t hi, mid, lo;
     uint32_t o;
     uint32_t taken;      // words that have entered the window
 
@@ -296,19 +295,15 @@ struct BitReader {
         ++p;
         return v;
     }
-    __device__ __forceinline__ uint32_t word(uint32_t i) const {
-        const uint32_t v = i == 0 ? cur.x : i == 1 ? cur.y : i == 2 ? cur.z : cur.w;
-        return __byte_perm(v, 0, 0x0123);
-    }
-    __device__ __forceinline__ uint32_t take() {  // next word of the stream
-        const uint32_t v = word(k);
+    __device__ __forceinline__ uint32_t take() {  // next big-endian word of the stream
+        const uint32_t v = k == 0 ? cur.x : k == 1 ? cur.y : k == 2 ? cur.z : cur.w;
         ++taken;
         if (++k == 4) {
             k = 0;
             cur = nxt;
             nxt = load();
         }
-        return v;
+        return __byte_perm(v, 0, 0x0123);
     }
     __device__ __forceinline__ void init(const uint8_t* payload, uint64_t off, uint32_t nbytes) {
         p = reinterpret_cast<const uint4*>(payload + (off & ~15ull));
@@ -318,26 +313,40 @@ struct BitReader {
         k = 0;
         taken = 0;
         hi = take();
+        mid = take();
         lo = take();
         o = (uint32_t)(off & 15) * 8;
         while (o >= 32) {
             o -= 32;
-            hi = lo;
-            lo = take();
+            shift();
         }
     }
-    __device__ __forceinline__ uint32_t peek() const { return __funnelshift_l(lo, hi, o); }
-    __device__ __forceinline__ void consume(uint32_t n) {  // n <= 32
-        o += n;
-        if (o >= 32) {
-            o -= 32;
-            hi = lo;
-            lo = take();
+    __device__ __forceinline__ void shift() {
+        hi = mid;
+        mid = lo;
+        lo = take();
+    }
+    // 32 bits starting `at` bits ahead (at <= 32)
+    __device__ __forceinline__ uint32_t peek(uint32_t at = 0) const {
+        const uint32_t s = o + at;
+        const bool second = s >= 32;
+        return __funnelshift_l(second ? lo : mid, second ? mid : hi, s);  // shift taken mod 32
+    }
+    __device__ __forceinline__ void advance(uint32_t n) {  // n <= 64
+        uint32_t s = o + n;
+        if (s >= 32) {
+            s -= 32;
+            shift();
+            if (s >= 32) {
+                s -= 32;
+                shift();
+            }
         }
+        o = s;
     }
     // payload bits consumed (words before hi, plus o, minus the leading skip)
     __device__ __forceinline__ int64_t consumed(uint64_t off) const {
-        return ((int64_t)taken - 2) * 32 + (int64_t)o - (int64_t)(off & 15) * 8;
+        return ((int64_t)taken - 3) * 32 + (int64_t)o - (int64_t)(off & 15) * 8;
     }
 };
 
@@ -349,12 +358,13 @@ constexpr uint32_t kRlU0 = 3, kRlU1 = 2, kRlD0 = 1, kRlD1 = 1, kRlMaxRP = 32 * 4
 // S(n) = sum_{i<n} 2^(i>>1) = 2 (2^(n>>1) - 1) + (n & 1) 2^(n>>1):
 //   kP & 3 in {0,1}:  sum = 2^(kP>>2) S(c)
 //   kP & 3 in {2,3}:  sum = 2^(kP>>2) (S(c+1) - 1)
-// c <= 32 and kP >> 2 <= 31 keep the result below 2^49.
-__device__ __forceinline__ uint64_t run_ones_length(uint32_t kP, uint32_t c) {
+// Every term is below 2^k with k = (kP + 2c) >> 2, so when the whole run code
+// (c ones, a zero, k bits) fits 32 bits the length fits 32 bits too.
+__device__ __forceinline__ uint32_t run_ones_length(uint32_t kP, uint32_t c) {
     const uint32_t hi = (kP >> 1) & 1u;  // exponent pairs start one late
     const uint32_t n = c + hi;
-    const uint64_t h = 1ull << (n >> 1);
-    const uint64_t S = 2 * (h - 1) + (n & 1u) * h - hi;
+    const uint32_t h = 1u << (n >> 1);
+    const uint32_t S = 2 * (h - 1) + (n & 1u) * h - hi;
     return S << (kP >> 2);
 }
 
@@ -367,12 +377,13 @@ __device__ __forceinline__ uint64_t run_ones_length(uint32_t kP, uint32_t c) {
 // One iteration = an optional zero run (run mode, kP >= 4) followed by one
 // Golomb-Rice symbol, or a run that ends the slice.  The common case is one
 // straight line that every lane of a warp executes in step, whatever mode
-// its slice is in: the run's leading ones are counted with one clz and summed
-// in closed form (run_ones_length), the run's terminator and k bits and the
-// symbol's code are each taken from one 32-bit peek.  Rare cases leave the
-// line: 31+ leading ones or a run code longer than 32 bits, a Golomb-Rice
-// code longer than 32 bits (wide remainders, the 32-ones escape), symbols of
-// 2^23 or more, and runs that reach the end of a plane.
+// its slice is in (a lane outside run mode computes an empty run): the run's
+// leading ones are counted with one clz and summed in closed form
+// (run_ones_length), the run code and the symbol's code are both read from
+// the 96-bit window and consumed by one advance.  Rare cases leave the line:
+// a run code longer than 32 bits, a Golomb-Rice code longer than 32 bits
+// (wide remainders, the 32-ones escape), symbols of 2^23 or more, and runs
+// that reach the end of a plane.
 template <int T>
 __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, const int32_t* __restrict__ order,
                                               int nslices, const uint8_t* __restrict__ payload, float* __restrict__ coef,
@@ -388,8 +399,9 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
         return;
     }
     const uint64_t off = wk.col_off;
+    const uint32_t csz = wk.csz;
     BitReader br;
-    br.init(payload, off, wk.csz);
+    br.init(payload, off, csz);
     const int64_t cs = wk.coef_stride;
     const int64_t wrap = (int64_t)(2 * N - 1) * cs;  // last coefficient of a plane -> top of the next
     float* dst = coef + wk.coef_off + (uint64_t)(N - 1) * cs + wk.coef_lane;  // coefficient of the next symbol
@@ -400,39 +412,42 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
     for (;;) {
         // ---- zero run (entropy_codec.cc:226-241) ----
         const bool run = kP >= 4;
-        uint32_t v = br.peek();
+        const uint32_t v = br.peek();
         uint32_t c = run ? __clz(~v) : 0u;       // leading ones
         uint32_t kP2 = kP + 2 * c;               // kP after the ones
-        uint32_t k = run ? (kP2 >> 2) : 0u;      // bits of the run's remainder
-        uint64_t m = 0;
-        if (run && c + 1 + k <= 32) {
-            m = run_ones_length(kP, c) + (uint32_t)((uint64_t)((v << c) << 1) >> (32 - k));
-            br.consume(c + 1 + k);
-        } else if (run) {  // 31+ ones, or the remainder runs past this peek
-            m = 0;
-            k = kP >> 2;
+        const uint32_t k = run ? (kP2 >> 2) : 0u;
+        uint32_t r = run ? c + 1 + k : 0u;       // bits of the run code
+        uint32_t m;                              // zeros in the run
+        if (r <= 32) {
+            const uint32_t tail = (v << c) << 1;  // the k remainder bits, left-aligned
+            m = run ? run_ones_length(kP, c) + (k ? tail >> (32 - k) : 0u) : 0u;
+        } else {  // 31+ ones, or the remainder runs past 32 bits
+            uint64_t m64 = 0;
+            uint32_t kk = kP >> 2;
             kP2 = kP;
             int guard = 0;
             do {
                 c = __clz(~br.peek());
                 for (uint32_t i = 0; i < c; ++i) {
-                    m += 1ull << (k & 31);
+                    m64 += 1ull << (kk & 31);
                     kP2 += kRlU1;
-                    k = kP2 >> 2;
+                    kk = kP2 >> 2;
                 }
-                br.consume(c);
+                br.advance(c);
             } while (c == 32 && ++guard < 64);
-            br.consume(1);
-            if (k > 31) {
+            br.advance(1);
+            if (kk > 31) {
                 err = PVVC_ERR_OVERRUN;
                 break;
             }
-            m += br.peek() >> (32 - k);
-            br.consume(k);
+            m64 += br.peek() >> (32 - kk);
+            br.advance(kk);
+            m = m64 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)m64;
+            r = 0;  // consumed
         }
-        if (run) {
-            // skip m zeros (they may cross plane boundaries)
-            uint32_t z = m < left ? (uint32_t)m : left;
+        // skip m zeros (they may cross plane boundaries)
+        {
+            uint32_t z = m < left ? m : left;
             left -= z;
             if (z < rem) {
                 dst -= (int64_t)z * cs;
@@ -446,33 +461,37 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
                 dst -= (int64_t)z * cs;
                 rem -= z;
             }
-            if (left == 0) break;
+        }
+        if (left == 0) {
+            br.advance(r);
+            break;
         }
         // ---- Golomb-Rice symbol (GRRead, entropy_codec.cc:196-205) ----
         const uint32_t kR = kRP >> 2;
-        v = br.peek();
-        const uint32_t q = __clz(~v);
+        const uint32_t v2 = br.peek(r);
+        const uint32_t q = __clz(~v2);
+        const uint32_t len = q + 1 + kR;
         uint32_t u, pq;
         uint64_t uw;
         bool wide;  // u does not fit the fast symbol path
-        if (q + 1 + kR <= 32) {  // the whole code is in this peek
-            u = (q << kR) | (uint32_t)((uint64_t)((v << q) << 1) >> (32 - kR));
-            br.consume(q + 1 + kR);
+        if (len <= 32) {  // the whole code is in this peek
+            u = (q << kR) | ((v2 >> (32 - len)) & ((1u << kR) - 1u));
+            br.advance(r + len);
             pq = q;
             uw = u;
             wide = u >= (1u << 23);
         } else if (q < 32) {
-            br.consume(q + 1);
-            const uint32_t r = kR == 32 ? br.peek() : (br.peek() >> (32 - kR));
-            br.consume(kR);
-            uw = ((uint64_t)q << kR) | r;
+            br.advance(r + q + 1);
+            const uint32_t rr = kR == 32 ? br.peek() : (br.peek() >> (32 - kR));
+            br.advance(kR);
+            uw = ((uint64_t)q << kR) | rr;
             u = (uint32_t)uw | (uint32_t)(uw >> 32);  // nonzero iff uw is
             pq = q;
             wide = true;
         } else {  // 32 ones: a raw 32-bit value follows
-            br.consume(32);
+            br.advance(r + 32);
             u = br.peek();
-            br.consume(32);
+            br.advance(32);
             uw = u;
             // p may be far above the kRP cap; any p > kRlMaxRP saturates
             // kRP + p - 1 at the cap (kRP >= 0), so clamp p to kRlMaxRP + 1,
@@ -502,7 +521,7 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
     }
     // bits consumed vs the payload (the reference reads past it, which is undefined)
     if (!err) {
-        if (br.consumed(off) > 8ll * wk.csz) err = PVVC_ERR_OVERRUN;
+        if (br.consumed(off) > 8ll * csz) err = PVVC_ERR_OVERRUN;
     }
     rstatus[item] = err;
 }
@@ -819,27 +838,43 @@ __device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool
 
 
 // k_raht_group: persistent CTAs; each takes the next group of slices that
-// share a slot (the frames of one patch) from a queue.  Its 8 warps split the
-// nodes of each level; lane f of every warp owns frame f (same control flow
-// in all lanes, node records are broadcast loads).  The level signal lives in
-// the CTA's own scratch region as [node][lane][yuv], so warp accesses are
-// contiguous.  The intra slice, when the group has one, is lane 0 and hands
-// its leaf colours to the predictive lanes by shuffle.  The last level runs
-// in chunks of 8 nodes whose leaves are consecutive: each chunk's finished
-// points are staged in shared memory and written per frame as contiguous,
-// coalesced runs.
+// share a slot (the frames of one patch) from a queue.  Lane f of every warp
+// owns frame f (same control flow in all lanes, node records are broadcast
+// loads).  The intra slice, when the group has one, is lane 0 and hands its
+// leaf colours to the predictive lanes by shuffle.
+//
+// Levels above the last internal one: the 8 warps split each level's nodes
+// and the CTA synchronises per level.  The level signal lives in the CTA's
+// own scratch region as [node][yuv][lane], so each warp access is one
+// 128-byte line.
+//
+// Last internal level (most of the nodes): warp w takes a contiguous range
+// of nodes, whose leaves are contiguous too, and stages its finished points
+// in its own shared-memory rows [frame][leaf]; when the next node's leaves
+// would not fit, the warp writes the staged leaves of every frame as
+// contiguous runs and goes on -- no CTA-wide barrier at this level.
 constexpr int kGrpWarps = 8;
-constexpr int kStageLeaves = 8 * kGrpWarps;  // leaves of 8 nodes at most
+constexpr int kWarpLeaves = 16;              // staged leaves per warp (a node adds <= 8)
+constexpr int kStageRow = kWarpLeaves + 1;   // odd row length: the 32 lanes' column stores hit 32 banks
+static_assert(kWarpLeaves == 16, "the flush maps a frame's staged leaves onto a half-warp");
 
-// Rows are one word longer than kStageLeaves so that the 32 lanes, which
-// store to the same column of their own rows, hit 32 different banks.
-constexpr int kStageRow = kStageLeaves + 1;
-struct GroupStage {
-    float x[32][kStageRow], y[32][kStageRow], z[32][kStageRow];
+// A warp stages colours only: leaf centres are the same in every frame of
+// the group, and the flush transforms them with each frame's matrix.
+template <bool P24>
+struct WarpStage {
+    uint32_t rgb[32][kStageRow];
+};
+template <>
+struct WarpStage<true> {
     uint32_t rgb[32][kStageRow];
     float fr[32][kStageRow], fg[32][kStageRow], fb[32][kStageRow];  // points24 colours
 };
+template <bool P24>
+struct GroupStage {
+    WarpStage<P24> w[kGrpWarps];
+};
 
+template <bool P24>
 __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* __restrict__ work,
                                                                const GroupDesc* __restrict__ groups, int ngroups,
                                                                const int32_t* __restrict__ items, StateView st,
@@ -850,12 +885,13 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
                                                                float* __restrict__ scratch, uint64_t scratch_floats,
                                                                int* __restrict__ counter) {
     extern __shared__ __align__(16) unsigned char s_raw[];
-    GroupStage& sg = *reinterpret_cast<GroupStage*>(s_raw);
+    GroupStage<P24>& sg = *reinterpret_cast<GroupStage<P24>*>(s_raw);
     __shared__ int s_g, s_H, s_ls[kMaxLevels + 1];
     __shared__ uint64_t s_out[32];
     __shared__ int s_act[32], s_white[32];
-    __shared__ uint32_t s_base, s_end;
+    __shared__ float s_mv[32][13];  // each frame's transform rows (odd stride: the lanes' row fills hit 32 banks)
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    WarpStage<P24>& ws = sg.w[wid];
     float* const bufA = scratch + (uint64_t)blockIdx.x * scratch_floats;
     float* const bufB = bufA + scratch_floats / 2;
     for (;;) {
@@ -881,6 +917,8 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
             s_act[lane] = act;
             s_out[lane] = act ? w.out_off : 0;
             s_white[lane] = act && w.n < 10;
+#pragma unroll
+            for (int i = 0; i < 12; ++i) s_mv[lane][i] = act ? w.mv[i] : 0.f;
         }
         const bool any = __any_sync(0xffffffffu, act);  // the same in every warp
         const bool ref_lane0 = G.intra && !ierr;
@@ -899,8 +937,7 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
             const float* cy = coef + (act ? w.coef_off + lane : 0);
             const float* cu = cy + (size_t)N * 32;
             const float* cv = cu + (size_t)N * 32;
-            const float* m = w.mv;
-            // one finished leaf of this lane's frame into the stage
+            // one finished leaf of this lane's frame into the warp's stage
             auto finish = [&](uint32_t leaf, uint32_t slot_local, float y, float u, float v) {
                 float ry, ru, rv;
                 if (ref_lane0) {
@@ -924,70 +961,76 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
                     u = __fadd_rn(u, ru);
                     v = __fadd_rn(v, rv);
                 }
-                const float* p = st.xyz + (lb + leaf) * 3;
-                const float x0 = __ldg(p), y0 = __ldg(p + 1), z0 = __ldg(p + 2);
-                sg.x[lane][slot_local] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
-                sg.y[lane][slot_local] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
-                sg.z[lane][slot_local] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
                 const float du = __fsub_rn(u, 128.0f), dv = __fsub_rn(v, 128.0f);
                 const float R = __fadd_rn(y, __fmul_rn(1.4020f, dv));
                 const float Gc = __fsub_rn(__fsub_rn(y, __fmul_rn(0.3441f, du)), __fmul_rn(0.7141f, dv));
                 const float B = __fadd_rn(y, __fmul_rn(1.7720f, du));
-                sg.rgb[lane][slot_local] = (uint32_t)to_u8(R) | ((uint32_t)to_u8(Gc) << 8) | ((uint32_t)to_u8(B) << 16);
-                if (o.p24) {
-                    sg.fr[lane][slot_local] = __fdiv_rn(R, 255.0f);
-                    sg.fg[lane][slot_local] = __fdiv_rn(Gc, 255.0f);
-                    sg.fb[lane][slot_local] = __fdiv_rn(B, 255.0f);
+                ws.rgb[lane][slot_local] = (uint32_t)to_u8(R) | ((uint32_t)to_u8(Gc) << 8) | ((uint32_t)to_u8(B) << 16);
+                if constexpr (P24) {
+                    ws.fr[lane][slot_local] = __fdiv_rn(R, 255.0f);
+                    ws.fg[lane][slot_local] = __fdiv_rn(Gc, 255.0f);
+                    ws.fb[lane][slot_local] = __fdiv_rn(B, 255.0f);
                 }
             };
-            // write the staged leaves [s_base, s_end) of every active frame
-            auto flush = [&]() {
-                const uint32_t base = s_base, cnt = s_end - s_base;
-                for (uint32_t t = tid; t < 32 * cnt; t += 32 * kGrpWarps) {
-                    const uint32_t f = t / cnt, i = t - f * cnt;
-                    if (!s_act[f]) continue;
+            // the warp writes its staged leaves [base, base + cnt) of every active
+            // frame, two frames per pass: half-warp h writes frame f0 + h, its
+            // lanes consecutive points of that frame.  The leaf centre (read
+            // once) goes through the frame's transform here.
+            auto flush = [&](uint32_t base, uint32_t cnt) {
+                __syncwarp();
+                const uint32_t i = lane & 15, h = lane >> 4;
+                float x0 = 0.f, y0 = 0.f, z0 = 0.f;
+                if (i < cnt) {
+                    const float* p = st.xyz + (lb + base + i) * 3;
+                    x0 = __ldg(p);
+                    y0 = __ldg(p + 1);
+                    z0 = __ldg(p + 2);
+                }
+                for (uint32_t f0 = 0; f0 < 32; f0 += 2) {
+                    const uint32_t f = f0 + h;
+                    if (i >= cnt || !s_act[f]) continue;
                     const uint64_t oi = s_out[f] + base + i;
+                    const float* m = s_mv[f];
+                    const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
+                    const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
+                    const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
                     if (o.xyz) {
-                        o.xyz[oi * 3 + 0] = sg.x[f][i];
-                        o.xyz[oi * 3 + 1] = sg.y[f][i];
-                        o.xyz[oi * 3 + 2] = sg.z[f][i];
+                        o.xyz[oi * 3 + 0] = X;
+                        o.xyz[oi * 3 + 1] = Y;
+                        o.xyz[oi * 3 + 2] = Z;
                     }
-                    const uint32_t c = sg.rgb[f][i];
+                    const uint32_t c = ws.rgb[f][i];
                     if (o.rgb) {
                         o.rgb[oi * 3 + 0] = (uint8_t)c;
                         o.rgb[oi * 3 + 1] = (uint8_t)(c >> 8);
                         o.rgb[oi * 3 + 2] = (uint8_t)(c >> 16);
                     }
-                    if (o.p24) {
+                    if constexpr (P24) {
                         float* q = o.p24 + oi * 6;
                         const bool white = s_white[f];
-                        q[0] = sg.x[f][i];
-                        q[1] = sg.y[f][i];
-                        q[2] = sg.z[f][i];
-                        q[3] = white ? 1.0f : sg.fr[f][i];
-                        q[4] = white ? 1.0f : sg.fg[f][i];
-                        q[5] = white ? 1.0f : sg.fb[f][i];
+                        q[0] = X;
+                        q[1] = Y;
+                        q[2] = Z;
+                        q[3] = white ? 1.0f : ws.fr[f][i];
+                        q[4] = white ? 1.0f : ws.fg[f][i];
+                        q[5] = white ? 1.0f : ws.fb[f][i];
                     }
                 }
+                __syncwarp();
             };
             if (H == 1) {
                 if (wid == 0) {
                     const float gy = act ? cy[0] : 0.f, gu = act ? cu[0] : 0.f, gv = act ? cv[0] : 0.f;
                     finish(0, 0, gy, gu, gv);
+                    flush(0, 1);
                 }
-                if (tid == 0) {
-                    s_base = 0;
-                    s_end = 1;
-                }
-                __syncthreads();
-                flush();
             } else {
                 float* gA = bufA;
                 float* gB = bufB;
                 if (wid == 0) {
-                    gA[lane * 3 + 0] = act ? cy[0] : 0.f;
-                    gA[lane * 3 + 1] = act ? cu[0] : 0.f;
-                    gA[lane * 3 + 2] = act ? cv[0] : 0.f;
+                    gA[lane] = act ? cy[0] : 0.f;
+                    gA[32 + lane] = act ? cu[0] : 0.f;
+                    gA[64 + lane] = act ? cv[0] : 0.f;
                 }
                 __syncthreads();
                 for (int l = 0; l < H - 2; ++l) {  // internal levels above the last
@@ -995,18 +1038,18 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
                     for (int j = wid; j < b - a; j += kGrpWarps) {
                         const size_t node = nb + a + j;
                         const uint32_t byte = __ldg(st.occ + node), cb = __ldg(st.cbase + node);
-                        const float* g3 = gA + ((size_t)j * 32 + lane) * 3;
+                        const float* g3 = gA + (size_t)j * 96 + lane;
                         float oy[8], ou[8], ov[8];
-                        lane_node<32>(st, node, act, cy, cu, cv, g3[0], g3[1], g3[2], oy, ou, ov);
+                        lane_node<32>(st, node, act, cy, cu, cv, g3[0], g3[32], g3[64], oy, ou, ov);
                         uint32_t r = 0;
 #pragma unroll
                         for (int c = 0; c < 8; ++c) {
                             if (!(byte & (0x80u >> c))) continue;
-                            float* go = gB + ((size_t)(cb + r) * 32 + lane) * 3;
+                            float* go = gB + (size_t)(cb + r) * 96 + lane;
                             ++r;
                             go[0] = oy[c];
-                            go[1] = ou[c];
-                            go[2] = ov[c];
+                            go[32] = ou[c];
+                            go[64] = ov[c];
                         }
                     }
                     __syncthreads();
@@ -1014,39 +1057,34 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
                     gA = gB;
                     gB = t;
                 }
-                // last internal level: chunks of 8 consecutive nodes
-                const int a = s_ls[H - 2], b = s_ls[H - 1];
-                for (int j0 = 0; j0 < b - a; j0 += kGrpWarps) {
-                    const int j = j0 + wid;
-                    const bool mine = j < b - a;
-                    uint32_t byte = 0, cb = 0;
-                    if (mine) {
-                        const size_t node = nb + a + j;
-                        byte = __ldg(st.occ + node);
-                        cb = __ldg(st.cbase + node);
+                // last internal level: a contiguous node range per warp
+                const int a = s_ls[H - 2], cnt = s_ls[H - 1] - a;
+                const int per = (cnt + kGrpWarps - 1) / kGrpWarps;
+                const int j0 = min(cnt, wid * per), j1 = min(cnt, j0 + per);
+                uint32_t base = 0, staged = 0;
+                if (j0 < j1) base = __ldg(st.cbase + nb + a + j0);
+                for (int j = j0; j < j1; ++j) {
+                    const size_t node = nb + a + j;
+                    const uint32_t byte = __ldg(st.occ + node), cb = __ldg(st.cbase + node);
+                    const uint32_t k = __popc(byte);
+                    if (staged + k > (uint32_t)kWarpLeaves) {
+                        flush(base, staged);
+                        base += staged;
+                        staged = 0;
                     }
-                    if (lane == 0 && wid == 0) s_base = cb;
-                    const int lastw = min(kGrpWarps, b - a - j0) - 1;
-                    if (lane == 0 && wid == lastw) s_end = cb + __popc(byte);
-                    __syncthreads();
-                    if (mine) {
-                        const size_t node = nb + a + j;
-                        const float* g3 = gA + ((size_t)j * 32 + lane) * 3;
-                        float oy[8], ou[8], ov[8];
-                        lane_node<32>(st, node, act, cy, cu, cv, g3[0], g3[1], g3[2], oy, ou, ov);
-                        const uint32_t base = s_base;
-                        uint32_t r = 0;
+                    const float* g3 = gA + (size_t)j * 96 + lane;
+                    float oy[8], ou[8], ov[8];
+                    lane_node<32>(st, node, act, cy, cu, cv, g3[0], g3[32], g3[64], oy, ou, ov);
+                    uint32_t r = 0;
 #pragma unroll
-                        for (int c = 0; c < 8; ++c) {
-                            if (!(byte & (0x80u >> c))) continue;
-                            finish(cb + r, cb + r - base, oy[c], ou[c], ov[c]);
-                            ++r;
-                        }
+                    for (int c = 0; c < 8; ++c) {
+                        if (!(byte & (0x80u >> c))) continue;
+                        finish(cb + r, cb + r - base, oy[c], ou[c], ov[c]);
+                        ++r;
                     }
-                    __syncthreads();
-                    flush();
-                    __syncthreads();
+                    staged = cb + k - base;
                 }
+                if (staged) flush(base, staged);
             }
         }
         __syncthreads();
@@ -1071,7 +1109,15 @@ cudaError_t prepare_kernels() {
     if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
     e = cudaFuncSetAttribute(k_raht_slice<kRahtThreads>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_raht_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupStage));
+        e = cudaFuncSetAttribute(k_raht_group<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(GroupStage<false>));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_raht_group<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(GroupStage<true>));
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rlgr<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rlgr<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rlgr<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rlgr<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
     if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return e;
 }
@@ -1083,15 +1129,17 @@ cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payloa
     return cudaGetLastError();
 }
 
+// smem: dynamic shared memory reserved per CTA (unused by the kernel; it
+// limits which CTAs share an SM, see kRlgrLongSmem)
 cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
-                        int32_t* rstatus, int block, cudaStream_t s) {
+                        int32_t* rstatus, int block, int smem, cudaStream_t s) {
     if (nslices <= 0) return cudaSuccess;
     const int grid = (nslices + block - 1) / block;
     switch (block) {
-        case 32: k_rlgr<32><<<grid, 32, 0, s>>>(work, order, nslices, payload, coef, rstatus); break;
-        case 64: k_rlgr<64><<<grid, 64, 0, s>>>(work, order, nslices, payload, coef, rstatus); break;
-        case 128: k_rlgr<128><<<grid, 128, 0, s>>>(work, order, nslices, payload, coef, rstatus); break;
-        case 256: k_rlgr<256><<<grid, 256, 0, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 32: k_rlgr<32><<<grid, 32, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 64: k_rlgr<64><<<grid, 64, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 128: k_rlgr<128><<<grid, 128, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 256: k_rlgr<256><<<grid, 256, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -1116,8 +1164,12 @@ cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, in
     if (cudaMemsetAsync(counter, 0, sizeof(int), s) != cudaSuccess) return cudaGetLastError();
     OutPtrs o{xyz, rgb, p24, status};
     const int grid = ngroups < nctas ? ngroups : nctas;
-    k_raht_group<<<grid, 32 * kGrpWarps, sizeof(GroupStage), s>>>(work, groups, ngroups, items, st, coef, tstatus, rstatus,
-                                                                  fstatus, o, scratch, scratch_floats, counter);
+    if (p24)
+        k_raht_group<true><<<grid, 32 * kGrpWarps, sizeof(GroupStage<true>), s>>>(
+            work, groups, ngroups, items, st, coef, tstatus, rstatus, fstatus, o, scratch, scratch_floats, counter);
+    else
+        k_raht_group<false><<<grid, 32 * kGrpWarps, sizeof(GroupStage<false>), s>>>(
+            work, groups, ngroups, items, st, coef, tstatus, rstatus, fstatus, o, scratch, scratch_floats, counter);
     return cudaGetLastError();
 }
 

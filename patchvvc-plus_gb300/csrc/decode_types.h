@@ -9,6 +9,16 @@ namespace pvvc {
 constexpr int kMaxLevels = 32;  // octree height limit (the header stores a u8)
 
 // One slice in the work queue (queue order = intra first, then by size).
+// RLGR launches split by slice length: a CTA of the long-slice launch (128
+// threads, one warp per scheduler) reserves this much dynamic shared memory,
+// which no RLGR code uses, so that no other CTA of either launch fits on its
+// SM; a CTA of the other launch reserves kRlgrShortSmem, more than such an
+// SM has left.  The serial bit chains of the longest slices then run without
+// sharing issue slots, while the short slices fill the remaining SMs.
+constexpr int kRlgrLongSmem = 200 * 1024;
+constexpr int kRlgrShortSmem = 32 * 1024;
+constexpr int kRlgrLongBlock = 128;
+
 struct SliceWork {
     uint64_t col_off;   // colour payload byte offset
     uint64_t geo_off;   // geometry payload byte offset (intra)

@@ -69,6 +69,59 @@ def make_pairs(npairs: int, seed: int = 0, max_deg: float = 15.0, max_trans: flo
     return Pairs(src, tgt, np.array(Ts))
 
 
+def make_pairs_packed(npairs: int, seed: int = 0, max_deg: float = 15.0, max_trans: float = 20.0, noise: float = 0.5,
+                      outliers: float = 0.05, synth=None, device="cuda"):
+    """The make_pairs workload generated in one vectorised pass on `device`
+    (torch ops; for large training sets).  Returns packed device clouds
+    (src [S,3] f32, src_off [n+1] i32, tgt [T,3] f32, tgt_off [n+1] i32)
+    and T_true [n,4,4] (numpy float64)."""
+    import torch
+    from .synth import Synth, config
+    if synth is None:
+        synth = Synth(config("seq300", nframes=1, gof=1, seed=seed))
+    npat = synth.patch_count(0)
+    pats = [synth.patch(0, p)[0].astype(np.float32) for p in range(npat)]
+    dev = torch.device(device)
+    g = torch.Generator(device=dev).manual_seed(seed + 54321)
+    f64 = torch.float64
+    sizes = torch.tensor([p.shape[0] for p in pats], device=dev)
+    poff = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), torch.cumsum(sizes, 0)])
+    allp = torch.from_numpy(np.concatenate(pats)).to(dev, f64)
+    cent = torch.stack([torch.from_numpy(p.astype(np.float64).mean(0)) for p in pats]).to(dev)
+    pid = torch.randint(0, npat, (npairs,), generator=g, device=dev)
+    ax = torch.randn(npairs, 3, generator=g, device=dev, dtype=f64)
+    ax = ax / ax.norm(dim=1, keepdim=True)
+    th = torch.deg2rad(torch.rand(npairs, generator=g, device=dev, dtype=f64) * max_deg)
+    K = torch.zeros(npairs, 3, 3, device=dev, dtype=f64)
+    K[:, 0, 1], K[:, 0, 2], K[:, 1, 2] = -ax[:, 2], ax[:, 1], -ax[:, 0]
+    K[:, 1, 0], K[:, 2, 0], K[:, 2, 1] = ax[:, 2], -ax[:, 1], ax[:, 0]
+    R = torch.eye(3, device=dev, dtype=f64) + torch.sin(th)[:, None, None] * K + (1 - torch.cos(th))[:, None, None] * (K @ K)
+    t = (torch.rand(npairs, 3, generator=g, device=dev, dtype=f64) * 2 - 1) * max_trans
+    n = sizes[pid]
+    soff = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), torch.cumsum(n, 0)])
+    owner = torch.repeat_interleave(torch.arange(npairs, device=dev), n)
+    local = torch.arange(int(soff[-1]), device=dev) - soff[:-1][owner]
+    S = allp[poff[pid][owner] + local]
+    c = cent[pid]
+    Q = torch.bmm(R[owner], (S - c[owner]).unsqueeze(2)).squeeze(2) + (c + t)[owner]
+    Q = Q + torch.randn(Q.shape, generator=g, device=dev, dtype=f64) * noise
+    lo = torch.full((npairs, 3), float("inf"), device=dev, dtype=f64).scatter_reduce(0, owner[:, None].expand(-1, 3), Q, "amin")
+    hi = torch.full((npairs, 3), float("-inf"), device=dev, dtype=f64).scatter_reduce(0, owner[:, None].expand(-1, 3), Q, "amax")
+    k = torch.round(outliers * n.to(f64)).to(torch.int64)
+    oown = torch.repeat_interleave(torch.arange(npairs, device=dev), k)
+    O = lo[oown] + torch.rand(int(k.sum()), 3, generator=g, device=dev, dtype=f64) * (hi - lo)[oown]
+    toff = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), torch.cumsum(n + k, 0)])
+    tgt = torch.empty(int(toff[-1]), 3, device=dev, dtype=torch.float32)
+    tgt[toff[:-1][owner] + local] = Q.float()                      # the moved source first, then its outliers
+    kof = torch.cat([torch.zeros(1, dtype=torch.int64, device=dev), torch.cumsum(k, 0)])
+    ko = torch.arange(int(k.sum()), device=dev) - kof[:-1][oown]
+    tgt[toff[:-1][oown] + n[oown] + ko] = O.float()
+    T = torch.eye(4, device=dev, dtype=f64).repeat(npairs, 1, 1)
+    T[:, :3, :3] = R
+    T[:, :3, 3] = c + t - torch.bmm(R, c.unsqueeze(2)).squeeze(2)
+    return S.float(), soff.to(torch.int32), tgt, toff.to(torch.int32), T.cpu().numpy()
+
+
 def _pack(clouds):
     off = np.zeros(len(clouds) + 1, np.uint32)
     off[1:] = np.cumsum([c.shape[0] for c in clouds])
@@ -78,18 +131,23 @@ def _pack(clouds):
 class IcpBatch:
     """Device-resident batch of (source, target) pairs."""
 
-    def __init__(self, pairs: Pairs, device="cuda"):
+    def __init__(self, pairs: Pairs | None, device="cuda", packed=None):
+        """pairs: host clouds, or packed=(src, src_off, tgt, tgt_off) device
+        tensors as make_pairs_packed returns them."""
         import torch
         self.torch = torch
-        s, so = _pack(pairs.src)
-        t, to = _pack(pairs.tgt)
-        self.n = pairs.n
-        self.ns, self.nt = int(so[-1]), int(to[-1])
         dev = torch.device(device)
-        self.src = torch.from_numpy(s).to(dev)
-        self.tgt = torch.from_numpy(t).to(dev)
-        self.soff = torch.from_numpy(so.astype(np.int32)).to(dev)
-        self.toff = torch.from_numpy(to.astype(np.int32)).to(dev)
+        if packed is None:
+            s, so = _pack(pairs.src)
+            t, to = _pack(pairs.tgt)
+            self.src = torch.from_numpy(s).to(dev)
+            self.tgt = torch.from_numpy(t).to(dev)
+            self.soff = torch.from_numpy(so.astype(np.int32)).to(dev)
+            self.toff = torch.from_numpy(to.astype(np.int32)).to(dev)
+        else:
+            self.src, self.soff, self.tgt, self.toff = packed
+        self.n = int(self.soff.numel()) - 1
+        self.ns, self.nt = int(self.src.shape[0]), int(self.tgt.shape[0])
         b = C.c_uint64(0)
         L.check(L.lib().pvvc_icp_workspace_size(self.n, self.ns, self.nt, C.byref(b)), "pvvc_icp_workspace_size")
         self.ws = torch.empty(max(int(b.value), 256), dtype=torch.uint8, device=dev)
