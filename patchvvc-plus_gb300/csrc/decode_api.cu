@@ -4,9 +4,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <memory>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "../host/bitstream.h"
@@ -94,6 +96,21 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     for (int i : intra) fill(q++, i);
     for (int i : pred) fill(q++, i);
     p->total_points = pts;
+    // RLGR order: all slices by size, so that a warp decodes similar lengths
+    p->order.resize(n);
+    std::iota(p->order.begin(), p->order.end(), 0);
+    std::stable_sort(p->order.begin(), p->order.end(), [&](int32_t a, int32_t b) {
+        if (p->work[a].n != p->work[b].n) return p->work[a].n > p->work[b].n;
+        return p->work[a].slot < p->work[b].slot;
+    });
+    // the head of that order goes to the long-slice launch (at most a quarter
+    // of the slices, so that small batches still spread over many SMs)
+    p->nlong = 0;
+    if (p->tune.rlgr_long_ctas > 0 && n >= 8) {
+        p->nlong = std::min<int32_t>(kRlgrLongBlock * p->tune.rlgr_long_ctas, n / 4);
+        if (p->side.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+    }
+    if (!intra.empty() && p->tree.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
     // inverse-RAHT schedule: slices grouped by slot (largest slots first)
     {
         std::vector<std::vector<int32_t>> per;  // queue indices per slot, in queue order
@@ -130,6 +147,21 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
                 }
             }
         }
+        // phase-A groups that hold a slice of the long-slice RLGR launch first:
+        // the others can be inverse-transformed as soon as the short launch ends
+        {
+            std::vector<uint8_t> is_long(n, 0);
+            for (int i = 0; i < p->nlong; ++i) is_long[p->order[i]] = 1;
+            std::vector<GroupDesc> gl, gs;
+            for (const GroupDesc& g : ga) {
+                bool any = false;
+                for (int l = 0; l < g.count; ++l) any = any || is_long[items[g.first + l]];
+                (any ? gl : gs).push_back(g);
+            }
+            p->ngroups_a_long = (int32_t)gl.size();
+            ga = gl;
+            ga.insert(ga.end(), gs.begin(), gs.end());
+        }
         p->groups = ga;
         p->groups.insert(p->groups.end(), gb.begin(), gb.end());
         p->ngroups_a = (int32_t)ga.size();
@@ -163,20 +195,13 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         }
         coef = c;
         p->coef_floats = coef;
-    }
-    // RLGR order: all slices by size, so that a warp decodes similar lengths
-    p->order.resize(n);
-    std::iota(p->order.begin(), p->order.end(), 0);
-    std::stable_sort(p->order.begin(), p->order.end(), [&](int32_t a, int32_t b) {
-        if (p->work[a].n != p->work[b].n) return p->work[a].n > p->work[b].n;
-        return p->work[a].slot < p->work[b].slot;
-    });
-    // the head of that order goes to the long-slice launch (at most a quarter
-    // of the slices, so that small batches still spread over many SMs)
-    p->nlong = 0;
-    if (p->tune.rlgr_long_ctas > 0 && n >= 8) {
-        p->nlong = std::min<int32_t>(kRlgrLongBlock * p->tune.rlgr_long_ctas, n / 4);
-        if (p->side.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+        // the prefix of the planes that the long-slice RLGR launch writes
+        // (its groups come first; a long slice outside a group extends it)
+        p->coef_long_floats = 0;
+        for (int i = 0; i < p->nlong; ++i) {
+            const SliceWork& w = p->work[p->order[i]];
+            p->coef_long_floats = std::max<uint64_t>(p->coef_long_floats, w.coef_off + 3ull * w.n * w.coef_stride);
+        }
     }
     // workspace layout
     uint64_t off = 0;
@@ -245,32 +270,65 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
         return !events || cudaEventRecord(static_cast<cudaEvent_t>(events[i]), s) == cudaSuccess;
     };
     if (!mark(0)) return PVVC_ERR_CUDA;
-    if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) return PVVC_ERR_CUDA;
-    // zero symbols are not written by the decoder: clear the planes first
-    if (cudaMemsetAsync(coef, 0, 4ull * p->coef_floats, s) != cudaSuccess) return PVVC_ERR_CUDA;
+    // The tree expansion reads only geometry payloads and writes only slot
+    // tables, the coefficient clear and RLGR only colour payloads and
+    // coefficient planes: without stage markers the tree runs beside them on
+    // a stream of its own, joined before the inverse RAHT.
+    const bool tree_aside = !events && p->nintra > 0;
+    if (tree_aside) {
+        const SideStream& tr = p->tree;
+        if (cudaEventRecord(tr.fork, s) != cudaSuccess || cudaStreamWaitEvent(tr.s, tr.fork, 0) != cudaSuccess ||
+            launch_tree(dw, p->nintra, payload, st->v, ts, tr.s) != cudaSuccess || cudaEventRecord(tr.join, tr.s) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+    } else if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) {
+        return PVVC_ERR_CUDA;
+    }
+    // Zero symbols are not written by the decoder: clear the planes first.
+    // Without stage markers, only the long launch's prefix is cleared before
+    // it forks; the rest is cleared beside it, before the short launch.
+    const uint64_t clear_first = (p->nlong > 0 && !events) ? p->coef_long_floats : p->coef_floats;
+    if (cudaMemsetAsync(coef, 0, 4ull * clear_first, s) != cudaSuccess) return PVVC_ERR_CUDA;
+    float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
+    int* cnt = reinterpret_cast<int*>(w + p->ws_counter);  // queue counters: A long, B, A short
+    const GroupDesc* dg = static_cast<const GroupDesc*>(p->d_groups.p);
+    const int32_t* di = static_cast<const int32_t*>(p->d_idx.p);
+    auto raht_groups = [&](int first, int count, int* counter) {
+        return launch_raht_group(dw, dg + first, count, di, st->v, coef, ts, rs, fs, xyz, rgb, p24, status, gsc,
+                                 p->grp_floats, p->grp_ctas, counter, s) == cudaSuccess;
+    };
+    const int na_long = p->ngroups_a_long, na_short = p->ngroups_a - p->ngroups_a_long;
     if (p->nlong > 0) {
-        // the longest slices (the head of the size order) on SMs of their own,
-        // side by side with the rest
+        // The longest slices (the head of the size order) decode on SMs of
+        // their own beside the rest.  Without stage markers, the phase-A
+        // groups that hold none of them are inverse-transformed as soon as the
+        // short launch ends, still beside the long one; the others after it.
         const SideStream& sd = p->side;
         if (cudaEventRecord(sd.fork, s) != cudaSuccess || cudaStreamWaitEvent(sd.s, sd.fork, 0) != cudaSuccess ||
             launch_rlgr(dw, ord, p->nlong, payload, coef, rs, kRlgrLongBlock, kRlgrLongSmem, sd.s) != cudaSuccess ||
             cudaEventRecord(sd.join, sd.s) != cudaSuccess ||
+            (clear_first < p->coef_floats &&
+             cudaMemsetAsync(coef + clear_first, 0, 4ull * (p->coef_floats - clear_first), s) != cudaSuccess) ||
             launch_rlgr(dw, ord + p->nlong, p->nslices - p->nlong, payload, coef, rs, p->tune.rlgr_block, kRlgrShortSmem,
-                        s) != cudaSuccess ||
-            cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess || !mark(2))
+                        s) != cudaSuccess)
             return PVVC_ERR_CUDA;
-    } else if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, p->tune.rlgr_block, 0, s) != cudaSuccess || !mark(2)) {
-        return PVVC_ERR_CUDA;
+        if (events) {
+            if (cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess || !mark(2)) return PVVC_ERR_CUDA;
+            if (!raht_groups(0, p->ngroups_a, cnt)) return PVVC_ERR_CUDA;
+        } else {
+            if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;
+            if (!raht_groups(na_long, na_short, cnt + 2) || cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess ||
+                !raht_groups(0, na_long, cnt))
+                return PVVC_ERR_CUDA;
+        }
+    } else {
+        if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, p->tune.rlgr_block, 0, s) != cudaSuccess || !mark(2))
+            return PVVC_ERR_CUDA;
+        if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;
+        if (!raht_groups(0, p->ngroups_a, cnt)) return PVVC_ERR_CUDA;
     }
-    float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
-    int* cnt = reinterpret_cast<int*>(w + p->ws_counter);
-    const GroupDesc* dg = static_cast<const GroupDesc*>(p->d_groups.p);
-    const int32_t* di = static_cast<const int32_t*>(p->d_idx.p);
-    // phase A: groups holding their slot's intra slice, slots without an intra slice here
-    if (launch_raht_group(dw, dg, p->ngroups_a, di, st->v, coef, ts, rs, fs, xyz, rgb, p24, status, gsc, p->grp_floats,
-                          p->grp_ctas, cnt, s) != cudaSuccess ||
-        launch_raht_slice(dw, di + p->list_a_off, p->nlist_a, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap, s) !=
-            cudaSuccess ||
+    // phase A: the slices of slots without a group here, inverse-transformed by a CTA each
+    if (launch_raht_slice(dw, di + p->list_a_off, p->nlist_a, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap,
+                          s) != cudaSuccess ||
         !mark(3))
         return PVVC_ERR_CUDA;
     // phase B: predictive slices whose intra colours phase A produced
@@ -380,7 +438,9 @@ extern "C" int pvvc_plan_info_get(const pvvc_plan* p, pvvc_plan_info* info) {
     info->group_ctas = p->grp_ctas;
     info->tune = p->tune;
     if (p->nslices > 0)
-        info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) + (p->ngroups_a > 0) + (p->nlist_a > 0) + (p->ngroups_b > 0) + (p->nlist_b > 0);
+        info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) +
+                        (p->nlong > 0 ? (p->ngroups_a_long > 0) + (p->ngroups_a > p->ngroups_a_long) : (p->ngroups_a > 0)) +
+                        (p->nlist_a > 0) + (p->ngroups_b > 0) + (p->nlist_b > 0);
     return PVVC_OK;
 }
 
@@ -548,110 +608,162 @@ extern "C" int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const
     return run_decode(plan, st, payload, xyz, rgb, points24, status, workspace, workspace_bytes, (cudaStream_t)stream, events);
 }
 
+namespace {
+// Runs fn(i) for i in [0, n) on up to `threads` host threads.
+template <class F>
+void parallel_for(int n, int threads, F fn) {
+    threads = std::max(1, std::min(threads, n));
+    if (threads == 1) {
+        for (int i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&] {
+            for (int i; (i = next.fetch_add(1)) < n;) fn(i);
+        });
+    for (auto& th : pool) th.join();
+}
+}  // namespace
+
 extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* const* frame_bytes,
                                        const uint64_t* frame_len, float* xyz_host, uint8_t* rgb_host, uint64_t cap_points,
                                        uint64_t* npoints_out, int32_t* status_host, int32_t status_cap, void* stream) {
     if (!st || nframes < 0 || (nframes && (!frame_bytes || !frame_len))) return PVVC_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    // parse (io::LoadFrame) and inflate zstd on the host
+    const int threads = (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
+    // parse (io::LoadFrame) and inflate zstd on the host, frames in parallel
     std::vector<Frame> frames(nframes);
-    for (int f = 0; f < nframes; ++f) {
-        int r = parse_frame(frame_bytes[f], frame_len[f], &frames[f]);
+    std::vector<int> prc(nframes, PVVC_OK);
+    parallel_for(nframes, threads, [&](int f) {
+        prc[f] = parse_frame(frame_bytes[f], frame_len[f], &frames[f]);
+        if (!prc[f]) prc[f] = frame_inflate(&frames[f]);
+    });
+    for (int r : prc)
         if (r) return r;
-        r = frame_inflate(&frames[f]);
-        if (r) return r;
-    }
-    // pack payloads (4-byte aligned) and build the batch description
+    // payload layout (4-byte aligned) and the batch description, in frame order
     uint64_t bytes = 0, pts = 0;
     int32_t nsl = 0;
-    for (auto& fr : frames) {
-        for (size_t i = 0; i < fr.count(); ++i) {
-            bytes = align_up(bytes + fr.geometry[i].size(), 4);
-            bytes = align_up(bytes + fr.color[i].size(), 4);
-            pts += fr.size[i];
-        }
-        nsl += (int32_t)fr.count();
+    std::vector<int32_t> ffirst(nframes + 1, 0);
+    for (int f = 0; f < nframes; ++f) {
+        ffirst[f] = nsl;
+        nsl += (int32_t)frames[f].count();
+    }
+    ffirst[nframes] = nsl;
+    std::vector<int32_t> slot(nsl), index(nsl);
+    std::vector<uint8_t> type(nsl), qp(nsl);
+    std::vector<uint32_t> size(nsl), gsz(nsl), csz(nsl);
+    std::vector<float> mv(16ull * nsl);
+    std::vector<uint64_t> goff(nsl), coff(nsl), oo(nsl);
+    {
+        int32_t k = 0;
+        for (auto& fr : frames)
+            for (size_t i = 0; i < fr.count(); ++i, ++k) {
+                index[k] = fr.index[i];
+                type[k] = fr.type[i];
+                qp[k] = fr.qp[i];
+                size[k] = fr.size[i];
+                std::memcpy(&mv[16ull * k], &fr.mv[16 * i], 64);
+                gsz[k] = (uint32_t)fr.geometry[i].size();
+                csz[k] = (uint32_t)fr.color[i].size();
+                goff[k] = bytes;
+                bytes = align_up(bytes + gsz[k], 4);
+                coff[k] = bytes;
+                bytes = align_up(bytes + csz[k], 4);
+                oo[k] = pts;
+                pts += size[k];
+            }
     }
     if (npoints_out) *npoints_out = pts;
     if (pts > cap_points || (status_host && status_cap < nsl)) return PVVC_ERR_CAPACITY;
     if (st->h_payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     uint8_t* hp = static_cast<uint8_t*>(st->h_payload.p);
-    std::vector<int32_t> slot(nsl);
-    std::vector<uint8_t> type(nsl), qp(nsl);
-    std::vector<uint32_t> size(nsl), gsz(nsl), csz(nsl);
-    std::vector<float> mv(16ull * nsl);
-    std::vector<uint64_t> goff(nsl), coff(nsl), oo(nsl);
-    uint64_t off = 0, po = 0;
-    int32_t k = 0;
-    for (auto& fr : frames)
-        for (size_t i = 0; i < fr.count(); ++i, ++k) {
-            slot[k] = fr.index[i];
-            type[k] = fr.type[i];
-            qp[k] = fr.qp[i];
-            size[k] = fr.size[i];
-            std::memcpy(&mv[16ull * k], &fr.mv[16 * i], 64);
-            goff[k] = off;
-            gsz[k] = (uint32_t)fr.geometry[i].size();
-            if (gsz[k]) std::memcpy(hp + off, fr.geometry[i].data(), gsz[k]);
-            off = align_up(off + gsz[k], 4);
-            coff[k] = off;
-            csz[k] = (uint32_t)fr.color[i].size();
-            if (csz[k]) std::memcpy(hp + off, fr.color[i].data(), csz[k]);
-            off = align_up(off + csz[k], 4);
-            oo[k] = po;
-            po += size[k];
+    parallel_for(nframes, threads, [&](int f) {
+        const Frame& fr = frames[f];
+        for (size_t i = 0; i < fr.count(); ++i) {
+            const int32_t k = ffirst[f] + (int32_t)i;
+            if (gsz[k]) std::memcpy(hp + goff[k], fr.geometry[i].data(), gsz[k]);
+            if (csz[k]) std::memcpy(hp + coff[k], fr.color[i].data(), csz[k]);
         }
-    // intra slices of different frames of one call may hit the same slot:
-    // decode frame groups in order, one batch per run without a repeated slot
-    pvvc_batch_desc d{};
-    int32_t first = 0;
-    int rc = PVVC_OK;
-    // the decoder reads whole 16-byte blocks: pad past the last payload byte
+    });
+    std::memset(hp + bytes, 0, 16);  // the decoder reads whole 16-byte blocks
+    // Intra slices of different frames of one call may hit the same patch
+    // index (a new GoP).  Split the call into runs of frames without a
+    // repeated intra index.
+    const int32_t nslots = st->v.nslots;
+    std::vector<int32_t> bounds{0};  // first slice of each run
+    {
+        std::vector<uint8_t> seen(std::max(nslots, 1), 0);
+        for (int f = 0; f < nframes; ++f) {
+            bool clash = false;
+            for (int32_t k = ffirst[f]; k < ffirst[f + 1]; ++k)
+                if (!(type[k] & PVVC_TYPE_PREDICT) && index[k] >= 0 && index[k] < nslots && seen[index[k]]) clash = true;
+            if (clash) {
+                bounds.push_back(ffirst[f]);
+                std::fill(seen.begin(), seen.end(), 0);
+            }
+            for (int32_t k = ffirst[f]; k < ffirst[f + 1]; ++k)
+                if (index[k] >= 0 && index[k] < nslots) seen[index[k]] = 1;
+        }
+        bounds.push_back(nsl);
+    }
+    const int nruns = (int)bounds.size() - 1;
+    // All runs in one decode: each intra slice but an index's last one in
+    // the call writes a slot region of its own (run r of R -> region R-1-r
+    // of `stride` slots), predictive slices read the region of their index's
+    // latest intra slice, and every index ends in its own slot (region 0), as
+    // run-by-run decoding leaves it.  This needs every predictive slice's
+    // intra slice inside the call and R regions of slots in the state.
+    int32_t stride = 0;
+    for (int32_t k = 0; k < nsl; ++k) stride = std::max(stride, index[k] + 1);
+    bool merge = nruns > 1 && stride > 0 && (int64_t)nruns * stride <= nslots;
+    if (merge) {
+        std::vector<int32_t> region(stride, -1);  // region of each index's latest intra slice
+        std::vector<int32_t> last_run(stride, -1);
+        for (int r = 0; r < nruns; ++r)
+            for (int32_t k = bounds[r]; k < bounds[r + 1]; ++k)
+                if (index[k] >= 0 && !(type[k] & PVVC_TYPE_PREDICT)) last_run[index[k]] = r;
+        for (int r = 0; r < nruns && merge; ++r)
+            for (int32_t k = bounds[r]; k < bounds[r + 1]; ++k) {
+                const int32_t i = index[k];
+                if (i < 0) {
+                    slot[k] = i;  // rejected by the plan as before
+                    continue;
+                }
+                if (!(type[k] & PVVC_TYPE_PREDICT)) region[i] = last_run[i] == r ? 0 : nruns - 1 - r;
+                if (region[i] < 0) {  // predictive before any intra of its index in this call
+                    merge = false;
+                    break;
+                }
+                slot[k] = region[i] * stride + i;
+            }
+    }
+    if (!merge)
+        for (int32_t k = 0; k < nsl; ++k) slot[k] = index[k];
     if (st->payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
-    if (bytes && cudaMemcpyAsync(st->payload.p, hp, bytes, cudaMemcpyHostToDevice, s) != cudaSuccess) return PVVC_ERR_CUDA;
-    std::vector<uint8_t> seen(std::max(st->v.nslots, 1), 0);
-    k = 0;
-    std::vector<int32_t> bounds;  // slice index where each batch starts
-    bounds.push_back(0);
-    for (auto& fr : frames) {
-        bool clash = false;
-        for (size_t i = 0; i < fr.count(); ++i)
-            if (!(fr.type[i] & PVVC_TYPE_PREDICT) && fr.index[i] >= 0 && fr.index[i] < st->v.nslots && seen[fr.index[i]])
-                clash = true;
-        if (clash) {
-            bounds.push_back(k);
-            std::fill(seen.begin(), seen.end(), 0);
-        }
-        for (size_t i = 0; i < fr.count(); ++i, ++k)
-            if (fr.index[i] >= 0 && fr.index[i] < st->v.nslots) seen[fr.index[i]] = 1;
-    }
-    bounds.push_back(nsl);
-    for (size_t b = 0; b + 1 < bounds.size() && rc == PVVC_OK; ++b) {
-        first = bounds[b];
-        const int32_t cnt = bounds[b + 1] - first;
+    if (bytes && cudaMemcpyAsync(st->payload.p, hp, bytes + 16, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return PVVC_ERR_CUDA;
+    int rc = PVVC_OK;
+    const std::vector<int32_t> one_run{0, nsl};
+    const std::vector<int32_t>& runs = merge ? one_run : bounds;
+    for (size_t b = 0; b + 1 < runs.size() && rc == PVVC_OK; ++b) {
+        const int32_t first = runs[b], cnt = runs[b + 1] - first;
         if (cnt <= 0) continue;
-        d.nslices = cnt;
-        d.slot = slot.data() + first;
-        d.type = type.data() + first;
-        d.size = size.data() + first;
-        d.qp = qp.data() + first;
-        d.mv = mv.data() + 16ull * first;
-        d.geo_off = goff.data() + first;
-        d.geo_size = gsz.data() + first;
-        d.col_off = coff.data() + first;
-        d.col_size = csz.data() + first;
-        d.out_off = oo.data() + first;
+        pvvc_batch_desc d{cnt,          slot.data() + first, type.data() + first, size.data() + first, qp.data() + first,
+                          mv.data() + 16ull * first, goff.data() + first, gsz.data() + first, coff.data() + first,
+                          csz.data() + first, oo.data() + first};
         rc = build_plan(&d, &st->plan, nullptr, nullptr);
         if (rc) break;
         if (st->ws.ensure(st->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
         rc = run_decode(&st->plan, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
                         static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
                         st->ws.cap, s, nullptr);
-        // the plan's host arrays are rebuilt by the next batch: finish this one first
-        if (rc == PVVC_OK && bounds.size() > 2 && cudaStreamSynchronize(s) != cudaSuccess) rc = PVVC_ERR_CUDA;
+        // the plan's host arrays are rebuilt by the next run: finish this one first
+        if (rc == PVVC_OK && runs.size() > 2 && cudaStreamSynchronize(s) != cudaSuccess) rc = PVVC_ERR_CUDA;
     }
     if (rc) return rc;
     if (xyz_host && pts && cudaMemcpyAsync(xyz_host, st->xyz.p, 12 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)

@@ -113,6 +113,7 @@ struct pvvc_plan {
     uint64_t ws_grp = 0, ws_counter = 0, grp_floats = 0;  // group-kernel level buffers, queue counters
     int32_t grp_ctas = 0;
     uint64_t coef_floats = 0;
+    uint64_t coef_long_floats = 0;  // planes prefix the long-slice RLGR launch writes
     std::vector<pvvc::SliceWork> work;
     std::vector<int32_t> order;
     // inverse-RAHT schedule: phase A needs only this batch's trees; phase B
@@ -120,12 +121,14 @@ struct pvvc_plan {
     // lists to the per-slice kernel.
     std::vector<pvvc::GroupDesc> groups;  // [A groups | B groups]
     int32_t ngroups_a = 0, ngroups_b = 0;
+    int32_t ngroups_a_long = 0;           // leading phase-A groups that hold a long-launch slice
     std::vector<int32_t> idx;             // [group items | slice list A | slice list B]
     int32_t nlist_a = 0, nlist_b = 0, list_a_off = 0, list_b_off = 0;
     pvvc::DevBuf d_work, d_order, d_groups, d_idx;
     pvvc::HostBuf h_work, h_order, h_groups, h_idx;  // pinned mirrors of stream-ordered uploads
     int32_t nlong = 0;       // the first nlong slices of `order` go to the long-slice RLGR launch
     pvvc::SideStream side;   // its stream
+    pvvc::SideStream tree;   // the tree expansion's stream (beside the coefficient clear and RLGR)
 };
 
 struct pvvc_state {

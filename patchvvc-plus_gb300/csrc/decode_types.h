@@ -11,11 +11,12 @@ constexpr int kMaxLevels = 32;  // octree height limit (the header stores a u8)
 // One slice in the work queue (queue order = intra first, then by size).
 // RLGR launches split by slice length: a CTA of the long-slice launch (128
 // threads, one warp per scheduler) reserves this much dynamic shared memory,
-// which no RLGR code uses, so that no other CTA of either launch fits on its
-// SM; a CTA of the other launch reserves kRlgrShortSmem, more than such an
-// SM has left.  The serial bit chains of the longest slices then run without
-// sharing issue slots, while the short slices fill the remaining SMs.
-constexpr int kRlgrLongSmem = 200 * 1024;
+// which no RLGR code uses, so that no other CTA fits on its SM -- neither one
+// of the other RLGR launch (kRlgrShortSmem each) nor one of the grouped
+// inverse RAHT (~20 KB) that runs beside it.  The serial bit chains of the
+// longest slices then run without sharing issue slots, while the rest of the
+// decode fills the remaining SMs.
+constexpr int kRlgrLongSmem = 212 * 1024;
 constexpr int kRlgrShortSmem = 32 * 1024;
 constexpr int kRlgrLongBlock = 128;
 

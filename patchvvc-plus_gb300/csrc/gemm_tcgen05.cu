@@ -128,20 +128,39 @@ struct EpiArgs {
     int64_t ldaux;
 };
 
+// Shared memory of a CTA: `stages` (1..kStages) A and B tiles, 1024-byte
+// aligned as the 128-byte swizzle wants, then the barriers.  A GEMM with
+// fewer K blocks than kStages gets a shorter ring, so that more CTAs fit on
+// an SM (the network's GEMMs have K of 64..512).
+constexpr int kTileA = kBM * kBK * 2;  // 16 KB
 template <int BN>
-struct __align__(1024) GemmSmem {
-    __nv_bfloat16 a[kStages][kBM * kBK];  // 16 KB per stage
-    __nv_bfloat16 b[kStages][BN * kBK];
+struct GemmBars {
     uint64_t full[kStages], empty[kStages], done;
     uint32_t tmem_base;
+};
+template <int BN>
+__host__ __device__ constexpr size_t gemm_smem_bytes(int stages) {
+    return 1024 + (size_t)stages * (kTileA + BN * kBK * 2) + sizeof(GemmBars<BN>);
+}
+template <int BN>
+struct GemmSmem {
+    uint8_t* base;
+    int stages;
+    __device__ __forceinline__ void* a(int s) const { return base + (size_t)s * kTileA; }
+    __device__ __forceinline__ void* b(int s) const { return base + (size_t)stages * kTileA + (size_t)s * BN * kBK * 2; }
+    __device__ __forceinline__ GemmBars<BN>& bars() const {
+        return *reinterpret_cast<GemmBars<BN>*>(base + (size_t)stages * (kTileA + BN * kBK * 2));
+    }
 };
 
 template <int BN, int EPI>
 __global__ void __launch_bounds__(128, 1)
     k_gemm_bf16_tn(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M, int K,
-                   int kb_per_split, EpiArgs ep) {
+                   int kb_per_split, int stages, EpiArgs ep) {
     extern __shared__ uint8_t smem_raw[];
-    GemmSmem<BN>& sm = *reinterpret_cast<GemmSmem<BN>*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const GemmSmem<BN> L{reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023)),
+                         stages};
+    GemmBars<BN>& sm = L.bars();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
     const int nkb = K / kBK;
@@ -150,7 +169,7 @@ __global__ void __launch_bounds__(128, 1)
     if (kb0 >= kb1) return;  // uniform over the CTA
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < stages; ++s) {
             mbar_init(&sm.full[s], 1);
             mbar_init(&sm.empty[s], 1);
         }
@@ -171,20 +190,20 @@ __global__ void __launch_bounds__(128, 1)
 
     if (threadIdx.x == 0) {  // producer
         for (int kb = kb0; kb < kb1 && ok; ++kb) {
-            const int i = kb - kb0, s = i % kStages;
-            if (!(ok = mbar_wait(&sm.empty[s], ((i / kStages) & 1) ^ 1, 1))) break;
+            const int i = kb - kb0, s = i % stages;
+            if (!(ok = mbar_wait(&sm.empty[s], ((i / stages) & 1) ^ 1, 1))) break;
             mbar_expect_tx(&sm.full[s], (kBM + BN) * kBK * 2);
-            tma_load_2d(sm.a[s], &map_a, &sm.full[s], kb * kBK, m0);
-            tma_load_2d(sm.b[s], &map_b, &sm.full[s], kb * kBK, n0);
+            tma_load_2d(L.a(s), &map_a, &sm.full[s], kb * kBK, m0);
+            tma_load_2d(L.b(s), &map_b, &sm.full[s], kb * kBK, n0);
         }
     } else if (threadIdx.x == 32) {  // MMA issuer
         constexpr uint32_t idesc = idesc_bf16(kBM, BN);
         for (int kb = kb0; kb < kb1 && ok; ++kb) {
-            const int i = kb - kb0, s = i % kStages;
-            if (!(ok = mbar_wait(&sm.full[s], (i / kStages) & 1, 2))) break;
+            const int i = kb - kb0, s = i % stages;
+            if (!(ok = mbar_wait(&sm.full[s], (i / stages) & 1, 2))) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint64_t da = smem_desc_sw128(smem_u32(sm.a[s]));
-            const uint64_t db = smem_desc_sw128(smem_u32(sm.b[s]));
+            const uint64_t da = smem_desc_sw128(smem_u32(L.a(s)));
+            const uint64_t db = smem_desc_sw128(smem_u32(L.b(s)));
 #pragma unroll
             for (int k = 0; k < kBK / 16; ++k)  // +32 bytes per K=16 step inside the swizzle row
                 mma_bf16(tmem, da + 2 * k, db + 2 * k, idesc, (i > 0 || k > 0) ? 1u : 0u);
@@ -288,18 +307,19 @@ bool make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t K, int64_t
 template <int BN, int EPI>
 cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int K, int splits, const EpiArgs& ep,
                       cudaStream_t s) {
-    const size_t smem = sizeof(GemmSmem<BN>) + 1024;
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
     std::call_once(once, [&] {
-        attr = cudaFuncSetAttribute(k_gemm_bf16_tn<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr = cudaFuncSetAttribute(k_gemm_bf16_tn<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)gemm_smem_bytes<BN>(kStages));
     });
     if (attr != cudaSuccess) return attr;
     const int nkb = K / kBK;
     const int per = (nkb + splits - 1) / splits;
     const int z = (nkb + per - 1) / per;
+    const int stages = per < kStages ? per : kStages;  // K blocks one CTA walks
     dim3 grid((M + kBM - 1) / kBM, N / BN, z);
-    k_gemm_bf16_tn<BN, EPI><<<grid, 128, smem, s>>>(ma, mb, M, K, per, ep);
+    k_gemm_bf16_tn<BN, EPI><<<grid, 128, gemm_smem_bytes<BN>(stages), s>>>(ma, mb, M, K, per, stages, ep);
     return cudaGetLastError();
 }
 
