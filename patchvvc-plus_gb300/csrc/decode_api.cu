@@ -224,6 +224,10 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         p->grp_floats = 2ull * std::max<uint32_t>(maxn, 1) * 96;
         p->ws_grp = off;
         off = align_up(off + 4ull * p->grp_floats * std::max(p->grp_ctas, 1), 256);
+        // the long-slice groups run beside the others, with level buffers of their own
+        p->grp_ctas_long = p->nlong > 0 ? std::min<int32_t>(p->ngroups_a_long, p->grp_ctas) : 0;
+        p->ws_grp_long = off;
+        off = align_up(off + 4ull * p->grp_floats * p->grp_ctas_long, 256);
         p->ws_counter = off;
         off = align_up(off + 16, 256);
     }
@@ -292,9 +296,11 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     int* cnt = reinterpret_cast<int*>(w + p->ws_counter);  // queue counters: A long, B, A short
     const GroupDesc* dg = static_cast<const GroupDesc*>(p->d_groups.p);
     const int32_t* di = static_cast<const int32_t*>(p->d_idx.p);
-    auto raht_groups = [&](int first, int count, int* counter) {
-        return launch_raht_group(dw, dg + first, count, di, st->v, coef, ts, rs, fs, xyz, rgb, p24, status, gsc,
-                                 p->grp_floats, p->grp_ctas, counter, s) == cudaSuccess;
+    auto raht_groups = [&](int first, int count, int* counter, float* scratch = nullptr, int ctas = 0,
+                           cudaStream_t on = nullptr) {
+        return launch_raht_group(dw, dg + first, count, di, st->v, coef, ts, rs, fs, xyz, rgb, p24, status,
+                                 scratch ? scratch : gsc, p->grp_floats, ctas ? ctas : p->grp_ctas, counter,
+                                 scratch ? on : s) == cudaSuccess;
     };
     const int na_long = p->ngroups_a_long, na_short = p->ngroups_a - p->ngroups_a_long;
     if (p->nlong > 0) {
@@ -305,19 +311,28 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
         const SideStream& sd = p->side;
         if (cudaEventRecord(sd.fork, s) != cudaSuccess || cudaStreamWaitEvent(sd.s, sd.fork, 0) != cudaSuccess ||
             launch_rlgr(dw, ord, p->nlong, payload, coef, rs, kRlgrLongBlock, kRlgrLongSmem, sd.s) != cudaSuccess ||
-            cudaEventRecord(sd.join, sd.s) != cudaSuccess ||
             (clear_first < p->coef_floats &&
              cudaMemsetAsync(coef + clear_first, 0, 4ull * (p->coef_floats - clear_first), s) != cudaSuccess) ||
             launch_rlgr(dw, ord + p->nlong, p->nslices - p->nlong, payload, coef, rs, p->tune.rlgr_block, kRlgrShortSmem,
                         s) != cudaSuccess)
             return PVVC_ERR_CUDA;
         if (events) {
-            if (cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess || !mark(2)) return PVVC_ERR_CUDA;
+            if (cudaEventRecord(sd.join, sd.s) != cudaSuccess || cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess ||
+                !mark(2))
+                return PVVC_ERR_CUDA;
             if (!raht_groups(0, p->ngroups_a, cnt)) return PVVC_ERR_CUDA;
         } else {
+            // The long groups follow the long launch on its stream: they need
+            // the trees and the short launch too (a group can straddle the size
+            // cut).  The other groups follow the short launch on this stream.
+            float* gsc_long = reinterpret_cast<float*>(w + p->ws_grp_long);
             if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;
-            if (!raht_groups(na_long, na_short, cnt + 2) || cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess ||
-                !raht_groups(0, na_long, cnt))
+            if (na_long > 0 &&
+                (cudaEventRecord(sd.mid, s) != cudaSuccess || cudaStreamWaitEvent(sd.s, sd.mid, 0) != cudaSuccess ||
+                 !raht_groups(0, na_long, cnt, gsc_long, p->grp_ctas_long, sd.s)))
+                return PVVC_ERR_CUDA;
+            if (cudaEventRecord(sd.join, sd.s) != cudaSuccess || !raht_groups(na_long, na_short, cnt + 2) ||
+                cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess)
                 return PVVC_ERR_CUDA;
         }
     } else {

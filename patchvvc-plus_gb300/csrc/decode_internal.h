@@ -70,13 +70,14 @@ struct DevBuf {
 // side by side (also under stream capture, where they become graph branches)
 struct SideStream {
     cudaStream_t s = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, mid = nullptr;  // mid: a point of the main stream the side one waits for
     SideStream() = default;
     SideStream(const SideStream&) = delete;
     SideStream& operator=(const SideStream&) = delete;
     ~SideStream() {
         if (fork) cudaEventDestroy(fork);
         if (join) cudaEventDestroy(join);
+        if (mid) cudaEventDestroy(mid);
         if (s) cudaStreamDestroy(s);
     }
     cudaError_t ensure() {
@@ -84,6 +85,7 @@ struct SideStream {
         if (!s) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
         if (e == cudaSuccess && !fork) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
         if (e == cudaSuccess && !join) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+        if (e == cudaSuccess && !mid) e = cudaEventCreateWithFlags(&mid, cudaEventDisableTiming);
         return e;
     }
 };
@@ -111,7 +113,8 @@ struct pvvc_plan {
     uint64_t total_points = 0;
     uint64_t ws_coef = 0, ws_fb = 0, ws_tstatus = 0, ws_rstatus = 0, ws_fstatus = 0, ws_bytes = 0;
     uint64_t ws_grp = 0, ws_counter = 0, grp_floats = 0;  // group-kernel level buffers, queue counters
-    int32_t grp_ctas = 0;
+    int32_t grp_ctas = 0, grp_ctas_long = 0;
+    uint64_t ws_grp_long = 0;  // level buffers of the long-slice groups' launch
     uint64_t coef_floats = 0;
     uint64_t coef_long_floats = 0;  // planes prefix the long-slice RLGR launch writes
     std::vector<pvvc::SliceWork> work;

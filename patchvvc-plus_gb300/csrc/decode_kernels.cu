@@ -794,38 +794,40 @@ __device__ __forceinline__ void group_emit(const SliceWork& w, bool act, bool in
     }
 }
 
-// inverse_node for a lane that may be inactive (no coefficient loads then)
-template <int S>  // coefficient stride (32 in frame-interleaved group regions)
-__device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool act, const float* cy, const float* cu,
-                                          const float* cv, float gy, float gu, float gv, float (&oy)[8], float (&ou)[8],
-                                          float (&ov)[8]) {
-    const uint32_t m = __ldg(st.mask + node);
-    uint32_t ci = __ldg(st.coff + node);
-    const float2* ab = st.ab + node * 7;
+// inverse_node for a lane that may be inactive (no coefficient loads then),
+// given the node's coded-slot mask `m`, first coefficient `ci` and butterfly
+// pairs ab[i * AS] (AS = 1: the state's node record; 32: a warp's staged
+// rows).  Coded slot i reads coefficient ci + (coded slots below i), so the
+// node's coefficient loads are independent and issue together.
+template <int S, int AS>  // coefficient stride (32 in frame-interleaved group regions), ab stride
+__device__ __forceinline__ void lane_node_md(uint32_t m, uint32_t ci, const float2* ab, bool act, const float* cy,
+                                             const float* cu, const float* cv, float gy, float gu, float gv,
+                                             float (&oy)[8], float (&ou)[8], float (&ov)[8]) {
+    float hy[8], hu[8], hv[8];
+#pragma unroll
+    for (int i = 1; i < 8; ++i) {
+        const bool coded = act && (m & (1u << i));
+        const size_t k = (size_t)(ci + __popc(m & ((1u << i) - 2u))) * S;
+        hy[i] = coded ? __ldg(cy + k) : 0.f;
+        hu[i] = coded ? __ldg(cu + k) : 0.f;
+        hv[i] = coded ? __ldg(cv + k) : 0.f;
+    }
     float sy[8], su[8], sv[8];
     sy[1] = gy;
     su[1] = gu;
     sv[1] = gv;
 #pragma unroll
     for (int i = 1; i < 8; ++i) {
-        const float2 t = __ldg(ab + (i - 1));
-        float hy = 0.f, hu = 0.f, hv = 0.f;
-        if (m & (1u << i)) {
-            if (act) {
-                hy = __ldg(cy + (size_t)ci * S);
-                hu = __ldg(cu + (size_t)ci * S);
-                hv = __ldg(cv + (size_t)ci * S);
-            }
-            ++ci;
-        }
+        const float2 t = ab[(i - 1) * AS];
         const float ay = sy[i], au = su[i], av = sv[i];
         const float nbv = -t.y;
-        const float Gy = __fadd_rn(__fmul_rn(ay, t.x), __fmul_rn(hy, nbv));
-        const float Gu = __fadd_rn(__fmul_rn(au, t.x), __fmul_rn(hu, nbv));
-        const float Gv = __fadd_rn(__fmul_rn(av, t.x), __fmul_rn(hv, nbv));
-        const float Hy = __fadd_rn(__fmul_rn(ay, t.y), __fmul_rn(hy, t.x));
-        const float Hu = __fadd_rn(__fmul_rn(au, t.y), __fmul_rn(hu, t.x));
-        const float Hv = __fadd_rn(__fmul_rn(av, t.y), __fmul_rn(hv, t.x));
+        // [G;H] = [[a,-b],[b,a]] [g;h]   (InvertHaarTransform, octree_base.cc:186-206)
+        const float Gy = __fadd_rn(__fmul_rn(ay, t.x), __fmul_rn(hy[i], nbv));
+        const float Gu = __fadd_rn(__fmul_rn(au, t.x), __fmul_rn(hu[i], nbv));
+        const float Gv = __fadd_rn(__fmul_rn(av, t.x), __fmul_rn(hv[i], nbv));
+        const float Hy = __fadd_rn(__fmul_rn(ay, t.y), __fmul_rn(hy[i], t.x));
+        const float Hu = __fadd_rn(__fmul_rn(au, t.y), __fmul_rn(hu[i], t.x));
+        const float Hv = __fadd_rn(__fmul_rn(av, t.y), __fmul_rn(hv[i], t.x));
         if (pair0(i) < 8) {
             sy[pair0(i)] = Gy; su[pair0(i)] = Gu; sv[pair0(i)] = Gv;
             sy[pair1(i)] = Hy; su[pair1(i)] = Hu; sv[pair1(i)] = Hv;
@@ -836,6 +838,19 @@ __device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool
     }
 }
 
+template <int S>
+__device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool act, const float* cy, const float* cu,
+                                          const float* cv, float gy, float gu, float gv, float (&oy)[8], float (&ou)[8],
+                                          float (&ov)[8]) {
+    lane_node_md<S, 1>(__ldg(st.mask + node), __ldg(st.coff + node), st.ab + node * 7, act, cy, cu, cv, gy, gu, gv, oy, ou,
+                       ov);
+}
+
+// A warp's staged node records: 32 consecutive nodes of one level.
+struct NodeRows {
+    uint32_t occ[32], cb[32], mask[32], coff[32];
+    float2 ab[7][32];
+};
 
 // k_raht_group: persistent CTAs; each takes the next group of slices that
 // share a slot (the frames of one patch) from a queue.  Lane f of every warp
@@ -875,7 +890,7 @@ struct GroupStage {
 };
 
 template <bool P24>
-__global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* __restrict__ work,
+__global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWork* __restrict__ work,
                                                                const GroupDesc* __restrict__ groups, int ngroups,
                                                                const int32_t* __restrict__ items, StateView st,
                                                                const float* __restrict__ coef,
@@ -890,6 +905,7 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
     __shared__ uint64_t s_out[32];
     __shared__ int s_act[32], s_white[32];
     __shared__ float s_mv[32][13];  // each frame's transform rows (odd stride: the lanes' row fills hit 32 banks)
+    __shared__ NodeRows s_nodes[kGrpWarps];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     WarpStage<P24>& ws = sg.w[wid];
     float* const bufA = scratch + (uint64_t)blockIdx.x * scratch_floats;
@@ -1063,26 +1079,43 @@ __global__ void __launch_bounds__(32 * kGrpWarps) k_raht_group(const SliceWork* 
                 const int j0 = min(cnt, wid * per), j1 = min(cnt, j0 + per);
                 uint32_t base = 0, staged = 0;
                 if (j0 < j1) base = __ldg(st.cbase + nb + a + j0);
-                for (int j = j0; j < j1; ++j) {
-                    const size_t node = nb + a + j;
-                    const uint32_t byte = __ldg(st.occ + node), cb = __ldg(st.cbase + node);
-                    const uint32_t k = __popc(byte);
-                    if (staged + k > (uint32_t)kWarpLeaves) {
-                        flush(base, staged);
-                        base += staged;
-                        staged = 0;
-                    }
-                    const float* g3 = gA + (size_t)j * 96 + lane;
-                    float oy[8], ou[8], ov[8];
-                    lane_node<32>(st, node, act, cy, cu, cv, g3[0], g3[32], g3[64], oy, ou, ov);
-                    uint32_t r = 0;
+                NodeRows& nr = s_nodes[wid];
+                for (int jb = j0; jb < j1; jb += 32) {
+                    // the next 32 node records, one node per lane, all loads in flight at once
+                    const int nn = min(32, j1 - jb);
+                    __syncwarp();
+                    if (lane < nn) {
+                        const size_t node = nb + a + jb + lane;
+                        nr.occ[lane] = __ldg(st.occ + node);
+                        nr.cb[lane] = __ldg(st.cbase + node);
+                        nr.mask[lane] = __ldg(st.mask + node);
+                        nr.coff[lane] = __ldg(st.coff + node);
+                        const float2* ab = st.ab + node * 7;
 #pragma unroll
-                    for (int c = 0; c < 8; ++c) {
-                        if (!(byte & (0x80u >> c))) continue;
-                        finish(cb + r, cb + r - base, oy[c], ou[c], ov[c]);
-                        ++r;
+                        for (int i = 0; i < 7; ++i) nr.ab[i][lane] = __ldg(ab + i);
                     }
-                    staged = cb + k - base;
+                    __syncwarp();
+                    for (int t = 0; t < nn; ++t) {
+                        const uint32_t byte = nr.occ[t], cb = nr.cb[t];
+                        const uint32_t k = __popc(byte);
+                        if (staged + k > (uint32_t)kWarpLeaves) {
+                            flush(base, staged);
+                            base += staged;
+                            staged = 0;
+                        }
+                        const float* g3 = gA + (size_t)(jb + t) * 96 + lane;
+                        float oy[8], ou[8], ov[8];
+                        lane_node_md<32, 32>(nr.mask[t], nr.coff[t], &nr.ab[0][t], act, cy, cu, cv, g3[0], g3[32], g3[64],
+                                             oy, ou, ov);
+                        uint32_t r = 0;
+#pragma unroll
+                        for (int c = 0; c < 8; ++c) {
+                            if (!(byte & (0x80u >> c))) continue;
+                            finish(cb + r, cb + r - base, oy[c], ou[c], ov[c]);
+                            ++r;
+                        }
+                        staged = cb + k - base;
+                    }
                 }
                 if (staged) flush(base, staged);
             }
