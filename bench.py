@@ -57,7 +57,7 @@ def parse_args():
     ap.add_argument("--frames", type=int, default=300)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--tune", default="", help="fixed launch shapes 'group_ctas,min_group,rlgr_block,long_ctas' "
+    ap.add_argument("--tune", default="", help="fixed launch shapes 'group_ctas,min_group,rlgr_block,long_ctas,mid_pct,long_lanes' "
                                                "instead of the autotuner")
     ap.add_argument("--icp-pairs", type=int, default=4096, help="batched ICP workload size (0: skip)")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned-ICP comparison")
@@ -240,8 +240,9 @@ def run_ours(args):
     stream = torch.cuda.current_stream(dev)
     t_tune = time.time()
     if args.tune:
-        g, m, b, l = (int(x) for x in args.tune.split(","))
-        tune, tune_ms = {"group_ctas_per_sm": g, "min_group": m, "rlgr_block": b, "rlgr_long_ctas": l}, None
+        g, m, b, l, mid, ln = (int(x) for x in args.tune.split(","))
+        tune, tune_ms = {"group_ctas_per_sm": g, "min_group": m, "rlgr_block": b, "rlgr_long_ctas": l,
+                         "rlgr_mid_pct": mid, "rlgr_long_lanes": ln}, None
     else:
         tune, tune_ms = pvvc.autotune(batch, dec, pay.data_ptr(), reps=2, stream=stream.cuda_stream)
     log(f"[rank {rank}] launch shapes {tune} ({tune_ms} ms) in {time.time() - t_tune:.1f}s")

@@ -98,6 +98,9 @@ typedef struct {
     int32_t rlgr_block;        /* threads per CTA of the RLGR kernel: 32, 64, 128 or 256 (default 128)         */
     int32_t rlgr_long_ctas;    /* CTAs of 128 threads that decode the longest slices alone on an SM each, side by
                                   side with the rest: 0..152 (default 32); -1 turns the split off                 */
+    int32_t rlgr_mid_pct;      /* with the split on: percent of the other slices (the larger ones) decoded, and
+                                  their groups inverse-transformed, on a third stream: 0..90 (default 30); -1 off */
+    int32_t rlgr_long_lanes;   /* slices per warp in the long-slice launch: 8, 16 or 32 (default 32)            */
 } pvvc_tune;
 int pvvc_plan_create_tuned(const pvvc_batch_desc* desc, const pvvc_tune* tune, pvvc_plan** out);
 
@@ -114,7 +117,7 @@ typedef struct {
 int pvvc_plan_info_get(const pvvc_plan* plan, pvvc_plan_info* info);
 
 /* Autotuner: plans `desc` under a set of candidate launch shapes (a
- * coordinate search over the four pvvc_tune fields, starting at the
+ * coordinate search over the six pvvc_tune fields, starting at the
  * defaults), captures one decode of the batch under each into a CUDA graph,
  * replays it `reps` times on `stream` timed with CUDA events, and returns the
  * fastest shapes and their mean device time per decode.  The

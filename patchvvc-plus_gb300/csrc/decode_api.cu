@@ -18,13 +18,17 @@ namespace pvvc {
 
 // zero fields -> defaults; out-of-range fields -> PVVC_ERR_ARG
 int resolve_tune(const pvvc_tune* in, pvvc_tune* out) {
-    pvvc_tune t{kGroupCtasPerSm, kMinGroup, kRlgrBlock, kRlgrLongCtas};
+    pvvc_tune t{kGroupCtasPerSm, kMinGroup, kRlgrBlock, kRlgrLongCtas, kRlgrMidPct, kRlgrLongLanes};
     if (in) {
         if (in->group_ctas_per_sm) t.group_ctas_per_sm = in->group_ctas_per_sm;
         if (in->min_group) t.min_group = in->min_group;
         if (in->rlgr_block) t.rlgr_block = in->rlgr_block;
         if (in->rlgr_long_ctas) t.rlgr_long_ctas = in->rlgr_long_ctas;
+        if (in->rlgr_mid_pct) t.rlgr_mid_pct = in->rlgr_mid_pct;
+        if (in->rlgr_long_lanes) t.rlgr_long_lanes = in->rlgr_long_lanes;
     }
+    if (t.rlgr_long_lanes != 8 && t.rlgr_long_lanes != 16 && t.rlgr_long_lanes != 32) return PVVC_ERR_ARG;
+    if (t.rlgr_mid_pct < -1 || t.rlgr_mid_pct > 90) return PVVC_ERR_ARG;
     if (t.group_ctas_per_sm < 1 || t.group_ctas_per_sm > 4 || t.min_group < 1 || t.min_group > 32) return PVVC_ERR_ARG;
     if (t.rlgr_long_ctas < -1 || t.rlgr_long_ctas > 152) return PVVC_ERR_ARG;
     if (t.rlgr_block != 32 && t.rlgr_block != 64 && t.rlgr_block != 128 && t.rlgr_block != 256) return PVVC_ERR_ARG;
@@ -106,9 +110,15 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     // the head of that order goes to the long-slice launch (at most a quarter
     // of the slices, so that small batches still spread over many SMs)
     p->nlong = 0;
+    p->nmid = 0;
     if (p->tune.rlgr_long_ctas > 0 && n >= 8) {
         p->nlong = std::min<int32_t>(kRlgrLongBlock * p->tune.rlgr_long_ctas, n / 4);
         if (p->side.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+        // the larger part of the rest forms the medium tier
+        if (p->tune.rlgr_mid_pct > 0) {
+            p->nmid = (int32_t)((int64_t)(n - p->nlong) * p->tune.rlgr_mid_pct / 100);
+            if (p->nmid > 0 && p->side2.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+        }
     }
     if (!intra.empty() && p->tree.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
     // inverse-RAHT schedule: slices grouped by slot (largest slots first)
@@ -149,17 +159,20 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         }
         // phase-A groups that hold a slice of the long-slice RLGR launch first:
         // the others can be inverse-transformed as soon as the short launch ends
+        // (tier 2), then those with a medium-tier slice (tier 1), then the rest
         {
-            std::vector<uint8_t> is_long(n, 0);
-            for (int i = 0; i < p->nlong; ++i) is_long[p->order[i]] = 1;
-            std::vector<GroupDesc> gl, gs;
+            std::vector<uint8_t> tier(n, 0);
+            for (int i = 0; i < p->nlong + p->nmid; ++i) tier[p->order[i]] = i < p->nlong ? 2 : 1;
+            std::vector<GroupDesc> gl, gm, gs;
             for (const GroupDesc& g : ga) {
-                bool any = false;
-                for (int l = 0; l < g.count; ++l) any = any || is_long[items[g.first + l]];
-                (any ? gl : gs).push_back(g);
+                int t = 0;
+                for (int l = 0; l < g.count; ++l) t = std::max<int>(t, tier[items[g.first + l]]);
+                (t == 2 ? gl : t == 1 ? gm : gs).push_back(g);
             }
             p->ngroups_a_long = (int32_t)gl.size();
+            p->ngroups_a_mid = (int32_t)gm.size();
             ga = gl;
+            ga.insert(ga.end(), gm.begin(), gm.end());
             ga.insert(ga.end(), gs.begin(), gs.end());
         }
         p->groups = ga;
@@ -198,9 +211,12 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         // the prefix of the planes that the long-slice RLGR launch writes
         // (its groups come first; a long slice outside a group extends it)
         p->coef_long_floats = 0;
-        for (int i = 0; i < p->nlong; ++i) {
+        p->coef_mid_floats = 0;
+        for (int i = 0; i < p->nlong + p->nmid; ++i) {
             const SliceWork& w = p->work[p->order[i]];
-            p->coef_long_floats = std::max<uint64_t>(p->coef_long_floats, w.coef_off + 3ull * w.n * w.coef_stride);
+            const uint64_t e = w.coef_off + 3ull * w.n * w.coef_stride;
+            if (i < p->nlong) p->coef_long_floats = std::max(p->coef_long_floats, e);
+            p->coef_mid_floats = std::max(p->coef_mid_floats, e);
         }
     }
     // workspace layout
@@ -228,6 +244,9 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         p->grp_ctas_long = p->nlong > 0 ? std::min<int32_t>(p->ngroups_a_long, p->grp_ctas) : 0;
         p->ws_grp_long = off;
         off = align_up(off + 4ull * p->grp_floats * p->grp_ctas_long, 256);
+        p->grp_ctas_mid = p->nmid > 0 ? std::min<int32_t>(p->ngroups_a_mid, p->grp_ctas) : 0;
+        p->ws_grp_mid = off;
+        off = align_up(off + 4ull * p->grp_floats * p->grp_ctas_mid, 256);
         p->ws_counter = off;
         off = align_up(off + 16, 256);
     }
@@ -287,59 +306,73 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     } else if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) {
         return PVVC_ERR_CUDA;
     }
-    // Zero symbols are not written by the decoder: clear the planes first.
-    // Without stage markers, only the long launch's prefix is cleared before
-    // it forks; the rest is cleared beside it, before the short launch.
-    const uint64_t clear_first = (p->nlong > 0 && !events) ? p->coef_long_floats : p->coef_floats;
-    if (cudaMemsetAsync(coef, 0, 4ull * clear_first, s) != cudaSuccess) return PVVC_ERR_CUDA;
     float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
-    int* cnt = reinterpret_cast<int*>(w + p->ws_counter);  // queue counters: A long, B, A short
+    int* cnt = reinterpret_cast<int*>(w + p->ws_counter);  // queue counters: A long, B, A short, A medium
     const GroupDesc* dg = static_cast<const GroupDesc*>(p->d_groups.p);
     const int32_t* di = static_cast<const int32_t*>(p->d_idx.p);
-    auto raht_groups = [&](int first, int count, int* counter, float* scratch = nullptr, int ctas = 0,
-                           cudaStream_t on = nullptr) {
-        return launch_raht_group(dw, dg + first, count, di, st->v, coef, ts, rs, fs, xyz, rgb, p24, status,
-                                 scratch ? scratch : gsc, p->grp_floats, ctas ? ctas : p->grp_ctas, counter,
-                                 scratch ? on : s) == cudaSuccess;
+    auto raht_groups = [&](int first, int count, int* counter, float* scratch, int ctas, cudaStream_t on) {
+        return count <= 0 || launch_raht_group(dw, dg + first, count, di, st->v, coef, ts, rs, fs, xyz, rgb, p24, status,
+                                               scratch, p->grp_floats, ctas, counter, on) == cudaSuccess;
     };
-    const int na_long = p->ngroups_a_long, na_short = p->ngroups_a - p->ngroups_a_long;
-    if (p->nlong > 0) {
-        // The longest slices (the head of the size order) decode on SMs of
-        // their own beside the rest.  Without stage markers, the phase-A
-        // groups that hold none of them are inverse-transformed as soon as the
-        // short launch ends, still beside the long one; the others after it.
-        const SideStream& sd = p->side;
-        if (cudaEventRecord(sd.fork, s) != cudaSuccess || cudaStreamWaitEvent(sd.s, sd.fork, 0) != cudaSuccess ||
-            launch_rlgr(dw, ord, p->nlong, payload, coef, rs, kRlgrLongBlock, kRlgrLongSmem, sd.s) != cudaSuccess ||
-            (clear_first < p->coef_floats &&
-             cudaMemsetAsync(coef + clear_first, 0, 4ull * (p->coef_floats - clear_first), s) != cudaSuccess) ||
-            launch_rlgr(dw, ord + p->nlong, p->nslices - p->nlong, payload, coef, rs, p->tune.rlgr_block, kRlgrShortSmem,
-                        s) != cudaSuccess)
-            return PVVC_ERR_CUDA;
-        if (events) {
-            if (cudaEventRecord(sd.join, sd.s) != cudaSuccess || cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess ||
-                !mark(2))
-                return PVVC_ERR_CUDA;
-            if (!raht_groups(0, p->ngroups_a, cnt)) return PVVC_ERR_CUDA;
-        } else {
-            // The long groups follow the long launch on its stream: they need
-            // the trees and the short launch too (a group can straddle the size
-            // cut).  The other groups follow the short launch on this stream.
-            float* gsc_long = reinterpret_cast<float*>(w + p->ws_grp_long);
-            if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;
-            if (na_long > 0 &&
-                (cudaEventRecord(sd.mid, s) != cudaSuccess || cudaStreamWaitEvent(sd.s, sd.mid, 0) != cudaSuccess ||
-                 !raht_groups(0, na_long, cnt, gsc_long, p->grp_ctas_long, sd.s)))
-                return PVVC_ERR_CUDA;
-            if (cudaEventRecord(sd.join, sd.s) != cudaSuccess || !raht_groups(na_long, na_short, cnt + 2) ||
-                cudaStreamWaitEvent(s, sd.join, 0) != cudaSuccess)
-                return PVVC_ERR_CUDA;
-        }
-    } else {
-        if (launch_rlgr(dw, ord, p->nslices, payload, coef, rs, p->tune.rlgr_block, 0, s) != cudaSuccess || !mark(2))
+    auto clear = [&](uint64_t from, uint64_t to) {
+        return to <= from || cudaMemsetAsync(coef + from, 0, 4ull * (to - from), s) == cudaSuccess;
+    };
+    auto fork = [&](const SideStream& sd) {
+        return cudaEventRecord(sd.fork, s) == cudaSuccess && cudaStreamWaitEvent(sd.s, sd.fork, 0) == cudaSuccess;
+    };
+    if (p->nlong == 0) {
+        // zero symbols are not written by the decoder: clear the planes first
+        if (!clear(0, p->coef_floats) ||
+            launch_rlgr(dw, ord, p->nslices, payload, coef, rs, p->tune.rlgr_block, 0, s) != cudaSuccess || !mark(2))
             return PVVC_ERR_CUDA;
         if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;
-        if (!raht_groups(0, p->ngroups_a, cnt)) return PVVC_ERR_CUDA;
+        if (!raht_groups(0, p->ngroups_a, cnt, gsc, p->grp_ctas, s)) return PVVC_ERR_CUDA;
+    } else {
+        // Size tiers, largest first in `order`: the long slices on SMs of their
+        // own (stream `side`), the medium ones (stream `side2`), the rest (this
+        // stream).  Each tier's planes are cleared just before it forks.
+        const SideStream& L = p->side;
+        const SideStream& M = p->side2;
+        const int nl = p->nlong, nm = p->nmid, ns = p->nslices - nl - nm;
+        const uint64_t cl = p->coef_long_floats, cm = std::max(p->coef_mid_floats, cl);
+        if (!clear(0, cl) || !fork(L) ||
+            launch_rlgr_long(dw, ord, nl, payload, coef, rs, p->tune.rlgr_long_lanes, kRlgrLongSmem, L.s) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        if (nm > 0 && (!clear(cl, cm) || !fork(M) ||
+                       launch_rlgr(dw, ord + nl, nm, payload, coef, rs, p->tune.rlgr_block, kRlgrShortSmem, M.s) !=
+                           cudaSuccess ||
+                       cudaEventRecord(M.mid, M.s) != cudaSuccess))
+            return PVVC_ERR_CUDA;
+        if (!clear(nm > 0 ? cm : cl, p->coef_floats) ||
+            launch_rlgr(dw, ord + nl + nm, ns, payload, coef, rs, p->tune.rlgr_block, kRlgrShortSmem, s) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        const int na_l = p->ngroups_a_long, na_m = p->ngroups_a_mid, na_s = p->ngroups_a - na_l - na_m;
+        if (events) {
+            // stage markers: every tier decoded, then every group
+            if (cudaEventRecord(L.join, L.s) != cudaSuccess || cudaStreamWaitEvent(s, L.join, 0) != cudaSuccess ||
+                (nm > 0 && cudaStreamWaitEvent(s, M.mid, 0) != cudaSuccess) || !mark(2) ||
+                !raht_groups(0, p->ngroups_a, cnt, gsc, p->grp_ctas, s))
+                return PVVC_ERR_CUDA;
+        } else {
+            // Each tier's groups follow its decode on its stream.  A group can
+            // straddle a size cut, so a tier's groups also wait for the
+            // smaller tiers' decode (which ends sooner); all wait for the trees.
+            if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;
+            if (cudaEventRecord(L.mid, s) != cudaSuccess) return PVVC_ERR_CUDA;  // the small tier decoded, trees built
+            if (nm > 0 && (cudaStreamWaitEvent(M.s, L.mid, 0) != cudaSuccess ||
+                           !raht_groups(na_l, na_m, cnt + 3, reinterpret_cast<float*>(w + p->ws_grp_mid), p->grp_ctas_mid,
+                                        M.s) ||
+                           cudaEventRecord(M.join, M.s) != cudaSuccess))
+                return PVVC_ERR_CUDA;
+            if (cudaStreamWaitEvent(L.s, L.mid, 0) != cudaSuccess ||
+                (nm > 0 && cudaStreamWaitEvent(L.s, M.mid, 0) != cudaSuccess) ||
+                !raht_groups(0, na_l, cnt, reinterpret_cast<float*>(w + p->ws_grp_long), p->grp_ctas_long, L.s) ||
+                cudaEventRecord(L.join, L.s) != cudaSuccess)
+                return PVVC_ERR_CUDA;
+            if (!raht_groups(na_l + na_m, na_s, cnt + 2, gsc, p->grp_ctas, s) ||
+                cudaStreamWaitEvent(s, L.join, 0) != cudaSuccess || (nm > 0 && cudaStreamWaitEvent(s, M.join, 0) != cudaSuccess))
+                return PVVC_ERR_CUDA;
+        }
     }
     // phase A: the slices of slots without a group here, inverse-transformed by a CTA each
     if (launch_raht_slice(dw, di + p->list_a_off, p->nlist_a, st->v, coef, fb, ts, rs, fs, xyz, rgb, p24, status, kRahtWcap,
@@ -453,8 +486,10 @@ extern "C" int pvvc_plan_info_get(const pvvc_plan* p, pvvc_plan_info* info) {
     info->group_ctas = p->grp_ctas;
     info->tune = p->tune;
     if (p->nslices > 0)
-        info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) +
-                        (p->nlong > 0 ? (p->ngroups_a_long > 0) + (p->ngroups_a > p->ngroups_a_long) : (p->ngroups_a > 0)) +
+        info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) + (p->nmid > 0) +
+                        (p->nlong > 0 ? (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
+                                            (p->ngroups_a > p->ngroups_a_long + p->ngroups_a_mid)
+                                      : (p->ngroups_a > 0)) +
                         (p->nlist_a > 0) + (p->ngroups_b > 0) + (p->nlist_b > 0);
     return PVVC_OK;
 }
@@ -520,17 +555,26 @@ extern "C" int pvvc_plan_autotune(const pvvc_batch_desc* desc, pvvc_state* st, c
     const int32_t groups[] = {2, 4, 8, 16};
     const int32_t blocks[] = {32, 64, 128, 256};
     const int32_t longs[] = {-1, 16, 32, 48, 64, 96};
+    const int32_t mids[] = {-1, 15, 30, 50, 70};
+    const int32_t lanes[] = {8, 16, 32};
     for (int pass = 0; pass < 2; ++pass) {
         bool moved = false;
-        for (int field = 0; field < 4; ++field) {
-            const int32_t* cand = field == 0 ? ctas : field == 1 ? groups : field == 2 ? blocks : longs;
-            const int nc = field == 3 ? 6 : 4;
+        for (int field = 0; field < 6; ++field) {
+            const int32_t* cand = field == 0 ? ctas
+                                : field == 1 ? groups
+                                : field == 2 ? blocks
+                                : field == 3 ? longs
+                                : field == 4 ? mids
+                                             : lanes;
+            const int nc = field == 3 ? 6 : field == 4 ? 5 : field == 5 ? 3 : 4;
             for (int c = 0; c < nc; ++c) {
                 pvvc_tune t = cur;
                 int32_t* f = field == 0 ? &t.group_ctas_per_sm
                            : field == 1 ? &t.min_group
                            : field == 2 ? &t.rlgr_block
-                                        : &t.rlgr_long_ctas;
+                           : field == 3 ? &t.rlgr_long_ctas
+                           : field == 4 ? &t.rlgr_mid_pct
+                                        : &t.rlgr_long_lanes;
                 if (*f == cand[c]) continue;
                 *f = cand[c];
                 pvvc_plan pl;

@@ -16,6 +16,8 @@ cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payloa
                         cudaStream_t s);
 cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
                         int32_t* rstatus, int block, int smem, cudaStream_t s);
+cudaError_t launch_rlgr_long(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
+                             int32_t* rstatus, int lanes, int smem, cudaStream_t s);
 cudaError_t prepare_kernels();
 cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int count, const StateView& st, const float* coef,
                               float* fallback, const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz,
@@ -32,6 +34,8 @@ constexpr int kGroupCtasPerSm = 3;
 constexpr int kMinGroup = 4;
 constexpr int kRlgrBlock = 128;
 constexpr int kRlgrLongCtas = 32;
+constexpr int kRlgrMidPct = 30;
+constexpr int kRlgrLongLanes = 32;
 
 // the SM count (queried once)
 inline int sm_count() {
@@ -113,10 +117,11 @@ struct pvvc_plan {
     uint64_t total_points = 0;
     uint64_t ws_coef = 0, ws_fb = 0, ws_tstatus = 0, ws_rstatus = 0, ws_fstatus = 0, ws_bytes = 0;
     uint64_t ws_grp = 0, ws_counter = 0, grp_floats = 0;  // group-kernel level buffers, queue counters
-    int32_t grp_ctas = 0, grp_ctas_long = 0;
-    uint64_t ws_grp_long = 0;  // level buffers of the long-slice groups' launch
+    int32_t grp_ctas = 0, grp_ctas_long = 0, grp_ctas_mid = 0;
+    uint64_t ws_grp_long = 0, ws_grp_mid = 0;  // level buffers of the long and medium groups' launches
     uint64_t coef_floats = 0;
     uint64_t coef_long_floats = 0;  // planes prefix the long-slice RLGR launch writes
+    uint64_t coef_mid_floats = 0;   // ... and the medium tier
     std::vector<pvvc::SliceWork> work;
     std::vector<int32_t> order;
     // inverse-RAHT schedule: phase A needs only this batch's trees; phase B
@@ -125,12 +130,15 @@ struct pvvc_plan {
     std::vector<pvvc::GroupDesc> groups;  // [A groups | B groups]
     int32_t ngroups_a = 0, ngroups_b = 0;
     int32_t ngroups_a_long = 0;           // leading phase-A groups that hold a long-launch slice
+    int32_t ngroups_a_mid = 0;            // the next phase-A groups: a medium-tier slice, no long one
     std::vector<int32_t> idx;             // [group items | slice list A | slice list B]
     int32_t nlist_a = 0, nlist_b = 0, list_a_off = 0, list_b_off = 0;
     pvvc::DevBuf d_work, d_order, d_groups, d_idx;
     pvvc::HostBuf h_work, h_order, h_groups, h_idx;  // pinned mirrors of stream-ordered uploads
     int32_t nlong = 0;       // the first nlong slices of `order` go to the long-slice RLGR launch
-    pvvc::SideStream side;   // its stream
+    int32_t nmid = 0;        // the next nmid slices to the medium tier
+    pvvc::SideStream side;   // the long tier's stream
+    pvvc::SideStream side2;  // the medium tier's stream
     pvvc::SideStream tree;   // the tree expansion's stream (beside the coefficient clear and RLGR)
 };
 

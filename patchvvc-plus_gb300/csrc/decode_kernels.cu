@@ -384,11 +384,17 @@ __device__ __forceinline__ uint32_t run_ones_length(uint32_t kP, uint32_t c) {
 // a run code longer than 32 bits, a Golomb-Rice code longer than 32 bits
 // (wide remainders, the 32-ones escape), symbols of 2^23 or more, and runs
 // that reach the end of a plane.
-template <int T>
+//
+// LANES < 32: only the first LANES lanes of each warp decode (the rest exit at
+// once), so a warp executes the union of fewer lanes' paths per iteration --
+// for the longest slices, whose serial chains set the kernel's length.
+template <int T, int LANES = 32>
 __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, const int32_t* __restrict__ order,
                                               int nslices, const uint8_t* __restrict__ payload, float* __restrict__ coef,
                                               int32_t* __restrict__ rstatus) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((g & 31) >= LANES) return;
+    const int t = (g >> 5) * LANES + (g & 31);
     if (t >= nslices) return;
     const int item = order[t];
     const SliceWork& wk = work[item];
@@ -1151,6 +1157,10 @@ cudaError_t prepare_kernels() {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rlgr<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rlgr<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_rlgr<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rlgr<256, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rlgr<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
     if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return e;
 }
@@ -1173,6 +1183,22 @@ cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices
         case 64: k_rlgr<64><<<grid, 64, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
         case 128: k_rlgr<128><<<grid, 128, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
         case 256: k_rlgr<256><<<grid, 256, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// The long-slice launch: kRlgrLongBlock slices per CTA, `lanes` (8, 16, 32)
+// of them per warp.
+cudaError_t launch_rlgr_long(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
+                             int32_t* rstatus, int lanes, int smem, cudaStream_t s) {
+    if (nslices <= 0) return cudaSuccess;
+    static_assert(kRlgrLongBlock == 128, "a long CTA holds 128 slices");
+    const int grid = (nslices + kRlgrLongBlock - 1) / kRlgrLongBlock;
+    switch (lanes) {
+        case 8: k_rlgr<512, 8><<<grid, 512, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 16: k_rlgr<256, 16><<<grid, 256, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        case 32: k_rlgr<128><<<grid, 128, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -31,7 +31,7 @@ class BatchDesc(C.Structure):
 
 class Tune(C.Structure):
     _fields_ = [("group_ctas_per_sm", C.c_int32), ("min_group", C.c_int32), ("rlgr_block", C.c_int32),
-                ("rlgr_long_ctas", C.c_int32)]
+                ("rlgr_long_ctas", C.c_int32), ("rlgr_mid_pct", C.c_int32), ("rlgr_long_lanes", C.c_int32)]
 
 
 class PlanInfo(C.Structure):

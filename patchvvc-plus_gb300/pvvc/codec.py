@@ -126,18 +126,19 @@ def _desc(b: Batch):
 
 def _tune(t) -> L.Tune:
     if t is None:
-        return L.Tune(0, 0, 0, 0)
+        return L.Tune(0, 0, 0, 0, 0, 0)
     if isinstance(t, L.Tune):
         return t
     if isinstance(t, dict):
         return L.Tune(int(t.get("group_ctas_per_sm", 0)), int(t.get("min_group", 0)), int(t.get("rlgr_block", 0)),
-                      int(t.get("rlgr_long_ctas", 0)))
+                      int(t.get("rlgr_long_ctas", 0)), int(t.get("rlgr_mid_pct", 0)), int(t.get("rlgr_long_lanes", 0)))
     return L.Tune(*[int(x) for x in t])
 
 
 def tune_dict(t: L.Tune) -> dict:
     return {"group_ctas_per_sm": int(t.group_ctas_per_sm), "min_group": int(t.min_group), "rlgr_block": int(t.rlgr_block),
-            "rlgr_long_ctas": int(t.rlgr_long_ctas)}
+            "rlgr_long_ctas": int(t.rlgr_long_ctas), "rlgr_mid_pct": int(t.rlgr_mid_pct),
+            "rlgr_long_lanes": int(t.rlgr_long_lanes)}
 
 
 def autotune(b: Batch, dec: "Decoder", payload_ptr: int, reps: int = 3, stream: int = 0) -> tuple[dict, float]:

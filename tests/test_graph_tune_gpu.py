@@ -22,9 +22,11 @@ def gop(pvvc_lib):
     return pvvc_lib.pack_frames([pvvc_lib.parse_frame(b) for b in s.frames()])
 
 
-# (group CTAs per SM, min group, RLGR block, long-slice CTAs; -1 = no split)
+# (group CTAs per SM, min group, RLGR block, long-slice CTAs (-1: no split), medium-tier % (-1: none),
+#  slices per warp of the long launch)
 TUNES = [
-    (1, 1, 32, -1), (2, 2, 64, 1), (3, 4, 128, -1), (4, 16, 256, 4), (1, 32, 128, 32), (2, 8, 32, 2), (4, 3, 64, 96),
+    (1, 1, 32, -1, -1, 32), (2, 2, 64, 1, -1, 8), (3, 4, 128, -1, 30, 16), (4, 16, 256, 4, 50, 16), (1, 32, 128, 32, 15, 32),
+    (2, 8, 32, 2, 70, 8), (4, 3, 64, 96, 90, 8),
 ]
 
 
@@ -40,11 +42,12 @@ def test_every_launch_shape_decodes_identically(pvvc_lib, torch, gop):
 
 def test_plan_info_counts(pvvc_lib, gop):
     default = pvvc_lib.Plan(gop).info()
-    assert default["tune"] == {"group_ctas_per_sm": 3, "min_group": 4, "rlgr_block": 128, "rlgr_long_ctas": 32}
+    assert default["tune"] == {"group_ctas_per_sm": 3, "min_group": 4, "rlgr_block": 128, "rlgr_long_ctas": 32,
+                               "rlgr_mid_pct": 30, "rlgr_long_lanes": 32}
     assert default["nslices"] == gop.nslices
     assert default["nintra"] == int(((gop.type & 0x02) == 0).sum())
     # every slot's intra slice heads a phase-A group; 8 frames -> its 7 P slices join it
-    ones = pvvc_lib.Plan(gop, tune=(3, 32, 128, -1)).info()
+    ones = pvvc_lib.Plan(gop, tune=(3, 32, 128, -1, -1, 32)).info()
     assert ones["groups_a"] == default["nintra"] and ones["singles_a"] == 0
     k = ones
     assert k["kernels"] == 2 + (k["groups_a"] > 0) + (k["singles_a"] > 0) + (k["groups_b"] > 0) + (k["singles_b"] > 0)
@@ -58,7 +61,8 @@ def test_autotune_returns_a_valid_shape(pvvc_lib, torch, gop):
     best, ms = pvvc_lib.autotune(gop, dec, pay.data_ptr(), reps=2, stream=stream)
     assert ms > 0
     assert best["group_ctas_per_sm"] in (1, 2, 3, 4) and best["rlgr_block"] in (32, 64, 128, 256)
-    assert best["rlgr_long_ctas"] in (-1, 16, 32, 48, 64, 96)
+    assert best["rlgr_long_ctas"] in (-1, 16, 32, 48, 64, 96) and best["rlgr_mid_pct"] in (-1, 15, 30, 50, 70)
+    assert best["rlgr_long_lanes"] in (8, 16, 32)
     assert 1 <= best["min_group"] <= 32
     out = decode_batch(torch, pvvc_lib, dec, gop, tune=best)
     for a, b in zip(ref, out):

@@ -105,7 +105,9 @@ def test_synth_is_deterministic_and_sized(pvvc_lib):
 def test_invalid_launch_shape_is_rejected_before_any_device_work(pvvc_lib):
     s = pvvc_lib.Synth(pvvc_lib.config("tiny", seed=3))
     batch = pvvc_lib.pack_frames([pvvc_lib.parse_frame(b) for b in s.frames()[:1]])
-    for t in [(5, 4, 128, 0), (1, 33, 128, 0), (1, 4, 96, 0), (-1, 4, 128, 0), (1, 4, 128, 153), (1, 4, 128, -2)]:
+    for t in [(5, 4, 128, 0, 0, 0), (1, 33, 128, 0, 0, 0), (1, 4, 96, 0, 0, 0), (-1, 4, 128, 0, 0, 0),
+              (1, 4, 128, 153, 0, 0), (1, 4, 128, -2, 0, 0), (1, 4, 128, 0, 91, 0), (1, 4, 128, 0, -2, 0),
+              (1, 4, 128, 0, 0, 12)]:
         with pytest.raises(pvvc_lib.PvvcError) as e:
             pvvc_lib.Plan(batch, tune=t)
         assert e.value.status == 1
