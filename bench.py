@@ -61,6 +61,7 @@ def parse_args():
                                                "instead of the autotuner")
     ap.add_argument("--icp-pairs", type=int, default=4096, help="batched ICP workload size (0: skip)")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned-ICP comparison")
+    ap.add_argument("--no-encode", dest="encode", action="store_false", help="skip the GPU encoder measurement")
     ap.add_argument("--learned-train-pairs", type=int, default=32768, help="pairs to train on when no weights are committed")
     ap.add_argument("--learned-train-epochs", type=int, default=8)
     ap.add_argument("--serve-streams", type=int, default=64, help="playback streams of the serving run (0: skip)")
@@ -328,13 +329,15 @@ def run_ours(args):
         cb = cpu_baseline(frames, args.cpu_seconds)
         icp = measure_icp(args, torch, peak) if args.icp_pairs > 0 else None
         learned = measure_learned(args, torch, pvvc) if args.icp_pairs > 0 and args.learned else None
+        encode = measure_encode(args, torch, pvvc, s, len(frames)) if args.encode else None
         serving = measure_serving(args, pvvc) if args.serve_streams > 0 and args.serve_seconds > 0 else None
         out = {"metric": "decoded Mpts/s (seq300, GoP 30, ~800k pts/frame)", "value": value, "unit": "Mpts/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
                "clocks": clk.summary(), "gpu_launches": info["kernels"] * args.steps, "points_per_step": P * world,
-               "plan": info, "autotune_ms": tune_ms, "icp": icp, "learned_icp": learned, "serving": serving}
+               "plan": info, "autotune_ms": tune_ms, "icp": icp, "learned_icp": learned, "encode": encode,
+               "serving": serving}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
@@ -442,6 +445,102 @@ def measure_learned(args, torch, pvvc):
             "mse_ratio_percentiles": {f"p{q}": float(np.percentile(ml / np.maximum(mse_plain, 1e-12), q))
                                       for q in (10, 50, 90, 99)},
             "rule": "proposal + <=10 ICP iterations (accept on relative dMSE < 1e-3), else plain ICP from identity"}
+
+
+def measure_encode(args, torch, pvvc, synth, nframes):
+    """GPU encoder back end on the decode workload: the colour payloads of all
+    slices of the sequence (every GoP's patches, 30 frames each: frame 0
+    absolute, the rest residuals), from per-leaf YUV and the geometry
+    payloads, in one pvvc_encode_colors call.  CPU baseline: the byte-identical
+    host encoder (pvvc_encode_patch_gop, one core) on a bounded sample of
+    patch GoPs."""
+    t0 = time.time()
+    gof = 30
+    ngof = (nframes + gof - 1) // gof
+    frames, leaves, sample = [], [], []
+    import concurrent.futures as cf
+
+    def one(gp):  # the C calls release the GIL
+        xyz, yuv, _ = synth.patch(*gp)
+        return (xyz, yuv) if gp[1] < 8 and gp[0] < 8 else None, pvvc.patch_leaf_yuv(xyz, yuv)
+
+    with cf.ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 4)) as ex:
+        for g in range(ngof):
+            npat = synth.patch_count(g)
+            geos = []
+            for smp, (geo, nl, leaf) in ex.map(one, [(g, p_) for p_ in range(npat)]):
+                geos.append((geo, nl))
+                leaves.append(leaf)
+                if smp is not None:
+                    sample.append(smp)
+            nf = min(gof, nframes - g * gof)
+            for f in range(nf):
+                frames.append((g, f, npat, geos))
+    # one batch: GoP g's patches in slots [g*stride, (g+1)*stride)
+    stride = max(fr[2] for fr in frames)
+    flist = []
+    for g, f, npat, geos in frames:
+        flist.append(pvvc.Frame(g * gof + f, np.arange(npat, dtype=np.int32), np.full(npat, 1 if f == 0 else 3, np.uint8),
+                                np.array([q[1] for q in geos], np.uint32), np.full(npat, args.qp, np.uint8),
+                                np.tile(np.eye(4, dtype=np.float32).reshape(16), (npat, 1)),
+                                [q[0] if f == 0 else b"" for q in geos], [b""] * npat))
+    per_gop = [[fr for fr in flist if fr.timestamp // gof == g] for g in range(ngof)]
+    batch = pvvc.concat_batches([pvvc.pack_frames(fs) for fs in per_gop], slot_stride=stride)
+    leaf_yuv = np.zeros((batch.points, 3), np.float32)
+    k = 0
+    base = 0
+    for g in range(ngof):
+        npat = synth.patch_count(g)
+        for f in range(min(gof, nframes - g * gof)):
+            for p_ in range(npat):
+                o = int(batch.out_off[k])
+                lf = leaves[base + p_][f]
+                leaf_yuv[o:o + lf.shape[0]] = lf
+                k += 1
+        base += npat
+    setup = time.time() - t0
+    dec = pvvc.Decoder(nslots=stride * ngof, max_leaves=8192, max_nodes=16384)
+    enc = pvvc.Encoder()
+    cap = ((8 * batch.size.astype(np.uint64) + 64 + 3) // 4 * 4).astype(np.uint32)
+    off = np.concatenate([[0], np.cumsum(cap.astype(np.uint64))[:-1]]).astype(np.uint64)
+    dev = torch.device("cuda")
+    pay = torch.from_numpy(batch.payload).to(dev)
+    ly = torch.from_numpy(leaf_yuv).to(dev)
+    out = torch.empty(int(cap.astype(np.uint64).sum()) + 16, dtype=torch.uint8, device=dev)
+    olen = torch.empty(batch.nslices, dtype=torch.int32, device=dev)
+    st = torch.empty(batch.nslices, dtype=torch.int32, device=dev)
+    sp = torch.cuda.current_stream().cuda_stream
+
+    def call():
+        enc.encode(batch, dec, pay.data_ptr(), ly.data_ptr(), out.data_ptr(), off, cap, olen.data_ptr(), st.data_ptr(), sp)
+
+    call()
+    assert (st.cpu().numpy() == 0).all()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record()
+    for _ in range(reps):
+        call()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    nbytes = int(olen.cpu().numpy().astype(np.int64).sum())
+    # CPU: the host encoder on sample patch GoPs (30 frames each), one core
+    c0 = time.perf_counter()
+    cpts = 0
+    for xyz, yuv in sample:
+        pvvc.encode_patch_gop(xyz, yuv, [args.qp] * yuv.shape[0])
+        cpts += xyz.shape[0] * yuv.shape[0]
+        if time.perf_counter() - c0 > args.cpu_seconds / 4:
+            break
+    cdt = time.perf_counter() - c0
+    log(f"encode: {batch.points} points in {ms:.2f} ms (setup {setup:.1f}s)")
+    return {"points": batch.points, "slices": batch.nslices, "ms": ms, "mpts_per_s": batch.points / (ms / 1e3) / 1e6,
+            "colour_bytes": nbytes, "bits_per_point": 8 * nbytes / batch.points,
+            "what": "forward RAHT + quantisation + RLGR of every slice (k_tree from the geometry payloads included)",
+            "cpu_baseline": {"value": cpts / cdt / 1e6, "unit": "Mpts/s", "cores": 1, "kind": "port",
+                             "sample": f"host encoder (octree, RAHT, quantisation, RLGR) on {len(sample)} patch GoPs, "
+                                       f"{cdt:.1f}s"}}
 
 
 def measure_serving(args, pvvc):

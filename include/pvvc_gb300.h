@@ -206,6 +206,36 @@ int pvvc_encode_patch_gop(const float* xyz, uint32_t n, const float* yuv, int32_
                           uint8_t* geo_out, uint64_t geo_cap, uint64_t* geo_len, uint8_t* col_out, uint64_t col_cap_per_frame,
                           uint64_t* col_len, uint32_t* leaf_count);
 
+/* Octree geometry payload of one patch and, per frame, its leaf signal: each
+ * leaf's mean YUV in decode (BFS) leaf order (RAHTOctree::MakeTree/GetOctree
+ * and the voxel averaging of RAHTOctree::RAHT, src/octree/raht_octree.cc:47-
+ * 211).  yuv: nframes x n x 3; leaf_out: nframes x leaf_cap x 3.  The input
+ * of pvvc_encode_colors. */
+int pvvc_patch_leaf_yuv(const float* xyz, uint32_t n, const float* yuv, int32_t nframes, uint8_t* geo_out,
+                        uint64_t geo_cap, uint64_t* geo_len, float* leaf_out, uint64_t leaf_cap, uint32_t* leaf_count);
+
+/* ---- GPU encoder back end -------------------------------------------------
+ * Colour payloads of a batch of slices on the GPU: forward RAHT
+ * (RAHTOctree::RAHT, src/octree/raht_octree.cc:189-247, HaarTransform
+ * octree_base.cc:164-184), quantisation (GoP_encoding.cc:184-189) and RLGR
+ * (RLGREncoder, src/common/entropy_codec.cc:65-159), byte-identical to the
+ * CPU encoder.  The batch is described as for pvvc_decode: slot, type (an
+ * intra slice's geometry payload at geo_off in `payload`, device, 16-byte
+ * aligned), size, qp; col_off/col_size are ignored.  leaf_yuv (device):
+ * slice k's leaf signal (pvvc_patch_leaf_yuv; frame 0 of a GoP absolute,
+ * later frames residuals) at float offset 3 * out_off[k].  out (device): slice
+ * k's payload at byte offset out_byte_off[k] (host array, multiple of 4), at
+ * most out_cap[k] bytes (host array, multiple of 4); out_len (device) gets
+ * its length, status (device) a PVVC status per slice (PVVC_ERR_CAPACITY when
+ * the payload does not fit).  Intra slices rebuild their slot's tree in `st`
+ * as decoding does.  Synchronises `stream`. */
+typedef struct pvvc_encoder pvvc_encoder;
+int pvvc_encoder_create(pvvc_encoder** out);
+int pvvc_encoder_destroy(pvvc_encoder* enc);
+int pvvc_encode_colors(pvvc_encoder* enc, const pvvc_batch_desc* desc, pvvc_state* st, const uint8_t* payload,
+                       const float* leaf_yuv, uint8_t* out, const uint64_t* out_byte_off, const uint32_t* out_cap,
+                       uint32_t* out_len, int32_t* status, void* stream);
+
 /* RLGR codec on host buffers (entropy_codec.cc:65-283) */
 int64_t pvvc_rlgr_encode(const int64_t* sym, uint64_t n, uint8_t* out, uint64_t cap);
 int pvvc_rlgr_decode_host(const uint8_t* in, uint64_t nbytes, uint64_t nsym, int64_t* out);

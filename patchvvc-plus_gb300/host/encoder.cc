@@ -284,16 +284,13 @@ namespace {
 struct YUV {
     float y, u, v;
 };
+static_assert(sizeof(YUV) == 12, "YUV rows alias float[3]");
 inline YUV axpby(YUV a, float s, YUV b, float t) {  // a*s + b*t, per channel
     return {a.y * s + b.y * t, a.u * s + b.u * t, a.v * s + b.v * t};
 }
 }  // namespace
 
-void PatchTree::raht(const float* yuv, std::vector<float>* coef_out) const {
-    const int H = height_;
-    // leaf signal: mean colour of the voxel's points (raht_octree.cc:204-211)
-    std::vector<YUV> g(leaf_count_), gn;
-    std::vector<int32_t> w(leaf_count_, 1), wn;
+void PatchTree::leaf_yuv(const float* yuv, float* out) const {
     for (size_t j = 0; j < leaf_count_; ++j) {
         YUV t{0, 0, 0};
         for (uint32_t q = leaf_first_[j]; q < leaf_first_[j + 1]; ++q) {
@@ -303,8 +300,18 @@ void PatchTree::raht(const float* yuv, std::vector<float>* coef_out) const {
             t.v += c[2];
         }
         const float cnt = (float)(leaf_first_[j + 1] - leaf_first_[j]);
-        g[j] = {t.y / cnt, t.u / cnt, t.v / cnt};
+        out[3 * j] = t.y / cnt;
+        out[3 * j + 1] = t.u / cnt;
+        out[3 * j + 2] = t.v / cnt;
     }
+}
+
+void PatchTree::raht(const float* yuv, std::vector<float>* coef_out) const {
+    const int H = height_;
+    // leaf signal: mean colour of the voxel's points (raht_octree.cc:204-211)
+    std::vector<YUV> g(leaf_count_), gn;
+    std::vector<int32_t> w(leaf_count_, 1), wn;
+    leaf_yuv(yuv, reinterpret_cast<float*>(g.data()));
     // bottom-up HierarchicalTransform (octree_base.cc:65-82); the AC
     // coefficients of each level are kept to be emitted top-down later.
     std::vector<std::vector<YUV>> ac(H > 1 ? H - 1 : 0);
@@ -414,5 +421,21 @@ extern "C" int pvvc_encode_patch_gop(const float* xyz, uint32_t n, const float* 
         std::memcpy(col_out + col_cap_per_frame * f, c.data(), c.size());
         col_len[f] = c.size();
     }
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_patch_leaf_yuv(const float* xyz, uint32_t n, const float* yuv, int32_t nframes, uint8_t* geo_out,
+                                   uint64_t geo_cap, uint64_t* geo_len, float* leaf_out, uint64_t leaf_cap,
+                                   uint32_t* leaf_count) {
+    if (!xyz || !n || !yuv || nframes <= 0 || !geo_out || !geo_len || !leaf_out || !leaf_count) return PVVC_ERR_ARG;
+    pvvc::PatchTree t;
+    int s = t.build(xyz, n);
+    if (s) return s;
+    auto g = t.geometry();
+    if (g.size() > geo_cap || t.leaf_count() > leaf_cap) return PVVC_ERR_CAPACITY;
+    std::memcpy(geo_out, g.data(), g.size());
+    *geo_len = g.size();
+    *leaf_count = (uint32_t)t.leaf_count();
+    for (int f = 0; f < nframes; ++f) t.leaf_yuv(yuv + 3ull * n * f, leaf_out + 3ull * leaf_cap * f);
     return PVVC_OK;
 }

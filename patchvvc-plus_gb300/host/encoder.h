@@ -29,6 +29,9 @@ class PatchTree {
     // Forward RAHT of per-input-point YUV (n x 3): leaf_count x 3
     // coefficients in stream (reversed) order (raht_octree.cc:189-247).
     void raht(const float* yuv, std::vector<float>* coef) const;
+    // Leaf signal of per-input-point YUV (n x 3): each leaf's mean colour in
+    // decode (BFS) leaf order, leaf_count x 3 (raht_octree.cc:204-211)
+    void leaf_yuv(const float* yuv, float* out) const;
     // leaf (decode-order) index of each input point
     const std::vector<uint32_t>& point_leaf() const { return point_leaf_; }
 

@@ -95,6 +95,11 @@ SIGNATURES = [
     ("pvvc_encode_patch_gop", C.c_int, [f32p, C.c_uint32, f32p, C.c_int32, u8p, u8p, C.c_uint64, u64p, u8p,
                                         C.c_uint64, u64p, u32p]),
     ("pvvc_rlgr_encode", C.c_int64, [i64p, C.c_uint64, u8p, C.c_uint64]),
+    ("pvvc_patch_leaf_yuv", C.c_int, [f32p, C.c_uint32, f32p, C.c_int32, u8p, C.c_uint64, u64p, f32p, C.c_uint64,
+                                      C.POINTER(C.c_uint32)]),
+    ("pvvc_encoder_create", C.c_int, [C.POINTER(vp)]),
+    ("pvvc_encoder_destroy", C.c_int, [vp]),
+    ("pvvc_encode_colors", C.c_int, [vp, C.POINTER(BatchDesc), vp, vp, vp, vp, u64p, C.POINTER(C.c_uint32), vp, vp, vp]),
     ("pvvc_rlgr_decode_host", C.c_int, [u8p, C.c_uint64, C.c_uint64, i64p]),
     ("pvvc_icp_workspace_size", C.c_int, [C.c_int32, C.c_uint64, C.c_uint64, u64p]),
     ("pvvc_icp_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, C.POINTER(IcpParams), vp, vp, vp, vp, vp, C.c_uint64,

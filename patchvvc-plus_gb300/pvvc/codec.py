@@ -225,3 +225,53 @@ class Graph:
             self.close()
         except Exception:
             pass
+
+
+def patch_leaf_yuv(xyz: np.ndarray, yuv: np.ndarray) -> tuple[bytes, int, np.ndarray]:
+    """Geometry payload, leaf count and per-frame leaf signal (frames x
+    leaves x 3, each leaf's mean YUV in decode leaf order) of one patch.
+    yuv: (nframes, n, 3): frame 0 absolute, later frames residuals."""
+    xyz = np.ascontiguousarray(xyz, np.float32)
+    yuv = np.ascontiguousarray(yuv, np.float32)
+    n, nf = xyz.shape[0], yuv.shape[0]
+    geo = np.zeros(25 + 32 * n + 64, np.uint8)
+    leaf = np.zeros((nf, n, 3), np.float32)
+    glen = C.c_uint64(0)
+    nl = C.c_uint32(0)
+    L.check(L.lib().pvvc_patch_leaf_yuv(_p(xyz, L.f32p), n, _p(yuv, L.f32p), nf, _p(geo, L.u8p), geo.size, C.byref(glen),
+                                        _p(leaf, L.f32p), n, C.byref(nl)), "pvvc_patch_leaf_yuv")
+    k = int(nl.value)
+    return geo[:glen.value].tobytes(), k, np.ascontiguousarray(leaf[:, :k])
+
+
+class Encoder:
+    """GPU colour encoder (pvvc_encode_colors): forward RAHT, quantisation and
+    RLGR of a batch of slices on the device."""
+
+    def __init__(self):
+        self.h = L.vp()
+        L.check(L.lib().pvvc_encoder_create(C.byref(self.h)), "pvvc_encoder_create")
+
+    def close(self):
+        if self.h:
+            L.lib().pvvc_encoder_destroy(self.h)
+            self.h = L.vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def encode(self, batch: Batch, dec: "Decoder", payload_ptr: int, leaf_yuv_ptr: int, out_ptr: int,
+               out_off: np.ndarray, out_cap: np.ndarray, out_len_ptr: int, status_ptr: int, stream: int = 0) -> None:
+        """Device buffers by pointer: payload (the batch's, 16-byte aligned),
+        leaf_yuv (float, slice k at 3*batch.out_off[k]), out (bytes), out_len
+        (uint32 per slice), status (int32 per slice).  out_off / out_cap:
+        host uint64 / uint32 arrays (multiples of 4)."""
+        d, keep = _desc(batch)
+        off = np.ascontiguousarray(out_off, np.uint64)
+        cap = np.ascontiguousarray(out_cap, np.uint32)
+        L.check(L.lib().pvvc_encode_colors(self.h, C.byref(d), dec.h, payload_ptr, leaf_yuv_ptr, out_ptr,
+                                           _p(off, L.u64p), _p(cap, L.u32p), out_len_ptr, status_ptr, stream),
+                "pvvc_encode_colors")
