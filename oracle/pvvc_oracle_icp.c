@@ -125,13 +125,15 @@ static double grid_nn(const grid_t* g, const double q[3], int* idx) {
     return best;
 }
 
-/* ---- 3x3 SVD by one-sided Jacobi (double) ---- */
+/* ---- 3x3 SVD by one-sided Jacobi (double) ----
+ * A pair of columns is rotated while |c| > 1e-15 sqrt(a b) (Demmel-Veselic
+ * relative test); the sweeps end when a whole sweep rotates nothing. */
 static void svd3(const double A[9], double U[9], double S[3], double V[9]) {
     double B[9];
     memcpy(B, A, sizeof(B));
     for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
     for (int sweep = 0; sweep < 60; ++sweep) {
-        double off = 0;
+        int rotated = 0;
         for (int p = 0; p < 2; ++p)
             for (int q = p + 1; q < 3; ++q) {
                 double a = 0, b = 0, c = 0;
@@ -140,8 +142,8 @@ static void svd3(const double A[9], double U[9], double S[3], double V[9]) {
                     b += B[3 * i + q] * B[3 * i + q];
                     c += B[3 * i + p] * B[3 * i + q];
                 }
-                off += c * c;
-                if (fabs(c) < 1e-300) continue;
+                if (!(fabs(c) > 1e-15 * sqrt(a * b))) continue;
+                rotated = 1;
                 double zeta = (b - a) / (2 * c);
                 double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1 + zeta * zeta));
                 double cs = 1 / sqrt(1 + t * t), sn = cs * t;
@@ -154,7 +156,7 @@ static void svd3(const double A[9], double U[9], double S[3], double V[9]) {
                     V[3 * i + q] = sn * vp + cs * vq;
                 }
             }
-        if (off < 1e-30) break;
+        if (!rotated) break;
     }
     for (int j = 0; j < 3; ++j) {
         double s = sqrt(B[j] * B[j] + B[3 + j] * B[3 + j] + B[6 + j] * B[6 + j]);

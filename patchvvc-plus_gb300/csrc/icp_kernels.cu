@@ -5,7 +5,8 @@
 // ICPBase::CloudMSE (src/registration/registration_base.cc:114-158).
 //
 //   k_grid   one CTA per pair: a uniform grid over the target points
-//            (at most 16 cells per axis): bounding box by block reduction,
+//            (at most 4096 cubic cells, spread over the box's shape):
+//            bounding box by block reduction,
 //            counting sort of the points into cells (shared-memory
 //            histogram + block scan), written to the workspace.
 //   k_icp    one CTA per pair, all iterations: each thread transforms its
@@ -87,13 +88,30 @@ __global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const
                 s_red[0][k] = fminf(s_red[0][k], s_red[w][k]);
                 s_red[0][3 + k] = fmaxf(s_red[0][3 + k], s_red[w][3 + k]);
             }
-        float ext = 0.f;
-        for (int k = 0; k < 3; ++k) ext = fmaxf(ext, s_red[0][3 + k] - s_red[0][k]);
+        // Cells spread over the box's own shape: edge h with about kCells
+        // cells in the box (an elongated patch gets more cells along its long
+        // axis), grown until the cell count fits; at least one voxel.
+        float e[3], ext = 0.f;
+        for (int k = 0; k < 3; ++k) {
+            e[k] = n ? s_red[0][3 + k] - s_red[0][k] : 0.f;
+            ext = fmaxf(ext, e[k]);
+        }
         GridHdr g;
-        g.h = fmaxf(ext / (float)kGridAxis * 1.0001f, 1.0f);
+        {
+            const float fl = fmaxf(ext / 1024.f, 1e-3f);  // floor for flat axes
+            const float vol = fmaxf(e[0], fl) * fmaxf(e[1], fl) * fmaxf(e[2], fl);
+            float h = fmaxf(cbrtf(vol / (float)kCells), 1.0f);
+            for (int guard = 0; guard < 200; ++guard) {
+                long long cells = 1;
+                for (int k = 0; k < 3; ++k) cells *= min((long long)floorf(e[k] / h) + 1, 1023ll);
+                if (cells <= kCells) break;
+                h *= 1.05f;
+            }
+            g.h = h;
+        }
         for (int k = 0; k < 3; ++k) {
             g.lo[k] = n ? s_red[0][k] : 0.f;
-            g.dim[k] = n ? min((int)floorf((s_red[0][3 + k] - s_red[0][k]) / g.h) + 1, kGridAxis) : 1;
+            g.dim[k] = n ? min((int)floorf(e[k] / g.h) + 1, 1023) : 1;
             s_box[k] = g.lo[k];
         }
         s_box[3] = g.h;
@@ -175,7 +193,17 @@ __device__ __forceinline__ float grid_nn(const GridHdr& g, const int* __restrict
         }
         for (int z = max(cz - r, 0); z <= min(cz + r, g.dim[2] - 1); ++z) {
             const bool zr = (z == cz - r) || (z == cz + r);
+            // squared distance from q to the cell's box along an axis
+            auto gap2 = [&](int c, float q, float lo) {
+                const float a = lo + (float)c * g.h, b = a + g.h;
+                const float d = q < a ? a - q : (q > b ? q - b : 0.f);
+                return d * d;
+            };
+            const float dz2 = gap2(z, qz, g.lo[2]);
+            if (dz2 * 0.999f > best) continue;
             for (int y = max(cy - r, 0); y <= min(cy + r, g.dim[1] - 1); ++y) {
+                const float dyz2 = dz2 + gap2(y, qy, g.lo[1]);
+                if (dyz2 * 0.999f > best) continue;
                 const bool yr = zr || (y == cy - r) || (y == cy + r);
                 // on interior rows only the two x faces belong to the ring
                 int x = max(cx - r, 0);
@@ -183,6 +211,9 @@ __device__ __forceinline__ float grid_nn(const GridHdr& g, const int* __restrict
                 const int step = yr ? 1 : max(2 * r, 1);
                 if (!yr && x != cx - r) x = (cx + r <= xe) ? cx + r : xe + 1;
                 for (; x <= xe; x += step) {
+                    // a cell farther than the best so far cannot hold a strictly
+                    // closer point (0.999: margin for the rounding of the bound)
+                    if ((dyz2 + gap2(x, qx, g.lo[0])) * 0.999f > best) continue;
                     const int c = (z * g.dim[1] + y) * g.dim[0] + x;
                     const int e = __ldg(cs + c + 1);
                     for (int k = __ldg(cs + c); k < e; ++k) {
@@ -208,6 +239,11 @@ __device__ __forceinline__ float grid_nn(const GridHdr& g, const int* __restrict
 }
 
 // ---- FP64 3x3 Kabsch (one-sided Jacobi SVD) ---------------------------------
+// A pair of columns is rotated only while |c| > 1e-15 sqrt(a b) (their cosine
+// above about 4.5 FP64 ulps, the Demmel-Veselic test); the sweeps end when a
+// whole sweep rotates nothing.  The test is relative, so it ends after a few
+// sweeps whatever the scale of A (the correspondence sums reach 1e7 and
+// more); the rounding of c is below 3.5 ulps of sqrt(a b), so it always ends.
 __device__ void svd3(const double* A, double* U, double* S, double* V) {
     double B[9];
     for (int i = 0; i < 9; ++i) {
@@ -215,7 +251,7 @@ __device__ void svd3(const double* A, double* U, double* S, double* V) {
         V[i] = (i % 4 == 0) ? 1.0 : 0.0;
     }
     for (int sweep = 0; sweep < 40; ++sweep) {
-        double off = 0;
+        bool rotated = false;
         for (int p = 0; p < 2; ++p)
             for (int q = p + 1; q < 3; ++q) {
                 double a = 0, b = 0, c = 0;
@@ -224,8 +260,8 @@ __device__ void svd3(const double* A, double* U, double* S, double* V) {
                     b += B[3 * i + q] * B[3 * i + q];
                     c += B[3 * i + p] * B[3 * i + q];
                 }
-                off += c * c;
-                if (fabs(c) < 1e-300) continue;
+                if (!(fabs(c) > 1e-15 * sqrt(a * b))) continue;
+                rotated = true;
                 const double zeta = (b - a) / (2 * c);
                 const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1 + zeta * zeta));
                 const double cs = 1 / sqrt(1 + t * t), sn = cs * t;
@@ -238,7 +274,7 @@ __device__ void svd3(const double* A, double* U, double* S, double* V) {
                     V[3 * i + q] = sn * vp + cs * vq;
                 }
             }
-        if (off < 1e-30) break;
+        if (!rotated) break;
     }
     for (int j = 0; j < 3; ++j) {
         const double s = sqrt(B[j] * B[j] + B[3 + j] * B[3 + j] + B[6 + j] * B[6 + j]);
@@ -350,12 +386,16 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp(const float* __restrict__ s
             if (lane == 0) s_part[wid][k] = v;
         }
         __syncthreads();
+        // lane k of warp 0 totals sum k over the warps
+        if (wid == 0 && lane < kNSum) {
+            double v = 0;
+            for (int w = 0; w < kIcpThreads / 32; ++w) v += s_part[w][lane];
+            s_part[0][lane] = v;
+        }
+        __syncwarp();
         if (tid == 0) {
             double sum[kNSum];
-            for (int k = 0; k < kNSum; ++k) {
-                sum[k] = 0;
-                for (int w = 0; w < kIcpThreads / 32; ++w) sum[k] += s_part[w][k];
-            }
+            for (int k = 0; k < kNSum; ++k) sum[k] = s_part[0][k];
             const double cnt = sum[0];
             if (cnt < 3) {
                 s_done = 2;  // too few correspondences: not converged
