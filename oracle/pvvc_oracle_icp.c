@@ -36,6 +36,7 @@ typedef struct {
     int dim[3];
     int* start; /* cell -> first point (+ sentinel) */
     float* pts; /* points sorted by cell */
+    int* orig;  /* input index of each sorted point */
     size_t n;
 } grid_t;
 
@@ -56,8 +57,9 @@ static int grid_build(grid_t* g, const float* p, size_t n) {
     size_t nc = (size_t)g->dim[0] * g->dim[1] * g->dim[2];
     g->start = (int*)calloc(nc + 1, sizeof(int));
     g->pts = (float*)malloc(3 * n * sizeof(float) + 4);
+    g->orig = (int*)malloc(n * sizeof(int) + 4);
     int* cell = (int*)malloc(n * sizeof(int) + 4);
-    if (!g->start || !g->pts || !cell) { free(cell); return PVO_ERR_NOMEM; }
+    if (!g->start || !g->pts || !g->orig || !cell) { free(cell); return PVO_ERR_NOMEM; }
     for (size_t i = 0; i < n; ++i) {
         int c[3];
         for (int a = 0; a < 3; ++a) {
@@ -70,7 +72,10 @@ static int grid_build(grid_t* g, const float* p, size_t n) {
     for (size_t c = 0; c < nc; ++c) g->start[c + 1] += g->start[c];
     int* fill = (int*)malloc((nc + 1) * sizeof(int));
     memcpy(fill, g->start, (nc + 1) * sizeof(int));
-    for (size_t i = 0; i < n; ++i) memcpy(g->pts + 3 * fill[cell[i]]++, p + 3 * i, 3 * sizeof(float));
+    for (size_t i = 0; i < n; ++i) {
+        g->orig[fill[cell[i]]] = (int)i;
+        memcpy(g->pts + 3 * fill[cell[i]]++, p + 3 * i, 3 * sizeof(float));
+    }
     free(fill);
     free(cell);
     g->n = n;
@@ -80,10 +85,13 @@ static int grid_build(grid_t* g, const float* p, size_t n) {
 static void grid_free(grid_t* g) {
     free(g->start);
     free(g->pts);
+    free(g->orig);
 }
 
 /* squared distance to the nearest point, exact: rings of cells in growing
- * Chebyshev radius until the ring cannot hold anything closer */
+ * Chebyshev radius until the ring cannot hold anything closer.  Among points
+ * at the same distance the one first in the input wins, so the answer does
+ * not depend on the grid. */
 static double grid_nn(const grid_t* g, const double q[3], int* idx) {
     /* rings of cells around the query's cell clamped into the grid; a point in
      * ring r lies at least (r-1)*h from the query (also for queries outside) */
@@ -102,7 +110,7 @@ static double grid_nn(const grid_t* g, const double q[3], int* idx) {
     for (int r = 0; r <= maxr; ++r) {
         if (r > 0 && bi >= 0) {
             double lb = (r - 1) * g->h;
-            if (lb * lb > best) break;
+            if (lb * lb * 0.999 > best) break;
         }
         for (int z = c[2] - r; z <= c[2] + r; ++z) {
             if (z < 0 || z >= g->dim[2]) continue;
@@ -115,7 +123,7 @@ static double grid_nn(const grid_t* g, const double q[3], int* idx) {
                     for (int k = g->start[cc]; k < g->start[cc + 1]; ++k) {
                         double dx = g->pts[3 * k] - q[0], dy = g->pts[3 * k + 1] - q[1], dz = g->pts[3 * k + 2] - q[2];
                         double d = dx * dx + dy * dy + dz * dz;
-                        if (d < best) { best = d; bi = k; }
+                        if (d < best || (bi >= 0 && d == best && g->orig[k] < g->orig[bi])) { best = d; bi = k; }
                     }
                 }
             }

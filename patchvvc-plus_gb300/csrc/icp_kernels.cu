@@ -5,10 +5,12 @@
 // ICPBase::CloudMSE (src/registration/registration_base.cc:114-158).
 //
 //   k_grid   one CTA per pair: a uniform grid over the target points
-//            (at most 4096 cubic cells, spread over the box's shape):
+//            (cubic cells of at least one voxel, spread over the box's
+//            shape, about kmul cells per point and at most 16384):
 //            bounding box by block reduction,
 //            counting sort of the points into cells (shared-memory
-//            histogram + block scan), written to the workspace.
+//            histogram + block scan), written to the workspace as float4
+//            (x, y, z, index of the point in its pair).
 //   k_icp    one CTA per pair, all iterations: each thread transforms its
 //            source points, finds the exact nearest target point by rings of
 //            grid cells (FP32), and accumulates the correspondence sums with
@@ -27,8 +29,24 @@
 
 namespace pvvc {
 
-constexpr int kGridAxis = 16;
-constexpr int kCells = kGridAxis * kGridAxis * kGridAxis;
+// Cell budget of a grid over n points: kmul * n cells, at least 64 and at
+// most kMaxCells.  A pair's cell-start array (budget + 1 ints) begins at
+// kmul * (first point of the pair) + 65 * pair, so the regions of all pairs
+// follow from the point offsets alone and never overlap.
+constexpr int kMaxCells = 16384;
+constexpr int kGridSmem = 4 * (kMaxCells + 1);
+constexpr int kIcpCellMul = 2;      // cells per target point, pvvc_icp_batch / pvvc_cloud_mse_batch
+constexpr int kNoAllocCellMul = 2;  // cells per target point, pvvc_icp_batch_noalloc
+__host__ __device__ __forceinline__ int cell_budget(int kmul, uint32_t n) {
+    const long long c = (long long)kmul * n;
+    return (int)(c < 64 ? 64 : (c > kMaxCells ? kMaxCells : c));
+}
+__host__ __device__ __forceinline__ uint64_t cell_base(int kmul, uint32_t first, int pair) {
+    return (uint64_t)kmul * first + 65ull * (uint64_t)pair;
+}
+__host__ __device__ constexpr uint64_t cell_ints(int kmul, uint64_t npoints, int32_t npairs) {
+    return (uint64_t)kmul * npoints + 65ull * (uint64_t)npairs;
+}
 
 struct GridHdr {  // per pair
     float lo[3];
@@ -41,13 +59,14 @@ struct GridHdr {  // per pair
 template <int T>
 __global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const uint32_t* __restrict__ off,
                                             const float* __restrict__ xform, GridHdr* __restrict__ hdr,
-                                            int* __restrict__ cstart, float* __restrict__ sorted) {
-    __shared__ int s_cnt[kCells + 1];
+                                            int* __restrict__ cstart, float4* __restrict__ sorted, int kmul) {
+    extern __shared__ int s_cnt[];  // kGridSmem bytes: budget + 1 counters
     __shared__ float s_red[T / 32][6];
     __shared__ float s_box[6];
     __shared__ int s_warp[T / 32];
     const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t a = off[pair], b = off[pair + 1], n = b - a;
+    const int C = cell_budget(kmul, n);
     float M[12];
     const bool tr = xform != nullptr;
     if (tr)
@@ -80,7 +99,7 @@ __global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const
             s_red[wid][k] = mn[k];
             s_red[wid][3 + k] = mx[k];
         }
-    for (int c = tid; c <= kCells; c += T) s_cnt[c] = 0;
+    for (int c = tid; c <= C; c += T) s_cnt[c] = 0;
     __syncthreads();
     if (tid == 0) {
         for (int w = 1; w < T / 32; ++w)
@@ -88,7 +107,7 @@ __global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const
                 s_red[0][k] = fminf(s_red[0][k], s_red[w][k]);
                 s_red[0][3 + k] = fmaxf(s_red[0][3 + k], s_red[w][3 + k]);
             }
-        // Cells spread over the box's own shape: edge h with about kCells
+        // Cells spread over the box's own shape: edge h with about C
         // cells in the box (an elongated patch gets more cells along its long
         // axis), grown until the cell count fits; at least one voxel.
         float e[3], ext = 0.f;
@@ -100,19 +119,26 @@ __global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const
         {
             const float fl = fmaxf(ext / 1024.f, 1e-3f);  // floor for flat axes
             const float vol = fmaxf(e[0], fl) * fmaxf(e[1], fl) * fmaxf(e[2], fl);
-            float h = fmaxf(cbrtf(vol / (float)kCells), 1.0f);
+            float h = fmaxf(cbrtf(vol / (float)C), 1.0f);
             for (int guard = 0; guard < 200; ++guard) {
                 long long cells = 1;
                 for (int k = 0; k < 3; ++k) cells *= min((long long)floorf(e[k] / h) + 1, 1023ll);
-                if (cells <= kCells) break;
+                if (cells <= C) break;
                 h *= 1.05f;
             }
             g.h = h;
         }
+        long long cells = 1;
         for (int k = 0; k < 3; ++k) {
             g.lo[k] = n ? s_red[0][k] : 0.f;
             g.dim[k] = n ? min((int)floorf(e[k] / g.h) + 1, 1023) : 1;
+            cells *= g.dim[k];
             s_box[k] = g.lo[k];
+        }
+        // non-finite or absurd extents: one cell holding every point
+        if (!(g.h < FLT_MAX) || g.dim[0] < 1 || g.dim[1] < 1 || g.dim[2] < 1 || cells > C) {
+            g.h = FLT_MAX;
+            g.dim[0] = g.dim[1] = g.dim[2] = 1;
         }
         s_box[3] = g.h;
         s_box[4] = __int_as_float(g.dim[0]);
@@ -135,12 +161,12 @@ __global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const
         atomicAdd(&s_cnt[cell_of(p) + 1], 1);
     }
     __syncthreads();
-    // exclusive scan of kCells+1 counters (serial per warp chunk, then warp offsets)
-    const int per = (kCells + 1 + T - 1) / T;
+    // exclusive scan of C+1 counters (serial per warp chunk, then warp offsets)
+    const int per = (C + 1 + T - 1) / T;
     int loc = 0;
     for (int k = 0; k < per; ++k) {
         const int c = tid * per + k;
-        if (c <= kCells) loc += s_cnt[c];
+        if (c <= C) loc += s_cnt[c];
     }
     int x = loc;
     for (int o = 1; o < 32; o <<= 1) {
@@ -155,41 +181,41 @@ __global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const
     int run = (wid ? s_warp[wid - 1] : 0) + x - loc;
     for (int k = 0; k < per; ++k) {
         const int c = tid * per + k;
-        if (c <= kCells) {
+        if (c <= C) {
             run += s_cnt[c];
             s_cnt[c] = run;  // inclusive prefix of counts[0..c] == start of cell c (counts shifted by one)
         }
     }
     __syncthreads();
-    int* cs = cstart + (size_t)pair * (kCells + 1);
-    for (int c = tid; c <= kCells; c += T) cs[c] = s_cnt[c];
+    int* cs = cstart + cell_base(kmul, a, pair);
+    for (int c = tid; c <= C; c += T) cs[c] = s_cnt[c];
     __syncthreads();
     for (uint32_t i = a + tid; i < b; i += T) {
         float p[3];
         load(i, p);
         const int slot = atomicAdd(&s_cnt[cell_of(p)], 1);
-        float* d = sorted + 3ull * (a + slot);
-        d[0] = p[0];
-        d[1] = p[1];
-        d[2] = p[2];
+        sorted[a + slot] = make_float4(p[0], p[1], p[2], __int_as_float((int)(i - a)));
     }
 }
 
 // exact nearest neighbour: squared distance (and the point) of the closest
 // gridded point to q, searching rings of cells around q's cell clamped into
-// the grid; a point in ring r lies at least (r-1)*h from q
-__device__ __forceinline__ float grid_nn(const GridHdr& g, const int* __restrict__ cs, const float* __restrict__ sp, uint32_t base,
+// the grid; a point in ring r lies at least (r-1)*h from q.  Among points at
+// the same distance the one first in the input wins, so the answer does not
+// depend on the grid's cell size or on the order the cells are visited in.
+__device__ __forceinline__ float grid_nn(const GridHdr& g, const int* __restrict__ cs, const float4* __restrict__ sp, uint32_t base,
                                          float qx, float qy, float qz, float* nx, float* ny, float* nz) {
     const int cx = min(max((int)floorf((qx - g.lo[0]) / g.h), 0), g.dim[0] - 1);
     const int cy = min(max((int)floorf((qy - g.lo[1]) / g.h), 0), g.dim[1] - 1);
     const int cz = min(max((int)floorf((qz - g.lo[2]) / g.h), 0), g.dim[2] - 1);
     float best = FLT_MAX;
     float bx = 0.f, by = 0.f, bz = 0.f;
+    int bi = 0x7fffffff;
     const int maxr = max(g.dim[0], max(g.dim[1], g.dim[2]));
     for (int r = 0; r <= maxr; ++r) {
         if (r > 0 && best < FLT_MAX) {
             const float lb = (float)(r - 1) * g.h;
-            if (lb * lb > best) break;
+            if (lb * lb * 0.999f > best) break;
         }
         for (int z = max(cz - r, 0); z <= min(cz + r, g.dim[2] - 1); ++z) {
             const bool zr = (z == cz - r) || (z == cz + r);
@@ -217,15 +243,16 @@ __device__ __forceinline__ float grid_nn(const GridHdr& g, const int* __restrict
                     const int c = (z * g.dim[1] + y) * g.dim[0] + x;
                     const int e = __ldg(cs + c + 1);
                     for (int k = __ldg(cs + c); k < e; ++k) {
-                        const float* p = sp + 3ull * (base + k);
-                        const float px = __ldg(p), py = __ldg(p + 1), pz = __ldg(p + 2);
-                        const float dx = px - qx, dy = py - qy, dz = pz - qz;
+                        const float4 p = __ldg(sp + base + k);
+                        const float dx = p.x - qx, dy = p.y - qy, dz = p.z - qz;
                         const float d = dx * dx + dy * dy + dz * dz;
-                        if (d < best) {
+                        const int pi = __float_as_int(p.w);
+                        if (d < best || (d == best && pi < bi)) {
                             best = d;
-                            bx = px;
-                            by = py;
-                            bz = pz;
+                            bi = pi;
+                            bx = p.x;
+                            by = p.y;
+                            bz = p.z;
                         }
                     }
                 }
@@ -325,8 +352,8 @@ constexpr int kNSum = 17;  // count, sum p (3), sum q (3), sum p q^T (9), sum d^
 
 __global__ void __launch_bounds__(kIcpThreads) k_icp(const float* __restrict__ src, const uint32_t* __restrict__ soff,
                                                      const uint32_t* __restrict__ toff, const GridHdr* __restrict__ hdr,
-                                                     const int* __restrict__ cstart, const float* __restrict__ tsorted,
-                                                     const float* __restrict__ init, pvvc_icp_params prm,
+                                                     const int* __restrict__ cstart, const float4* __restrict__ tsorted,
+                                                     int kmul, const float* __restrict__ init, pvvc_icp_params prm,
                                                      float* __restrict__ T_out, float* __restrict__ mse_out,
                                                      int32_t* __restrict__ iters_out, uint8_t* __restrict__ conv_out) {
     __shared__ double s_part[kIcpThreads / 32][kNSum];
@@ -337,8 +364,8 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp(const float* __restrict__ s
     const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t a = soff[pair], b = soff[pair + 1];
     const GridHdr g = hdr[pair];
-    const int* cs = cstart + (size_t)pair * (kCells + 1);
     const uint32_t tb = toff[pair];
+    const int* cs = cstart + cell_base(kmul, tb, pair);
     const bool empty_t = toff[pair + 1] == tb;
     if (tid == 0) {
         for (int i = 0; i < 16; ++i) s_T[i] = init ? (double)init[pair * 16 + i] : ((i % 5 == 0) ? 1.0 : 0.0);
@@ -457,13 +484,13 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp(const float* __restrict__ s
 __global__ void __launch_bounds__(kIcpThreads) k_nn_mean(const float* __restrict__ q, const uint32_t* __restrict__ qoff,
                                                          const float* __restrict__ xform, const uint32_t* __restrict__ goff,
                                                          const GridHdr* __restrict__ hdr, const int* __restrict__ cstart,
-                                                         const float* __restrict__ sorted, float* __restrict__ out) {
+                                                         const float4* __restrict__ sorted, int kmul, float* __restrict__ out) {
     __shared__ double s_part[kIcpThreads / 32];
     const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t a = qoff[pair], b = qoff[pair + 1];
     const GridHdr g = hdr[pair];
-    const int* cs = cstart + (size_t)pair * (kCells + 1);
     const uint32_t gb = goff[pair];
+    const int* cs = cstart + cell_base(kmul, gb, pair);
     const bool empty = goff[pair + 1] == gb;
     float M[12];
     for (int i = 0; i < 12; ++i) M[i] = xform ? xform[pair * 16 + i] : ((i % 5 == 0) ? 1.f : 0.f);
@@ -496,12 +523,13 @@ constexpr int32_t kNoAllocMaxPairs = 512;
 constexpr uint64_t kNoAllocMaxTgtPoints = 1ull << 20;  // 1,048,576 target points
 constexpr uint64_t kNoAllocHdrOff = 0;
 constexpr uint64_t kNoAllocCellOff = (sizeof(GridHdr) * kNoAllocMaxPairs + 255) / 256 * 256;
-constexpr uint64_t kNoAllocSortedOff = kNoAllocCellOff + (4ull * (kCells + 1) * kNoAllocMaxPairs + 255) / 256 * 256;
-constexpr uint64_t kNoAllocBytes = kNoAllocSortedOff + (12ull * kNoAllocMaxTgtPoints + 255) / 256 * 256;  // ~21 MB
+constexpr uint64_t kNoAllocSortedOff =
+    kNoAllocCellOff + (4ull * cell_ints(kNoAllocCellMul, kNoAllocMaxTgtPoints, kNoAllocMaxPairs) + 255) / 256 * 256;
+constexpr uint64_t kNoAllocBytes = kNoAllocSortedOff + (16ull * kNoAllocMaxTgtPoints + 255) / 256 * 256;  // ~25 MB
 }  // namespace
 }  // namespace pvvc
 
-// Every GPU that loads this library holds this array (~21 MB) until the
+// Every GPU that loads this library holds this array (~25 MB) until the
 // process exits.  All calls share it and it keeps the last call's contents;
 // the grid build overwrites every byte a call reads, so nothing needs
 // clearing between calls.  Host code must not use the name as a pointer:
@@ -512,7 +540,22 @@ namespace pvvc {
 namespace {
 std::mutex g_noalloc_mu;
 void* g_noalloc_addr[128] = {};  // device address of the array, per device ordinal
+bool g_grid_attr[128] = {};      // k_grid's shared-memory opt-in done, per device ordinal
 }  // namespace
+
+// k_grid's histogram takes kGridSmem (64 KB) of dynamic shared memory, above
+// the 48 KB default: opt in once per device (the caller's current device).
+bool grid_attr_ready() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return false;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_grid_attr[dev]) {
+        if (cudaFuncSetAttribute(k_grid<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGridSmem) != cudaSuccess)
+            return false;
+        g_grid_attr[dev] = true;
+    }
+    return true;
+}
 
 __global__ void k_max2(const float* __restrict__ a, int n, float* __restrict__ o) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -528,10 +571,10 @@ inline uint64_t al(uint64_t v) { return (v + 255) / 256 * 256; }
 struct IcpWs {
     GridHdr* hdr;
     int* cstart;
-    float* sorted;
+    float4* sorted;
     GridHdr* hdr2;
     int* cstart2;
-    float* sorted2;
+    float4* sorted2;
     float* tmp;
 };
 uint64_t ws_bytes(int32_t npairs, uint64_t nsrc, uint64_t ntgt, IcpWs* w, void* base) {
@@ -541,17 +584,19 @@ uint64_t ws_bytes(int32_t npairs, uint64_t nsrc, uint64_t ntgt, IcpWs* w, void* 
         o = al(o + b);
         return r;
     };
-    const uint64_t h = take(sizeof(GridHdr) * npairs), c = take(4ull * (kCells + 1) * npairs), s = take(12ull * ntgt);
-    const uint64_t h2 = take(sizeof(GridHdr) * npairs), c2 = take(4ull * (kCells + 1) * npairs), s2 = take(12ull * nsrc);
+    const uint64_t h = take(sizeof(GridHdr) * npairs), c = take(4ull * cell_ints(kIcpCellMul, ntgt, npairs)),
+                   s = take(16ull * ntgt);
+    const uint64_t h2 = take(sizeof(GridHdr) * npairs), c2 = take(4ull * cell_ints(kIcpCellMul, nsrc, npairs)),
+                   s2 = take(16ull * nsrc);
     const uint64_t t = take(8ull * npairs);
     if (w && base) {
         uint8_t* p = static_cast<uint8_t*>(base);
         w->hdr = reinterpret_cast<GridHdr*>(p + h);
         w->cstart = reinterpret_cast<int*>(p + c);
-        w->sorted = reinterpret_cast<float*>(p + s);
+        w->sorted = reinterpret_cast<float4*>(p + s);
         w->hdr2 = reinterpret_cast<GridHdr*>(p + h2);
         w->cstart2 = reinterpret_cast<int*>(p + c2);
-        w->sorted2 = reinterpret_cast<float*>(p + s2);
+        w->sorted2 = reinterpret_cast<float4*>(p + s2);
         w->tmp = reinterpret_cast<float*>(p + t);
     }
     return o;
@@ -574,8 +619,10 @@ extern "C" int pvvc_icp_batch(int32_t npairs, const float* src_xyz, const uint32
     IcpWs w;
     if (ws_bytes(npairs, total_src_points, total_tgt_points, &w, workspace) > workspace_bytes) return PVVC_ERR_CAPACITY;
     cudaStream_t s = (cudaStream_t)stream;
-    k_grid<256><<<npairs, 256, 0, s>>>(tgt_xyz, tgt_off, nullptr, w.hdr, w.cstart, w.sorted);
-    k_icp<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, tgt_off, w.hdr, w.cstart, w.sorted, init, *params, T_out, mse_out,
+    if (!grid_attr_ready()) return PVVC_ERR_CUDA;
+    k_grid<256><<<npairs, 256, kGridSmem, s>>>(tgt_xyz, tgt_off, nullptr, w.hdr, w.cstart, w.sorted, kIcpCellMul);
+    k_icp<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, tgt_off, w.hdr, w.cstart, w.sorted, kIcpCellMul, init, *params,
+                                         T_out, mse_out,
                                          iters_out, converged_out);
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }
@@ -591,10 +638,11 @@ extern "C" int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const 
     if (ws_bytes(npairs, total_src_points, total_tgt_points, &w, workspace) > workspace_bytes) return PVVC_ERR_CAPACITY;
     cudaStream_t s = (cudaStream_t)stream;
     // transformed source -> target, and target -> transformed source; max of both
-    k_grid<256><<<npairs, 256, 0, s>>>(tgt_xyz, tgt_off, nullptr, w.hdr, w.cstart, w.sorted);
-    k_grid<256><<<npairs, 256, 0, s>>>(src_xyz, src_off, T, w.hdr2, w.cstart2, w.sorted2);
-    k_nn_mean<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, T, tgt_off, w.hdr, w.cstart, w.sorted, w.tmp);
-    k_nn_mean<<<npairs, kIcpThreads, 0, s>>>(tgt_xyz, tgt_off, nullptr, src_off, w.hdr2, w.cstart2, w.sorted2,
+    if (!grid_attr_ready()) return PVVC_ERR_CUDA;
+    k_grid<256><<<npairs, 256, kGridSmem, s>>>(tgt_xyz, tgt_off, nullptr, w.hdr, w.cstart, w.sorted, kIcpCellMul);
+    k_grid<256><<<npairs, 256, kGridSmem, s>>>(src_xyz, src_off, T, w.hdr2, w.cstart2, w.sorted2, kIcpCellMul);
+    k_nn_mean<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, T, tgt_off, w.hdr, w.cstart, w.sorted, kIcpCellMul, w.tmp);
+    k_nn_mean<<<npairs, kIcpThreads, 0, s>>>(tgt_xyz, tgt_off, nullptr, src_off, w.hdr2, w.cstart2, w.sorted2, kIcpCellMul,
                                              w.tmp + npairs);
     k_max2<<<(npairs + 255) / 256, 256, 0, s>>>(w.tmp, npairs, mse_out);
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
@@ -626,10 +674,12 @@ extern "C" int pvvc_icp_batch_noalloc(int32_t npairs, const float* src_xyz, cons
     uint8_t* b = static_cast<uint8_t*>(base);
     GridHdr* hdr = reinterpret_cast<GridHdr*>(b + kNoAllocHdrOff);
     int* cstart = reinterpret_cast<int*>(b + kNoAllocCellOff);
-    float* sorted = reinterpret_cast<float*>(b + kNoAllocSortedOff);
+    float4* sorted = reinterpret_cast<float4*>(b + kNoAllocSortedOff);
     cudaStream_t s = (cudaStream_t)stream;
-    k_grid<256><<<npairs, 256, 0, s>>>(tgt_xyz, tgt_off, nullptr, hdr, cstart, sorted);
-    k_icp<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, tgt_off, hdr, cstart, sorted, init, *params, T_out, mse_out,
+    if (!grid_attr_ready()) return PVVC_ERR_CUDA;
+    k_grid<256><<<npairs, 256, kGridSmem, s>>>(tgt_xyz, tgt_off, nullptr, hdr, cstart, sorted, kNoAllocCellMul);
+    k_icp<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, tgt_off, hdr, cstart, sorted, kNoAllocCellMul, init, *params, T_out,
+                                         mse_out,
                                          iters_out, converged_out);
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }
