@@ -113,6 +113,7 @@ typedef struct {
     int32_t kernels;              /* kernel launches per decode                    */
     int32_t group_ctas;           /* grid of the grouped inverse-RAHT kernel        */
     pvvc_tune tune;               /* the shapes in force (defaults resolved)         */
+    uint64_t clear_bytes;         /* coefficient bytes zeroed by memset nodes per decode */
 } pvvc_plan_info;
 int pvvc_plan_info_get(const pvvc_plan* plan, pvvc_plan_info* info);
 

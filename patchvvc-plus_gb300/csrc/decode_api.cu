@@ -485,6 +485,7 @@ extern "C" int pvvc_plan_info_get(const pvvc_plan* p, pvvc_plan_info* info) {
     info->singles_b = p->nlist_b;
     info->group_ctas = p->grp_ctas;
     info->tune = p->tune;
+    info->clear_bytes = 4ull * p->coef_floats;
     if (p->nslices > 0)
         info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) + (p->nmid > 0) +
                         (p->nlong > 0 ? (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +

@@ -176,35 +176,32 @@ __global__ void __launch_bounds__(32 * kEncWarps) k_fwd_raht(const SliceWork* __
 }
 
 // RLGREncoder: MSB-first bit writer over a 64-bit accumulator with the
-// reference's '+' (a value wider than its field carries into the bits before
-// it), bytes gathered into big-endian 32-bit words stored in order.
+// reference's '+' (a value wider than its field would carry into the pending
+// bits before it; every caller here passes v < 2^bits, since the symbols are
+// int32), emitted as big-endian 32-bit words in order.
 struct BitSink {
-    uint32_t* out;     // 4-byte aligned region
-    uint32_t cap;      // bytes
-    uint32_t nbytes = 0;
-    uint64_t acc = 0;
-    int n = 0;         // pending bits (< 8 between calls)
-    uint32_t word = 0;
+    uint32_t* out;       // 4-byte aligned region
+    uint32_t cap;        // bytes
+    uint32_t nwords = 0; // whole 32-bit words emitted
+    uint32_t nbytes = 0; // set by finish()
+    uint64_t acc = 0;    // pending bits in the low n bits
+    int n = 0;           // < 32 between calls
     bool overflow = false;
-    __device__ __forceinline__ void byte(uint32_t b) {
-        word = (word << 8) | (b & 0xFFu);
-        if ((++nbytes & 3u) == 0) {
-            if (nbytes <= cap) out[(nbytes >> 2) - 1] = __byte_perm(word, 0, 0x0123);
-            else overflow = true;
-            word = 0;
-        }
+    __device__ __forceinline__ void emit(uint32_t w) {
+        if (++nwords * 4u <= cap) out[nwords - 1] = __byte_perm(w, 0, 0x0123);
+        else overflow = true;
     }
     __device__ __forceinline__ void put(uint64_t v, int bits) {
-        if (bits > 56) {
+        if (bits > 32) {
             put(v >> 32, bits - 32);
             put(v & 0xFFFFFFFFull, 32);
             return;
         }
         acc = (acc << bits) + v;
         n += bits;
-        while (n >= 8) {
-            n -= 8;
-            byte((uint32_t)(acc >> n));
+        if (n >= 32) {
+            n -= 32;
+            emit((uint32_t)(acc >> n));
         }
     }
     __device__ __forceinline__ void gr(uint64_t x, int k) {  // GRWrite
@@ -217,12 +214,11 @@ struct BitSink {
             put(x, 32);
         }
     }
-    __device__ __forceinline__ void finish() {
-        if (n) put(0, 8 - n);  // byte padding
-        const uint32_t tail = nbytes & 3u;
-        if (tail) {
-            const uint32_t wv = word << (8 * (4 - tail));
-            if (nbytes <= cap) out[nbytes >> 2] = __byte_perm(wv, 0, 0x0123);
+    __device__ __forceinline__ void finish() {  // zero bits up to the byte boundary
+        nbytes = nwords * 4u + (uint32_t)((n + 7) >> 3);
+        if (n) {
+            const uint32_t w = (uint32_t)(acc << (32 - n));
+            if (nbytes <= cap) out[nwords] = __byte_perm(w, 0, 0x0123);
             else overflow = true;
         }
     }
@@ -248,8 +244,7 @@ __global__ void k_rlgr_enc(const SliceWork* __restrict__ work, const int32_t* __
     BitSink bw{reinterpret_cast<uint32_t*>(out + out_off[w.orig]), out_cap[w.orig]};
     uint64_t u = 0, kP = 0, kRP = 2 * kL, m = 0, k = 0;
     const uint64_t total = 3ull * N;
-    for (uint64_t i = 0; i < total && !bw.overflow; ++i) {
-        const int64_t x = s[i * cs];
+    auto encode = [&](int64_t x) {
         u = x < 0 ? ((uint64_t)(-x) << 1) - 1 : (uint64_t)x << 1;  // Sign2Unsign
         k = kP / kL;
         const uint64_t kR = kRP / kL;
@@ -275,6 +270,25 @@ __global__ void k_rlgr_enc(const SliceWork* __restrict__ work, const int32_t* __
             kP = u ? (kP < kD0 ? 0 : kP - kD0) : kP + kU0;
             m = 0;
         }
+    };
+    // The symbols of a slice sit coef_stride apart (frame-interleaved planes),
+    // one sector each: they are loaded kPf at a time, the next batch in flight
+    // while this one is encoded, so the chain does not wait on every load.
+    constexpr int kPf = 16;
+    int32_t cur[kPf], nxt[kPf];
+#pragma unroll
+    for (int j = 0; j < kPf; ++j) nxt[j] = (uint64_t)j < total ? s[(uint64_t)j * cs] : 0;
+    for (uint64_t b0 = 0; b0 < total && !bw.overflow; b0 += kPf) {
+#pragma unroll
+        for (int j = 0; j < kPf; ++j) cur[j] = nxt[j];
+        if (b0 + kPf < total) {
+#pragma unroll
+            for (int j = 0; j < kPf; ++j) nxt[j] = b0 + kPf + j < total ? s[(b0 + kPf + j) * cs] : 0;
+        }
+        const int cnt = total - b0 < (uint64_t)kPf ? (int)(total - b0) : kPf;
+#pragma unroll
+        for (int j = 0; j < kPf; ++j)
+            if (j < cnt) encode(cur[j]);
     }
     if (total > 0 && k && !u) {  // trailing run (entropy_codec.cc:144-147)
         bw.put(0, 1);

@@ -272,49 +272,107 @@ __device__ __forceinline__ float pooled_grad(const float* dh0, const __nv_bfloat
 }
 
 // dW3[n, :] = sum over clouds of g(c, n) X2[argmax(c, n), :];  db3[n] = sum g.
-// One channel per block, one input feature per thread.
+// One channel per block, one input feature per thread.  Clouds go in chunks:
+// the chunk's gradients and argmax rows are staged in shared memory by
+// independent loads, then the X2 rows are gathered kGather at a time, so the
+// loads overlap; the sums still run over the clouds in order.
+constexpr int kPoolChunk = 1024;
+constexpr int kGather = 8;
 __global__ void __launch_bounds__(kD2) k_pool_bwd_w3(int nclouds, const float* __restrict__ dh0,
                                                     const __nv_bfloat16* __restrict__ h0, const int32_t* __restrict__ amax,
                                                     const __nv_bfloat16* __restrict__ x2, float* __restrict__ gw3,
                                                     float* __restrict__ gb3) {
+    __shared__ float s_g[kPoolChunk];
+    __shared__ int32_t s_row[kPoolChunk];  // argmax row within the cloud
     const int n = blockIdx.x, k = threadIdx.x;
     float acc = 0.f, accb = 0.f;
-    for (int c = 0; c < nclouds; ++c) {
-        const float g = pooled_grad(dh0, h0, c, n);
-        if (g == 0.f) continue;
-        const int64_t row = (int64_t)c * kP + amax[c * kD3 + n];
-        acc += g * __bfloat162float(x2[row * kD2 + k]);
-        accb += g;
+    for (int c0 = 0; c0 < nclouds; c0 += kPoolChunk) {
+        const int cn = min(kPoolChunk, nclouds - c0);
+        __syncthreads();
+        for (int i = k; i < cn; i += kD2) {
+            s_g[i] = pooled_grad(dh0, h0, c0 + i, n);
+            s_row[i] = amax[(c0 + i) * kD3 + n];
+        }
+        __syncthreads();
+        for (int i0 = 0; i0 < cn; i0 += kGather) {
+            float xv[kGather];
+#pragma unroll
+            for (int j = 0; j < kGather; ++j) {
+                const int i = min(i0 + j, cn - 1);
+                xv[j] = __bfloat162float(x2[((int64_t)(c0 + i) * kP + s_row[i]) * kD2 + k]);
+            }
+#pragma unroll
+            for (int j = 0; j < kGather; ++j) {
+                const int i = i0 + j;
+                if (i < cn) {
+                    const float g = s_g[i];
+                    if (g != 0.f) {
+                        acc += g * xv[j];
+                        accb += g;
+                    }
+                }
+            }
+        }
     }
     gw3[n * kD2 + k] += acc;
     if (k == 0) gb3[n] += accb;
 }
 
 // dY2 = (sum over channels n of g(c, n) W3[n, :] scattered to row argmax(c, n))
-//       masked by X2 > 0, as dense bf16 rows.  One cloud per block.
+//       masked by X2 > 0, as dense bf16 rows.  One cloud per block.  The
+// channels with a gradient are bucketed by their argmax row (a stable
+// counting sort: channel order kept within a row); then each row's 128
+// outputs are summed over its bucket in channel order and written at once,
+// zero rows included.
 __global__ void __launch_bounds__(256) k_pool_bwd_x2(const float* __restrict__ dh0, const __nv_bfloat16* __restrict__ h0,
                                                     const int32_t* __restrict__ amax, const __nv_bfloat16* __restrict__ w3,
                                                     const __nv_bfloat16* __restrict__ x2, __nv_bfloat16* __restrict__ dy2) {
-    extern __shared__ float acc[];  // [kP][kD2]
-    const int c = blockIdx.x;
-    for (int i = threadIdx.x; i < kP * kD2; i += blockDim.x) acc[i] = 0.f;
+    static_assert(kD3 == 256 && kP == 256 && kD2 == 128, "one thread per channel and per row, two rows per pass");
+    __shared__ float s_g[kD3];
+    __shared__ int32_t s_row[kD3];
+    __shared__ int32_t s_start[kP + 1];  // bucket of row r: s_list[s_start[r] .. s_start[r + 1])
+    __shared__ int32_t s_list[kD3];
+    const int c = blockIdx.x, t = threadIdx.x;
+    const float g = pooled_grad(dh0, h0, c, t);
+    const int r = amax[c * kD3 + t];
+    s_g[t] = g;
+    s_row[t] = g != 0.f ? r : -1;
     __syncthreads();
-    const int k = threadIdx.x & (kD2 - 1), half = threadIdx.x >> 7;  // two channels at a time
-    for (int n0 = 0; n0 < kD3; n0 += 2) {
-        const int n = n0 + half;
-        const float g = pooled_grad(dh0, h0, c, n);
-        const int r = amax[c * kD3 + n];
-        // both halves may hit the same row: take turns
-        for (int turn = 0; turn < 2; ++turn) {
-            if (turn == half && g != 0.f) acc[r * kD2 + k] += g * __bfloat162float(w3[n * kD2 + k]);
-            __syncthreads();
-        }
+    // count of row t (thread t), then an exclusive scan over the 256 rows
+    int cnt = 0;
+    for (int n = 0; n < kD3; ++n) cnt += s_row[n] == t;
+    int x = cnt;
+    const int lane = t & 31, wid = t >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
+    __shared__ int32_t s_warp[8];
+    if (lane == 31) s_warp[wid] = x;
+    __syncthreads();
+    int before = 0;
+    for (int w = 0; w < wid; ++w) before += s_warp[w];
+    s_start[t] = before + x - cnt;
+    if (t == kP - 1) s_start[kP] = before + x;
+    __syncthreads();
+    // channel t goes after the channels below it with the same row
+    if (s_row[t] >= 0) {
+        int rank = 0;
+        for (int n = 0; n < t; ++n) rank += s_row[n] == s_row[t];
+        s_list[s_start[s_row[t]] + rank] = t;
+    }
+    __syncthreads();
+    const int k = t & (kD2 - 1), half = t >> 7;
     const int64_t base = (int64_t)c * kP;
-    for (int i = threadIdx.x; i < kP * kD2; i += blockDim.x) {
-        const int r = i / kD2, kk = i % kD2;
-        const int64_t idx = (base + r) * kD2 + kk;
-        dy2[idx] = __float2bfloat16_rn(__bfloat162float(x2[idx]) > 0.f ? acc[i] : 0.f);
+    for (int r0 = 0; r0 < kP; r0 += 2) {
+        const int row = r0 + half;
+        float acc = 0.f;
+        for (int j = s_start[row]; j < s_start[row + 1]; ++j) {
+            const int n = s_list[j];
+            acc += s_g[n] * __bfloat162float(w3[n * kD2 + k]);
+        }
+        const int64_t idx = (base + row) * kD2 + k;
+        dy2[idx] = __float2bfloat16_rn(__bfloat162float(x2[idx]) > 0.f ? acc : 0.f);
     }
 }
 
@@ -528,7 +586,7 @@ int backward(pvvc_regnet* n, int64_t B, cudaStream_t s) {
     // max-pool + layer 3 (sparse): dW3, db3, dY2
     k_pool_bwd_w3<<<kD3, kD2, 0, s>>>((int)(2 * B), F32(dh0), BF(h0), static_cast<int32_t*>(n->amax.p), BF(x2), g + kL.w3,
                                       g + kL.b3);
-    k_pool_bwd_x2<<<(unsigned)(2 * B), 256, kP * kD2 * sizeof(float), s>>>(F32(dh0), BF(h0), static_cast<int32_t*>(n->amax.p),
+    k_pool_bwd_x2<<<(unsigned)(2 * B), 256, 0, s>>>(F32(dh0), BF(h0), static_cast<int32_t*>(n->amax.p),
                                                                             BF(w3b), BF(x2), BF(dy2));
     // layer 2: dW2, db2, dY1
     if ((rc = weight_grad(M, kD2, kD1, BF(dy2), BF(x1), BF(ta), BF(tb), g + kL.w2, s))) return rc;
@@ -541,15 +599,6 @@ int backward(pvvc_regnet* n, int64_t B, cudaStream_t s) {
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }
 
-int prepare_attrs() {
-    static bool done = false;
-    if (done) return PVVC_OK;
-    if (cudaFuncSetAttribute(k_pool_bwd_x2, cudaFuncAttributeMaxDynamicSharedMemorySize, kP * kD2 * (int)sizeof(float)) !=
-        cudaSuccess)
-        return PVVC_ERR_CUDA;
-    done = true;
-    return PVVC_OK;
-}
 }  // namespace
 
 extern "C" int pvvc_regnet_param_count(void) { return (int)kL.total; }
@@ -557,7 +606,6 @@ extern "C" int pvvc_regnet_param_count(void) { return (int)kL.total; }
 extern "C" int pvvc_regnet_create(uint64_t seed, pvvc_regnet** out) {
     if (!out) return PVVC_ERR_ARG;
     *out = nullptr;
-    if (prepare_attrs()) return PVVC_ERR_CUDA;
     auto n = std::make_unique<pvvc_regnet>();
     n->nparam = kL.total;
     const size_t bytes = 4ull * kL.total;

@@ -37,7 +37,7 @@ class Tune(C.Structure):
 class PlanInfo(C.Structure):
     _fields_ = [("nslices", C.c_int32), ("nintra", C.c_int32), ("groups_a", C.c_int32), ("groups_b", C.c_int32),
                 ("singles_a", C.c_int32), ("singles_b", C.c_int32), ("kernels", C.c_int32), ("group_ctas", C.c_int32),
-                ("tune", Tune)]
+                ("tune", Tune), ("clear_bytes", C.c_uint64)]
 
 
 class ServerConfig(C.Structure):
