@@ -226,12 +226,33 @@ struct BitSink {
 
 constexpr uint64_t kL = 4, kU0 = 3, kD0 = 1, kU1 = 2, kD1 = 1;
 
-__global__ void k_rlgr_enc(const SliceWork* __restrict__ work, const int32_t* __restrict__ order, int nslices,
+constexpr int kEncRlgrBlock = 128;
+constexpr int kEncPf = 16;  // symbols per prefetch batch
+// The largest slices (first in `order`) are encoded kEncLongLanes to a warp
+// by the first CTAs of the launch, the rest kEncRestLanes to a warp: the
+// encoder's branches diverge between lanes, and a warp of 32 long slices
+// would take their divergent paths one after another.
+constexpr int kEncLongLanes = 2;
+constexpr int kEncLongCtas = 304;
+constexpr int kEncLongSlices = kEncLongCtas * (kEncRlgrBlock / 32) * kEncLongLanes;
+constexpr int kEncRestLanes = 32;
+
+__global__ void __launch_bounds__(kEncRlgrBlock) k_rlgr_enc(const SliceWork* __restrict__ work,
+                                                           const int32_t* __restrict__ order, int nslices, int nlong,
+                                                           int long_ctas,
                            const int32_t* __restrict__ sym, uint8_t* __restrict__ out, const uint64_t* __restrict__ out_off,
                            const uint32_t* __restrict__ out_cap, uint32_t* __restrict__ out_len,
                            int32_t* __restrict__ fstatus) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nslices) return;
+    __shared__ int32_t s_sym[kEncPf][kEncRlgrBlock];  // column threadIdx.x: this thread's batch
+    const int lane = threadIdx.x & 31;
+    int t;
+    if ((int)blockIdx.x < long_ctas) {
+        t = ((int)blockIdx.x * (kEncRlgrBlock / 32) + (int)(threadIdx.x >> 5)) * kEncLongLanes + lane;
+        if (lane >= kEncLongLanes || t >= nlong) return;
+    } else {
+        t = nlong + (((int)blockIdx.x - long_ctas) * (kEncRlgrBlock / 32) + (int)(threadIdx.x >> 5)) * kEncRestLanes + lane;
+        if (lane >= kEncRestLanes || t >= nslices) return;
+    }
     const int item = order[t];
     const SliceWork& w = work[item];
     if (fstatus[item] != PVVC_OK) {
@@ -272,23 +293,56 @@ __global__ void k_rlgr_enc(const SliceWork* __restrict__ work, const int32_t* __
         }
     };
     // The symbols of a slice sit coef_stride apart (frame-interleaved planes),
-    // one sector each: they are loaded kPf at a time, the next batch in flight
-    // while this one is encoded, so the chain does not wait on every load.
-    constexpr int kPf = 16;
-    int32_t cur[kPf], nxt[kPf];
+    // one sector each: they are loaded kEncPf at a time into registers, the
+    // next batch in flight while this one is encoded from the thread's own
+    // shared-memory column, so the chain does not wait on every load.
+    int32_t nxt[kEncPf];
 #pragma unroll
-    for (int j = 0; j < kPf; ++j) nxt[j] = (uint64_t)j < total ? s[(uint64_t)j * cs] : 0;
-    for (uint64_t b0 = 0; b0 < total && !bw.overflow; b0 += kPf) {
+    for (int j = 0; j < kEncPf; ++j) nxt[j] = (uint64_t)j < total ? s[(uint64_t)j * cs] : 0;
+    for (uint64_t b0 = 0; b0 < total && !bw.overflow; b0 += kEncPf) {
+        uint32_t nz = 0;  // bit j: symbol b0 + j is nonzero
 #pragma unroll
-        for (int j = 0; j < kPf; ++j) cur[j] = nxt[j];
-        if (b0 + kPf < total) {
-#pragma unroll
-            for (int j = 0; j < kPf; ++j) nxt[j] = b0 + kPf + j < total ? s[(b0 + kPf + j) * cs] : 0;
+        for (int j = 0; j < kEncPf; ++j) {
+            s_sym[j][threadIdx.x] = nxt[j];
+            nz |= (uint32_t)(nxt[j] != 0) << j;
         }
-        const int cnt = total - b0 < (uint64_t)kPf ? (int)(total - b0) : kPf;
+        if (b0 + kEncPf < total) {
 #pragma unroll
-        for (int j = 0; j < kPf; ++j)
-            if (j < cnt) encode(cur[j]);
+            for (int j = 0; j < kEncPf; ++j) nxt[j] = b0 + kEncPf + j < total ? s[(b0 + kEncPf + j) * cs] : 0;
+        }
+        const int cnt = total - b0 < (uint64_t)kEncPf ? (int)(total - b0) : kEncPf;
+        int j = 0;
+        while (j < cnt) {
+            const int32_t x = s_sym[j][threadIdx.x];
+            if (x != 0 || kP < kL) {
+                encode(x);
+                ++j;
+                continue;
+            }
+            // Zeros in run mode, taken together: each symbol would add one to
+            // m and, when m reaches 2^k, write a 1 and raise kP by kU1 (k only
+            // grows, so the run stays in run mode).  `k` ends as the value the
+            // last zero saw, as the trailing-run test after the loop expects.
+            const uint32_t rest = nz >> j;
+            int z = rest ? __ffs(rest) - 1 : cnt - j;
+            if (z > cnt - j) z = cnt - j;
+            j += z;
+            uint64_t left = (uint64_t)z;
+            while (left) {
+                k = kP / kL;
+                const uint64_t need = (1ull << k) - m;
+                if (left >= need) {
+                    left -= need;
+                    bw.put(1, 1);
+                    kP += kU1;
+                    m = 0;
+                } else {
+                    m += left;
+                    left = 0;
+                }
+            }
+            u = 0;
+        }
     }
     if (total > 0 && k && !u) {  // trailing run (entropy_codec.cc:144-147)
         bw.put(0, 1);
@@ -373,7 +427,12 @@ extern "C" int pvvc_encode_colors(pvvc_encoder* enc, const pvvc_batch_desc* desc
     k_fwd_raht<<<grid, 32 * kEncWarps, 0, s>>>(dw, static_cast<const GroupDesc*>(p.d_groups.p), ng,
                                                static_cast<const int32_t*>(p.d_idx.p), st->v, leaf_yuv, sym, ts, fs, scr,
                                                p.grp_floats, cnt);
-    k_rlgr_enc<<<(n + 127) / 128, 128, 0, s>>>(dw, static_cast<const int32_t*>(p.d_order.p), n, sym, out,
+    const int nlong = n < kEncLongSlices ? n : kEncLongSlices;
+    const int per_long_cta = (kEncRlgrBlock / 32) * kEncLongLanes;
+    const int long_ctas = (nlong + per_long_cta - 1) / per_long_cta;
+    const int per_rest_cta = (kEncRlgrBlock / 32) * kEncRestLanes;
+    k_rlgr_enc<<<long_ctas + (n - nlong + per_rest_cta - 1) / per_rest_cta, kEncRlgrBlock, 0, s>>>(
+        dw, static_cast<const int32_t*>(p.d_order.p), n, nlong, long_ctas, sym, out,
                                                 static_cast<const uint64_t*>(enc->off.p),
                                                 static_cast<const uint32_t*>(enc->cap.p), out_len, fs);
     k_status_out<<<(n + 255) / 256, 256, 0, s>>>(dw, n, fs, status);
