@@ -279,7 +279,7 @@ int pvvc_icp_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off
  * encoder embedded in a host application that has already reserved the
  * GPU's memory for its own pool, or a per-frame callback where cudaMalloc's
  * implicit device-wide synchronisation would stall work in flight.  The
- * grid scratch lives in one fixed device array of about 21 MB that every GPU
+ * grid scratch lives in one fixed device array of about 25 MB that every GPU
  * loading the library holds until exit.  Limits: npairs <= 512 and
  * total_tgt_points (which must equal tgt_off[npairs]) <= 1,048,576;
  * larger batches return PVVC_ERR_CAPACITY.  The first call on a device looks
