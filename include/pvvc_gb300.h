@@ -183,6 +183,13 @@ int pvvc_graph_destroy(pvvc_graph* graph);
 int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* const* frame_bytes, const uint64_t* frame_len,
                             float* xyz_host, uint8_t* rgb_host, uint64_t cap_points, uint64_t* npoints_out,
                             int32_t* status_host, int32_t status_cap, void* stream);
+/* Wall-clock milliseconds of the stages of the calling thread's last
+ * pvvc_decode_frames_host (no counterpart in the reference):
+ * out[0] parse + inflate, out[1] payload packing and the batch description,
+ * out[2] planning (host) and plan upload, out[3] H2D + decode + D2H up to the
+ * final stream synchronisation.  Fills min(n, 4) values; zeros before any
+ * call. */
+int pvvc_host_stage_times(double* out, int32_t n);
 
 /* ---- reference-signature shim --------------------------------------------
  * Same arguments as launch_cudaProcess (include/cuda/render.cuh:42-57) with

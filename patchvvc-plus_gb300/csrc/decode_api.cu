@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -36,6 +37,56 @@ int resolve_tune(const pvvc_tune* in, pvvc_tune* out) {
     return PVVC_OK;
 }
 
+namespace {
+// Runs fn(i) for i in [0, n) on up to `threads` host threads.
+template <class F>
+void parallel_for(int n, int threads, F fn) {
+    threads = std::max(1, std::min(threads, n));
+    if (threads == 1) {
+        for (int i = 0; i < n; ++i) fn(i);
+        return;
+    }
+    std::atomic<int> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t)
+        pool.emplace_back([&] {
+            for (int i; (i = next.fetch_add(1)) < n;) fn(i);
+        });
+    for (auto& th : pool) th.join();
+}
+
+// Host threads for the planner's and the host call's parallel loops.
+int host_threads() { return (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency())); }
+
+// Stable sort of slice indices by (size descending, slot ascending): an LSD
+// radix sort over four 16-bit digits of ((~size) << 32 | slot), skipping the
+// digits every key shares.  Ties keep their input order, as std::stable_sort
+// with that comparator would.
+void sort_by_size_slot(const uint32_t* size, const int32_t* slot, std::vector<int32_t>& ids) {
+    const size_t n = ids.size();
+    if (n < 2) return;
+    std::vector<uint64_t> key(n), key2(n);
+    std::vector<int32_t> ids2(n);
+    for (size_t i = 0; i < n; ++i) key[i] = ((uint64_t)(~size[ids[i]]) << 32) | (uint32_t)slot[ids[i]];
+    std::vector<uint32_t> cnt(65537);
+    for (int d = 0; d < 4; ++d) {
+        const int sh = 16 * d;
+        std::fill(cnt.begin(), cnt.end(), 0u);
+        for (size_t i = 0; i < n; ++i) ++cnt[((key[i] >> sh) & 0xFFFFu) + 1];
+        if (cnt[((key[0] >> sh) & 0xFFFFu) + 1] == n) continue;  // one bucket: nothing to reorder
+        for (int b = 0; b < 65536; ++b) cnt[b + 1] += cnt[b];
+        for (size_t i = 0; i < n; ++i) {
+            const uint32_t b = (uint32_t)((key[i] >> sh) & 0xFFFFu);
+            const uint32_t at = cnt[b]++;
+            key2[at] = key[i];
+            ids2[at] = ids[i];
+        }
+        key.swap(key2);
+        ids.swap(ids2);
+    }
+}
+}  // namespace
+
 int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload) {
     if (!d || d->nslices < 0) return PVVC_ERR_ARG;
     if (resolve_tune(tune, &p->tune)) return PVVC_ERR_ARG;
@@ -60,19 +111,18 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     }
     // largest first; equal sizes grouped by slot, so that the frames of one
     // patch run next to each other and share its tree tables in L2
-    auto by_size = [&](int32_t a, int32_t b) {
-        if (d->size[a] != d->size[b]) return d->size[a] > d->size[b];
-        if (d->slot[a] != d->slot[b]) return d->slot[a] < d->slot[b];
-        return a < b;
-    };
-    std::stable_sort(intra.begin(), intra.end(), by_size);
-    std::stable_sort(pred.begin(), pred.end(), by_size);
+    sort_by_size_slot(d->size, d->slot, intra);
+    sort_by_size_slot(d->size, d->slot, pred);
     p->nslices = n;
     p->nintra = (int32_t)intra.size();
     p->max_slot = max_slot;
     p->work.resize(n);
     uint64_t coef = 0, fb = 0, pts = 0;
-    auto fill = [&](int q, int i) {
+    // the queue: intra slices, then predictive ones.  The records are filled
+    // in parallel (the descriptor is gathered in sorted order, so most reads
+    // miss the cache); the coefficient regions are laid out further down.
+    auto fill = [&](int q) {
+        const int i = q < (int)intra.size() ? intra[q] : pred[q - intra.size()];
         SliceWork& w = p->work[q];
         std::memset(&w, 0, sizeof(w));
         w.col_off = d->col_off[i];
@@ -86,27 +136,41 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         w.type = d->type[i];
         w.qp = d->qp[i];
         for (int k = 0; k < 12; ++k) w.mv[k] = d->mv[16ull * i + k];
-        w.coef_off = coef;
-        coef += 3ull * w.n;
+    };
+    constexpr int kFillChunk = 4096;
+    if (n < 2 * kFillChunk) {
+        for (int q = 0; q < n; ++q) fill(q);
+    } else {
+        parallel_for((n + kFillChunk - 1) / kFillChunk, host_threads(), [&](int c) {
+            for (int q = c * kFillChunk, e = std::min(n, q + kFillChunk); q < e; ++q) fill(q);
+        });
+    }
+    for (int q = 0; q < n; ++q) {  // fallback-buffer offsets and the output extent, in queue order
+        SliceWork& w = p->work[q];
         if (w.n > (uint32_t)kRahtWcap) {
             w.fb_off = fb;
             fb += 6ull * w.n;
         } else {
             w.fb_off = ~0ull;
         }
-        pts = std::max<uint64_t>(pts, d->out_off[i] + w.n);
-    };
-    int q = 0;
-    for (int i : intra) fill(q++, i);
-    for (int i : pred) fill(q++, i);
+        pts = std::max<uint64_t>(pts, w.out_off + w.n);
+    }
     p->total_points = pts;
-    // RLGR order: all slices by size, so that a warp decodes similar lengths
+    // RLGR order: all slices by size, so that a warp decodes similar lengths.
+    // The queue holds the intra slices, then the predictive ones, each run
+    // already sorted by (size descending, slot): merging the two runs (ties
+    // from the first) is the stable sort of the whole queue by that key.
     p->order.resize(n);
-    std::iota(p->order.begin(), p->order.end(), 0);
-    std::stable_sort(p->order.begin(), p->order.end(), [&](int32_t a, int32_t b) {
-        if (p->work[a].n != p->work[b].n) return p->work[a].n > p->work[b].n;
-        return p->work[a].slot < p->work[b].slot;
-    });
+    {
+        const int ni = p->nintra;
+        std::vector<int32_t> qa(ni), qb(n - ni);
+        std::iota(qa.begin(), qa.end(), 0);
+        std::iota(qb.begin(), qb.end(), ni);
+        std::merge(qa.begin(), qa.end(), qb.begin(), qb.end(), p->order.begin(), [&](int32_t a, int32_t b) {
+            if (p->work[a].n != p->work[b].n) return p->work[a].n > p->work[b].n;
+            return p->work[a].slot < p->work[b].slot;
+        });
+    }
     // the head of that order goes to the long-slice launch (at most a quarter
     // of the slices, so that small batches still spread over many SMs)
     p->nlong = 0;
@@ -668,31 +732,34 @@ extern "C" int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const
     return run_decode(plan, st, payload, xyz, rgb, points24, status, workspace, workspace_bytes, (cudaStream_t)stream, events);
 }
 
+
 namespace {
-// Runs fn(i) for i in [0, n) on up to `threads` host threads.
-template <class F>
-void parallel_for(int n, int threads, F fn) {
-    threads = std::max(1, std::min(threads, n));
-    if (threads == 1) {
-        for (int i = 0; i < n; ++i) fn(i);
-        return;
+thread_local double g_stage_ms[4] = {0, 0, 0, 0};  // see pvvc_host_stage_times
+struct StageClock {
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    double lap() {  // ms since the previous lap
+        const auto now = std::chrono::steady_clock::now();
+        const double ms = std::chrono::duration<double, std::milli>(now - t).count();
+        t = now;
+        return ms;
     }
-    std::atomic<int> next{0};
-    std::vector<std::thread> pool;
-    for (int t = 0; t < threads; ++t)
-        pool.emplace_back([&] {
-            for (int i; (i = next.fetch_add(1)) < n;) fn(i);
-        });
-    for (auto& th : pool) th.join();
-}
+};
 }  // namespace
+
+extern "C" int pvvc_host_stage_times(double* out, int32_t n) {
+    if (!out || n < 0) return PVVC_ERR_ARG;
+    for (int i = 0; i < n && i < 4; ++i) out[i] = g_stage_ms[i];
+    return PVVC_OK;
+}
 
 extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* const* frame_bytes,
                                        const uint64_t* frame_len, float* xyz_host, uint8_t* rgb_host, uint64_t cap_points,
                                        uint64_t* npoints_out, int32_t* status_host, int32_t status_cap, void* stream) {
     if (!st || nframes < 0 || (nframes && (!frame_bytes || !frame_len))) return PVVC_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    const int threads = (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency()));
+    const int threads = host_threads();
+    StageClock clk;
+    for (double& v : g_stage_ms) v = 0;
     // parse (io::LoadFrame) and inflate zstd on the host, frames in parallel
     std::vector<Frame> frames(nframes);
     std::vector<int> prc(nframes, PVVC_OK);
@@ -702,6 +769,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     });
     for (int r : prc)
         if (r) return r;
+    g_stage_ms[0] = clk.lap();
     // payload layout (4-byte aligned) and the batch description, in frame order
     uint64_t bytes = 0, pts = 0;
     int32_t nsl = 0;
@@ -740,12 +808,16 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (st->h_payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     uint8_t* hp = static_cast<uint8_t*>(st->h_payload.p);
     parallel_for(nframes, threads, [&](int f) {
-        const Frame& fr = frames[f];
+        Frame& fr = frames[f];
         for (size_t i = 0; i < fr.count(); ++i) {
             const int32_t k = ffirst[f] + (int32_t)i;
             if (gsz[k]) std::memcpy(hp + goff[k], fr.geometry[i].data(), gsz[k]);
             if (csz[k]) std::memcpy(hp + coff[k], fr.color[i].data(), csz[k]);
         }
+        // the payload bytes are packed: free this frame's per-slice buffers
+        // here, in parallel, rather than all of them on return
+        std::vector<std::vector<uint8_t>>().swap(fr.geometry);
+        std::vector<std::vector<uint8_t>>().swap(fr.color);
     });
     std::memset(hp + bytes, 0, 16);  // the decoder reads whole 16-byte blocks
     // Intra slices of different frames of one call may hit the same patch
@@ -801,6 +873,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     }
     if (!merge)
         for (int32_t k = 0; k < nsl; ++k) slot[k] = index[k];
+    g_stage_ms[1] = clk.lap();
     if (st->payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
@@ -819,11 +892,13 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         rc = build_plan(&d, &st->plan, nullptr, nullptr);
         if (rc) break;
         if (st->ws.ensure(st->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
+        g_stage_ms[2] += clk.lap();
         rc = run_decode(&st->plan, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
                         static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
                         st->ws.cap, s, nullptr);
         // the plan's host arrays are rebuilt by the next run: finish this one first
         if (rc == PVVC_OK && runs.size() > 2 && cudaStreamSynchronize(s) != cudaSuccess) rc = PVVC_ERR_CUDA;
+        g_stage_ms[3] += clk.lap();
     }
     if (rc) return rc;
     if (xyz_host && pts && cudaMemcpyAsync(xyz_host, st->xyz.p, 12 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
@@ -833,6 +908,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (status_host && nsl && cudaMemcpyAsync(status_host, st->status.p, 4ull * nsl, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return PVVC_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return PVVC_ERR_CUDA;
+    g_stage_ms[3] += clk.lap();
     return PVVC_OK;
 }
 

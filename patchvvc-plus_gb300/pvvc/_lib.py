@@ -90,6 +90,7 @@ SIGNATURES = [
     ("pvvc_decode_profiled", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, vp, C.POINTER(vp)]),
     ("pvvc_decode_frames_host", C.c_int, [vp, C.c_int32, C.POINTER(u8p), u64p, f32p, u8p, C.c_uint64, u64p, i32p,
                                           C.c_int32, vp]),
+    ("pvvc_host_stage_times", C.c_int, [C.POINTER(C.c_double), C.c_int32]),
     ("pvvc_launch_cudaProcess", C.c_int, [C.c_int, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                           C.c_int, vp]),
     ("pvvc_encode_patch_gop", C.c_int, [f32p, C.c_uint32, f32p, C.c_int32, u8p, u8p, C.c_uint64, u64p, u8p,
