@@ -305,6 +305,32 @@ int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const uint32_t* s
                          const uint32_t* tgt_off, const float* T, float* mse_out, void* workspace,
                          uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream);
 
+/* ---- colour interpolation of the GoP encoder -------------------------------
+ * Replaces GoPEncoding::Interpolation and the k-NN loop of GoPEncoding::Encode
+ * (src/patch/GoP_encoding.cc:73-95,131-150) for many (query cloud, source
+ * patch) pairs: the query cloud is a GoP's fitting cloud, the source one
+ * frame's patch with its RGB colours.  Per query point: the k nearest source
+ * points by FP32 squared distance (x, y, z accumulated in order, as PCL's
+ * exact k-d tree), the lower source index first among equal distances, and
+ * fewer when the patch is smaller; weights 1/max(d, 1e-6) normalised by
+ * their sum; the weighted RGB converted to YUV by BT.601 (common.h:83-92),
+ * every operation rounded in the reference's order.  base_pair (optional):
+ * pair p with base_pair[p] >= 0 then becomes the residual against that pair
+ * (GoP_encoding.cc:144-148; the base needs no base of its own and the same
+ * query count).  All arrays are device memory:
+ *   query_xyz + 3*query_off[p], query_n[p] points   (pairs may share a cloud)
+ *   src_xyz, src_rgb: source p = points [src_off[p], src_off[p+1])
+ *   yuv_out + 3*out_off[p]: query_n[p] YUV triples
+ *   status (optional): per pair 0, or PVVC_ERR_ARG for an empty patch (its
+ *   output zeroed) or a bad base.
+ * k: 1..16 (the reference's patch.interpolation_num defaults to 10).
+ * Stream-ordered; workspace of pvvc_knn_colors_workspace_size bytes. */
+int pvvc_knn_colors_workspace_size(int32_t npairs, uint64_t total_src_points, uint64_t* bytes);
+int pvvc_knn_colors_batch(int32_t npairs, const float* query_xyz, const uint64_t* query_off, const uint32_t* query_n,
+                          const float* src_xyz, const uint8_t* src_rgb, const uint32_t* src_off, int32_t k,
+                          const int32_t* base_pair, float* yuv_out, const uint64_t* out_off, int32_t* status,
+                          void* workspace, uint64_t workspace_bytes, uint64_t total_src_points, void* stream);
+
 /* ---- BF16 tensor-core GEMM ------------------------------------------------
  * The building block of the registration network's training and inference
  * kernels (no reference counterpart: the reference registers with PCL ICP

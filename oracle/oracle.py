@@ -115,6 +115,11 @@ class Oracle:
                                           C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
             lib.pvo_cloud_mse.restype = C.c_float
             lib.pvo_cloud_mse.argtypes = [_f32p, C.c_size_t, _f32p, C.c_size_t]
+            lib.pvo_knn_colors.restype = C.c_int
+            lib.pvo_knn_colors.argtypes = [_f32p, C.c_size_t, _f32p, _u8p, C.c_size_t, C.c_int, C.c_int, _f32p]
+            lib.pvo_knn_colors_batch.restype = C.c_int
+            lib.pvo_knn_colors_batch.argtypes = [C.c_int, _f32p, C.POINTER(C.c_uint64), _u32p, _f32p, _u8p, _u32p,
+                                                 C.c_int, _f32p, C.POINTER(C.c_uint64), C.c_int]
 
     # ---- RLGR ----
     def rlgr_encode(self, sym: np.ndarray) -> bytes:
@@ -245,6 +250,37 @@ class Oracle:
         a = np.ascontiguousarray(a, np.float32)
         b = np.ascontiguousarray(b, np.float32)
         return float(self.lib.pvo_cloud_mse(_ptr(a, _f32p), a.shape[0], _ptr(b, _f32p), b.shape[0]))
+
+    # ---- colour interpolation (GoP_encoding.cc:73-95,131-150) ----
+    def knn_colors(self, q, src, rgb, k=10, brute=False) -> np.ndarray:
+        """YUV [nq,3] interpolated at the query points from the k nearest
+        source points (pvo_knn_colors)."""
+        q = np.ascontiguousarray(q, np.float32).reshape(-1, 3)
+        src = np.ascontiguousarray(src, np.float32).reshape(-1, 3)
+        rgb = np.ascontiguousarray(rgb, np.uint8).reshape(-1, 3)
+        out = np.zeros((max(q.shape[0], 1), 3), np.float32)
+        st = self.lib.pvo_knn_colors(_ptr(q, _f32p), q.shape[0], _ptr(src, _f32p), _ptr(rgb, _u8p), src.shape[0], k,
+                                     1 if brute else 0, _ptr(out, _f32p))
+        if st:
+            raise RuntimeError(f"knn status {st}")
+        return out[:q.shape[0]]
+
+    def knn_colors_batch(self, queries, sources, rgbs, k, nthreads) -> list:
+        """knn_colors over many (query, source) pairs on nthreads threads."""
+        n = len(sources)
+        q = np.ascontiguousarray(np.concatenate(queries), np.float32)
+        qn = np.array([x.shape[0] for x in queries], np.uint32)
+        qoff = np.zeros(n, np.uint64); qoff[1:] = np.cumsum(qn.astype(np.uint64))[:-1]
+        s = np.ascontiguousarray(np.concatenate(sources), np.float32)
+        c = np.ascontiguousarray(np.concatenate(rgbs), np.uint8)
+        so = np.zeros(n + 1, np.uint32); so[1:] = np.cumsum([x.shape[0] for x in sources])
+        out = np.zeros((max(int(qn.sum()), 1), 3), np.float32)
+        st = self.lib.pvo_knn_colors_batch(n, _ptr(q, _f32p), qoff.ctypes.data_as(C.POINTER(C.c_uint64)), _ptr(qn, _u32p),
+                                           _ptr(s, _f32p), _ptr(c, _u8p), _ptr(so, _u32p), k, _ptr(out, _f32p),
+                                           qoff.ctypes.data_as(C.POINTER(C.c_uint64)), nthreads)
+        if st:
+            raise RuntimeError(f"knn status {st}")
+        return [out[int(a):int(a) + int(m)] for a, m in zip(qoff, qn)]
 
 
 class OracleDecoder:

@@ -127,6 +127,22 @@ int pvo_icp_batch(int npairs, const float* src, const uint32_t* soff, const floa
 /* Symmetric mean squared NN distance, max of both directions. */
 float pvo_cloud_mse(const float* a, size_t na, const float* b, size_t nb);
 
+/* Colour interpolation of the GoP encoder (GoPEncoding::Interpolation and its
+ * k-NN loop, src/patch/GoP_encoding.cc:73-95,131-150): for each query point,
+ * the k nearest source points by FP32 squared distance (ties: lower source
+ * index first; fewer when the source is smaller), weights 1/max(d, 1e-6)
+ * normalised by their sum, the weighted RGB, then BT.601 to YUV (common.h:
+ * 83-92).  yuv_out: nq x 3 floats.  brute = 1 tests every source point (the
+ * definition); brute = 0 searches a uniform grid and returns the same
+ * neighbours.  Returns 0 or PVO_ERR_ARG (empty source, k < 1 or k > 64). */
+int pvo_knn_colors(const float* q, size_t nq, const float* src, const uint8_t* rgb, size_t ns, int k, int brute,
+                   float* yuv_out);
+/* pvo_knn_colors over many pairs (query ranges qoff/qn, source ranges soff,
+ * outputs at out_off) with the grid search on nthreads threads. */
+int pvo_knn_colors_batch(int npairs, const float* q, const uint64_t* qoff, const uint32_t* qn, const float* src,
+                         const uint8_t* rgb, const uint32_t* soff, int k, float* yuv, const uint64_t* out_off,
+                         int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -331,3 +331,232 @@ int pvo_icp_batch(int npairs, const float* src, const uint32_t* soff, const floa
     pthread_mutex_destroy(&j.mu);
     return PVO_OK;
 }
+
+/* ---- colour interpolation (GoPEncoding::Interpolation + the k-NN loop of
+ * GoPEncoding::Encode, src/patch/GoP_encoding.cc:73-95,131-150) ----
+ * PCL's KdTree (FLANN, exact) returns the k nearest points with squared
+ * distances accumulated in float, x then y then z, sorted ascending; ties
+ * here go to the lower source index.  The arithmetic below follows the
+ * reference's statement order in float. */
+#define KNN_MAX 64
+typedef struct {
+    float d[KNN_MAX];
+    int i[KNN_MAX];
+    int n, k;
+} knn_t;
+
+static int knn_less(float da, int ia, float db, int ib) { return da < db || (da == db && ia < ib); }
+
+static void knn_offer(knn_t* s, float d, int idx) {
+    if (s->n == s->k && !knn_less(d, idx, s->d[s->n - 1], s->i[s->n - 1])) return;
+    int j = s->n < s->k ? s->n++ : s->n - 1;
+    while (j > 0 && knn_less(d, idx, s->d[j - 1], s->i[j - 1])) {
+        s->d[j] = s->d[j - 1];
+        s->i[j] = s->i[j - 1];
+        --j;
+    }
+    s->d[j] = d;
+    s->i[j] = idx;
+}
+
+static float sqdist(const float* p, float qx, float qy, float qz) {
+    float dx = p[0] - qx, dy = p[1] - qy, dz = p[2] - qz;
+    float a = dx * dx;
+    a = a + dy * dy;
+    a = a + dz * dz;
+    return a;
+}
+
+/* the reference's Interpolation on the found neighbours, then ColorYUV(r,g,b,false) */
+static void knn_interp(const knn_t* s, const uint8_t* rgb, float* out) {
+    float w[KNN_MAX];
+    for (int j = 0; j < s->n; ++j) {
+        float d = s->d[j];
+        if (d <= 1e-6f) d = 1e-6f;
+        w[j] = 1.0f / d;
+    }
+    float sum = 0.0f;
+    for (int j = 0; j < s->n; ++j) sum = sum + w[j];
+    for (int j = 0; j < s->n; ++j) w[j] = w[j] / sum;
+    float r = 0.0f, g = 0.0f, b = 0.0f;
+    for (int j = 0; j < s->n; ++j) {
+        const uint8_t* c = rgb + 3 * (size_t)s->i[j];
+        r = r + w[j] * (float)c[0];
+        g = g + w[j] * (float)c[1];
+        b = b + w[j] * (float)c[2];
+    }
+    out[0] = r * 0.299f + g * 0.587f + b * 0.114f;
+    out[1] = r * -0.168736f - g * 0.331264f + b * 0.5f + 128;
+    out[2] = r * 0.5f - g * 0.418688f - b * 0.081312f + 128;
+}
+
+/* uniform float grid over the source: about two points per cell, cells of
+ * at least one voxel; ring search pruned by the k-th distance */
+typedef struct {
+    float lo[3], h;
+    int dim[3];
+    int* start;
+    int* idx; /* source indices sorted by cell */
+} fgrid_t;
+
+static int fgrid_build(fgrid_t* g, const float* p, size_t n) {
+    float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (size_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) {
+            if (p[3 * i + a] < lo[a]) lo[a] = p[3 * i + a];
+            if (p[3 * i + a] > hi[a]) hi[a] = p[3 * i + a];
+        }
+    double vol = 1;
+    for (int a = 0; a < 3; ++a) vol *= fmax(hi[a] - lo[a], 1.0);
+    double h = cbrt(vol / (2.0 * (double)n));
+    if (h < 1.0) h = 1.0;
+    for (;;) {
+        double cells = 1;
+        for (int a = 0; a < 3; ++a) cells *= floor((hi[a] - lo[a]) / h) + 1;
+        if (cells <= 4.0 * (double)n + 64) break;
+        h *= 1.25;
+    }
+    g->h = (float)h;
+    size_t nc = 1;
+    for (int a = 0; a < 3; ++a) {
+        g->lo[a] = lo[a];
+        g->dim[a] = (int)floor((hi[a] - lo[a]) / h) + 1;
+        nc *= (size_t)g->dim[a];
+    }
+    g->start = (int*)calloc(nc + 1, sizeof(int));
+    g->idx = (int*)malloc(n * sizeof(int) + 4);
+    int* cell = (int*)malloc(n * sizeof(int) + 4);
+    if (!g->start || !g->idx || !cell) {
+        free(cell);
+        return PVO_ERR_NOMEM;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        int c[3];
+        for (int a = 0; a < 3; ++a) {
+            c[a] = (int)floor(((double)p[3 * i + a] - g->lo[a]) / g->h);
+            if (c[a] < 0) c[a] = 0;
+            if (c[a] >= g->dim[a]) c[a] = g->dim[a] - 1;
+        }
+        cell[i] = (c[2] * g->dim[1] + c[1]) * g->dim[0] + c[0];
+        g->start[cell[i] + 1]++;
+    }
+    for (size_t c = 0; c < nc; ++c) g->start[c + 1] += g->start[c];
+    int* fill = (int*)malloc((nc + 1) * sizeof(int));
+    memcpy(fill, g->start, (nc + 1) * sizeof(int));
+    for (size_t i = 0; i < n; ++i) g->idx[fill[cell[i]]++] = (int)i;
+    free(fill);
+    free(cell);
+    return PVO_OK;
+}
+
+static void fgrid_free(fgrid_t* g) {
+    free(g->start);
+    free(g->idx);
+}
+
+static void fgrid_knn(const fgrid_t* g, const float* src, float qx, float qy, float qz, knn_t* s) {
+    const double q[3] = {qx, qy, qz};
+    int c[3];
+    for (int a = 0; a < 3; ++a) {
+        double t = floor((q[a] - g->lo[a]) / g->h);
+        if (t < 0) t = 0;
+        if (t > g->dim[a] - 1) t = g->dim[a] - 1;
+        c[a] = (int)t;
+    }
+    int maxr = g->dim[0];
+    if (g->dim[1] > maxr) maxr = g->dim[1];
+    if (g->dim[2] > maxr) maxr = g->dim[2];
+    for (int r = 0; r <= maxr; ++r) {
+        if (r > 0 && s->n == s->k) {
+            /* a point in ring r lies at least (r-1)*h away (margin for rounding) */
+            double lb = (r - 1) * (double)g->h;
+            if (lb * lb * 0.999 > s->d[s->n - 1]) break;
+        }
+        for (int z = c[2] - r; z <= c[2] + r; ++z) {
+            if (z < 0 || z >= g->dim[2]) continue;
+            for (int y = c[1] - r; y <= c[1] + r; ++y) {
+                if (y < 0 || y >= g->dim[1]) continue;
+                for (int x = c[0] - r; x <= c[0] + r; ++x) {
+                    if (x < 0 || x >= g->dim[0]) continue;
+                    if (abs(x - c[0]) != r && abs(y - c[1]) != r && abs(z - c[2]) != r) continue;
+                    const int cc = (z * g->dim[1] + y) * g->dim[0] + x;
+                    for (int m = g->start[cc]; m < g->start[cc + 1]; ++m) {
+                        const int i = g->idx[m];
+                        knn_offer(s, sqdist(src + 3 * (size_t)i, qx, qy, qz), i);
+                    }
+                }
+            }
+        }
+    }
+}
+
+int pvo_knn_colors(const float* q, size_t nq, const float* src, const uint8_t* rgb, size_t ns, int k, int brute,
+                   float* yuv_out) {
+    if (!src || !rgb || !ns || k < 1 || k > KNN_MAX || (nq && (!q || !yuv_out))) return PVO_ERR_ARG;
+    fgrid_t g;
+    memset(&g, 0, sizeof(g));
+    if (!brute && fgrid_build(&g, src, ns)) return PVO_ERR_NOMEM;
+    for (size_t t = 0; t < nq; ++t) {
+        knn_t s;
+        s.n = 0;
+        s.k = k < (int)ns ? k : (int)ns;
+        const float qx = q[3 * t], qy = q[3 * t + 1], qz = q[3 * t + 2];
+        if (brute) {
+            for (size_t i = 0; i < ns; ++i) knn_offer(&s, sqdist(src + 3 * i, qx, qy, qz), (int)i);
+        } else {
+            fgrid_knn(&g, src, qx, qy, qz, &s);
+        }
+        knn_interp(&s, rgb, yuv_out + 3 * t);
+    }
+    if (!brute) fgrid_free(&g);
+    return PVO_OK;
+}
+
+typedef struct {
+    int npairs, k;
+    const float* q;
+    const uint64_t* qoff;
+    const uint32_t* qn;
+    const float* src;
+    const uint8_t* rgb;
+    const uint32_t* soff;
+    float* yuv;
+    const uint64_t* out_off;
+    pthread_mutex_t mu;
+    int next, rc;
+} knn_job_t;
+
+static void* knn_worker(void* arg) {
+    knn_job_t* j = (knn_job_t*)arg;
+    for (;;) {
+        pthread_mutex_lock(&j->mu);
+        int p = j->next++;
+        pthread_mutex_unlock(&j->mu);
+        if (p >= j->npairs) break;
+        const uint32_t a = j->soff[p], b = j->soff[p + 1];
+        int rc = pvo_knn_colors(j->q + 3 * j->qoff[p], j->qn[p], j->src + 3ull * a, j->rgb + 3ull * a, b - a, j->k, 0,
+                                j->yuv + 3 * j->out_off[p]);
+        if (rc) {
+            pthread_mutex_lock(&j->mu);
+            j->rc = rc;
+            pthread_mutex_unlock(&j->mu);
+        }
+    }
+    return NULL;
+}
+
+int pvo_knn_colors_batch(int npairs, const float* q, const uint64_t* qoff, const uint32_t* qn, const float* src,
+                         const uint8_t* rgb, const uint32_t* soff, int k, float* yuv, const uint64_t* out_off,
+                         int nthreads) {
+    knn_job_t j = {npairs, k, q, qoff, qn, src, rgb, soff, yuv, out_off};
+    pthread_mutex_init(&j.mu, NULL);
+    j.next = 0;
+    j.rc = 0;
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 256) nthreads = 256;
+    pthread_t th[256];
+    for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, knn_worker, &j);
+    for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&j.mu);
+    return j.rc;
+}

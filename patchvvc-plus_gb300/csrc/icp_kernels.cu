@@ -19,6 +19,9 @@
 //            FP64 and applies the convergence tests of the PCL criteria.
 //   k_nn_mean  mean squared NN distance of (transformed) query points to a
 //            gridded cloud, per pair.
+//   k_knn_color  colour interpolation of the GoP encoder (k nearest source
+//            points per query point, inverse-distance weights, BT.601 YUV);
+//            k_knn_sub turns later frames into residuals against frame 0.
 #include <cuda_runtime.h>
 
 #include <cfloat>
@@ -515,6 +518,153 @@ __global__ void __launch_bounds__(kIcpThreads) k_nn_mean(const float* __restrict
 }
 
 // ---------------------------------------------------------------------------
+// Colour interpolation of the GoP encoder (GoPEncoding::Interpolation and the
+// k-NN loop of GoPEncoding::Encode, src/patch/GoP_encoding.cc:73-95,131-150):
+// for every point of a query cloud (the GoP's fitting cloud), the k nearest
+// points of a source patch by FP32 squared distance, accumulated x, y, z as
+// PCL's exact k-d tree does; among equal distances the lower source index
+// first.  Weights 1/max(d, 1e-6) normalised by their sum, weighted RGB, then
+// BT.601 to YUV (common.h:83-92), each operation rounded in the reference's
+// order.  The source patch is gridded by k_grid (points carry their index).
+constexpr int kKnnMax = 16;
+constexpr int kKnnThreads = 256;
+
+__device__ __forceinline__ bool knn_less(float da, int ia, float db, int ib) { return da < db || (da == db && ia < ib); }
+
+// The min(k, n) nearest gridded points to q, ascending in the thread's
+// shared-memory columns ld[0..k-1][tid], li[...]; returns how many.  The
+// k-th entry stays in registers: most candidates lose against it, and an
+// insertion shifts the column (rare once the k-th distance is tight).
+__device__ __forceinline__ int grid_knn(const GridHdr& g, const int* __restrict__ cs, const float4* __restrict__ sp,
+                                        uint32_t base, float qx, float qy, float qz, int k, float (*ld)[kKnnThreads],
+                                        int (*li)[kKnnThreads]) {
+    const int tid = threadIdx.x;
+    int cnt = 0;
+    float kd = INFINITY;  // the k-th entry (distance, index) once k are held
+    int ki = 0x7fffffff;
+    const int cx = min(max((int)floorf((qx - g.lo[0]) / g.h), 0), g.dim[0] - 1);
+    const int cy = min(max((int)floorf((qy - g.lo[1]) / g.h), 0), g.dim[1] - 1);
+    const int cz = min(max((int)floorf((qz - g.lo[2]) / g.h), 0), g.dim[2] - 1);
+    auto gap2 = [&](int c, float q, float lo) {
+        const float a = lo + (float)c * g.h, b = a + g.h;
+        const float d = q < a ? a - q : (q > b ? q - b : 0.f);
+        return d * d;
+    };
+    const int maxr = max(g.dim[0], max(g.dim[1], g.dim[2]));
+    for (int r = 0; r <= maxr; ++r) {
+        if (r > 0 && cnt == k) {
+            const float lb = (float)(r - 1) * g.h;
+            if (lb * lb * 0.999f > kd) break;
+        }
+        for (int z = max(cz - r, 0); z <= min(cz + r, g.dim[2] - 1); ++z) {
+            const bool zr = (z == cz - r) || (z == cz + r);
+            const float dz2 = gap2(z, qz, g.lo[2]);
+            if (dz2 * 0.999f > kd) continue;
+            for (int y = max(cy - r, 0); y <= min(cy + r, g.dim[1] - 1); ++y) {
+                const float dyz2 = dz2 + gap2(y, qy, g.lo[1]);
+                if (dyz2 * 0.999f > kd) continue;
+                const bool yr = zr || (y == cy - r) || (y == cy + r);
+                int x = max(cx - r, 0);
+                const int xe = min(cx + r, g.dim[0] - 1);
+                const int step = yr ? 1 : max(2 * r, 1);
+                if (!yr && x != cx - r) x = (cx + r <= xe) ? cx + r : xe + 1;
+                for (; x <= xe; x += step) {
+                    // a cell whose box is farther than the k-th cannot hold a
+                    // point that ranks before it (0.999: rounding margin)
+                    if ((dyz2 + gap2(x, qx, g.lo[0])) * 0.999f > kd) continue;
+                    const int c = (z * g.dim[1] + y) * g.dim[0] + x;
+                    const int e = __ldg(cs + c + 1);
+                    for (int m = __ldg(cs + c); m < e; ++m) {
+                        const float4 p = __ldg(sp + base + m);
+                        const float dx = __fsub_rn(p.x, qx), dy = __fsub_rn(p.y, qy), dz = __fsub_rn(p.z, qz);
+                        const float d = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+                        const int pi = __float_as_int(p.w);
+                        if (!knn_less(d, pi, kd, ki)) continue;
+                        int j = cnt < k ? cnt++ : k - 1;  // the slot freed (or the k-th, dropped)
+                        while (j > 0 && knn_less(d, pi, ld[j - 1][tid], li[j - 1][tid])) {
+                            ld[j][tid] = ld[j - 1][tid];
+                            li[j][tid] = li[j - 1][tid];
+                            --j;
+                        }
+                        ld[j][tid] = d;
+                        li[j][tid] = pi;
+                        if (cnt == k) {
+                            kd = ld[k - 1][tid];
+                            ki = li[k - 1][tid];
+                        }
+                    }
+                }
+            }
+        }
+    }
+    return cnt;
+}
+
+__global__ void __launch_bounds__(kKnnThreads) k_knn_color(const float* __restrict__ q, const uint64_t* __restrict__ qoff,
+                                                           const uint32_t* __restrict__ qn, const uint32_t* __restrict__ soff,
+                                                           const GridHdr* __restrict__ hdr, const int* __restrict__ cstart,
+                                                           const float4* __restrict__ sorted, int kmul,
+                                                           const uint8_t* __restrict__ rgb, int k, float* __restrict__ yuv,
+                                                           const uint64_t* __restrict__ out_off, int32_t* __restrict__ status) {
+    __shared__ float s_d[kKnnMax][kKnnThreads];
+    __shared__ int s_i[kKnnMax][kKnnThreads];
+    const int pair = blockIdx.x, tid = threadIdx.x;
+    const uint32_t sb = soff[pair], ns = soff[pair + 1] - sb, n = qn[pair];
+    const float* qp = q + 3 * qoff[pair];
+    float* op = yuv + 3 * out_off[pair];
+    if (ns == 0) {  // the reference's k-d tree rejects an empty cloud
+        for (uint32_t i = tid; i < 3 * n; i += kKnnThreads) op[i] = 0.f;
+        if (tid == 0 && status) status[pair] = PVVC_ERR_ARG;
+        return;
+    }
+    const GridHdr g = hdr[pair];
+    const int* cs = cstart + cell_base(kmul, sb, pair);
+    const int kk = min(k, (int)ns);
+    for (uint32_t t = tid; t < n; t += kKnnThreads) {
+        const int cnt = grid_knn(g, cs, sorted, sb, qp[3 * t], qp[3 * t + 1], qp[3 * t + 2], kk, s_d, s_i);
+        // GoPEncoding::Interpolation: weights 1/max(d, 1e-6), their sum in
+        // order, then the normalised weights times the colours in order
+        float sum = 0.f;
+        for (int j = 0; j < cnt; ++j) {
+            const float d = s_d[j][tid];
+            sum = __fadd_rn(sum, __fdiv_rn(1.0f, d <= 1e-6f ? 1e-6f : d));
+        }
+        float r = 0.f, gc = 0.f, b = 0.f;
+        for (int j = 0; j < cnt; ++j) {
+            const float d = s_d[j][tid];
+            const float wj = __fdiv_rn(__fdiv_rn(1.0f, d <= 1e-6f ? 1e-6f : d), sum);
+            const uint8_t* c = rgb + 3 * (size_t)(sb + (uint32_t)s_i[j][tid]);
+            r = __fadd_rn(r, __fmul_rn(wj, (float)c[0]));
+            gc = __fadd_rn(gc, __fmul_rn(wj, (float)c[1]));
+            b = __fadd_rn(b, __fmul_rn(wj, (float)c[2]));
+        }
+        op[3 * t] = __fadd_rn(__fadd_rn(__fmul_rn(r, 0.299f), __fmul_rn(gc, 0.587f)), __fmul_rn(b, 0.114f));
+        op[3 * t + 1] =
+            __fadd_rn(__fadd_rn(__fsub_rn(__fmul_rn(r, -0.168736f), __fmul_rn(gc, 0.331264f)), __fmul_rn(b, 0.5f)), 128.0f);
+        op[3 * t + 2] =
+            __fadd_rn(__fsub_rn(__fsub_rn(__fmul_rn(r, 0.5f), __fmul_rn(gc, 0.418688f)), __fmul_rn(b, 0.081312f)), 128.0f);
+    }
+    if (tid == 0 && status) status[pair] = PVVC_OK;
+}
+
+// residuals of the later frames (GoP_encoding.cc:144-148): pair p with
+// base[p] >= 0 subtracts that pair's colours, point by point; the base must
+// have no base of its own and as many query points
+__global__ void k_knn_sub(int npairs, const uint32_t* __restrict__ qn, const int32_t* __restrict__ base,
+                          float* __restrict__ yuv, const uint64_t* __restrict__ out_off, int32_t* __restrict__ status) {
+    const int pair = blockIdx.x;
+    const int b = base[pair];
+    if (b < 0) return;
+    if (b >= npairs || base[b] >= 0 || qn[b] != qn[pair]) {
+        if (threadIdx.x == 0 && status) status[pair] = PVVC_ERR_ARG;
+        return;
+    }
+    float* o = yuv + 3 * out_off[pair];
+    const float* f0 = yuv + 3 * out_off[b];
+    for (uint32_t i = threadIdx.x; i < 3 * qn[pair]; i += blockDim.x) o[i] = __fsub_rn(o[i], f0[i]);
+}
+
+// ---------------------------------------------------------------------------
 // pvvc_icp_batch_noalloc: the same two kernels as pvvc_icp_batch, with the
 // target grid kept in a fixed file-scope device array instead of a
 // caller-provided workspace, so that the call allocates nothing.
@@ -645,6 +795,54 @@ extern "C" int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const 
     k_nn_mean<<<npairs, kIcpThreads, 0, s>>>(tgt_xyz, tgt_off, nullptr, src_off, w.hdr2, w.cstart2, w.sorted2, kIcpCellMul,
                                              w.tmp + npairs);
     k_max2<<<(npairs + 255) / 256, 256, 0, s>>>(w.tmp, npairs, mse_out);
+    return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
+}
+
+namespace {
+uint64_t knn_ws_bytes(int32_t npairs, uint64_t nsrc, GridHdr** hdr, int** cstart, float4** sorted, void* base) {
+    uint64_t o = 0;
+    auto take = [&](uint64_t b) {
+        const uint64_t r = o;
+        o = al(o + b);
+        return r;
+    };
+    const uint64_t h = take(sizeof(GridHdr) * npairs), c = take(4ull * cell_ints(kIcpCellMul, nsrc, npairs)),
+                   s = take(16ull * nsrc);
+    if (base) {
+        uint8_t* p = static_cast<uint8_t*>(base);
+        *hdr = reinterpret_cast<GridHdr*>(p + h);
+        *cstart = reinterpret_cast<int*>(p + c);
+        *sorted = reinterpret_cast<float4*>(p + s);
+    }
+    return o;
+}
+}  // namespace
+
+extern "C" int pvvc_knn_colors_workspace_size(int32_t npairs, uint64_t total_src_points, uint64_t* bytes) {
+    if (npairs < 0 || !bytes) return PVVC_ERR_ARG;
+    *bytes = knn_ws_bytes(npairs, total_src_points, nullptr, nullptr, nullptr, nullptr);
+    return PVVC_OK;
+}
+
+extern "C" int pvvc_knn_colors_batch(int32_t npairs, const float* query_xyz, const uint64_t* query_off,
+                                     const uint32_t* query_n, const float* src_xyz, const uint8_t* src_rgb,
+                                     const uint32_t* src_off, int32_t k, const int32_t* base_pair, float* yuv_out,
+                                     const uint64_t* out_off, int32_t* status, void* workspace, uint64_t workspace_bytes,
+                                     uint64_t total_src_points, void* stream) {
+    if (npairs < 0 || k < 1 || k > kKnnMax) return PVVC_ERR_ARG;
+    if (npairs == 0) return PVVC_OK;
+    if (!query_xyz || !query_off || !query_n || !src_xyz || !src_rgb || !src_off || !yuv_out || !out_off || !workspace)
+        return PVVC_ERR_ARG;
+    GridHdr* hdr = nullptr;
+    int* cstart = nullptr;
+    float4* sorted = nullptr;
+    if (knn_ws_bytes(npairs, total_src_points, &hdr, &cstart, &sorted, workspace) > workspace_bytes) return PVVC_ERR_CAPACITY;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!grid_attr_ready()) return PVVC_ERR_CUDA;
+    k_grid<256><<<npairs, 256, kGridSmem, s>>>(src_xyz, src_off, nullptr, hdr, cstart, sorted, kIcpCellMul);
+    k_knn_color<<<npairs, kKnnThreads, 0, s>>>(query_xyz, query_off, query_n, src_off, hdr, cstart, sorted, kIcpCellMul, src_rgb, k,
+                                       yuv_out, out_off, status);
+    if (base_pair) k_knn_sub<<<npairs, 256, 0, s>>>(npairs, query_n, base_pair, yuv_out, out_off, status);
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }
 

@@ -108,6 +108,9 @@ SIGNATURES = [
     ("pvvc_icp_batch_noalloc", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, C.POINTER(IcpParams), vp, vp, vp, vp,
                                          C.c_uint64, vp]),
     ("pvvc_cloud_mse_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
+    ("pvvc_knn_colors_workspace_size", C.c_int, [C.c_int32, C.c_uint64, u64p]),
+    ("pvvc_knn_colors_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, C.c_int32, vp, vp, vp, vp, vp, C.c_uint64,
+                                        C.c_uint64, vp]),
     ("pvvc_gemm_bf16", C.c_int, [C.c_int32, C.c_int32, C.c_int32, vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp, vp,
                                  C.c_int64, C.c_int32, C.c_int32, vp]),
     ("pvvc_device_error_take", C.c_int, [i32p]),

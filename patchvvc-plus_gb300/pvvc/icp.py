@@ -186,6 +186,60 @@ class IcpBatch:
         return out.cpu().numpy()
 
 
+class KnnColorBatch:
+    """Device-resident colour interpolation of the GoP encoder
+    (pvvc_knn_colors_batch; GoPEncoding::Interpolation and its k-NN loop,
+    src/patch/GoP_encoding.cc:73-95,131-150).  queries: float32 [n,3] clouds
+    (a pair names one by query_of[p]); sources: float32 [m,3] patches with
+    rgbs: uint8 [m,3]; base: optional base pair per pair (-1: none), which
+    turns a pair into the residual against its base."""
+
+    def __init__(self, queries, query_of, sources, rgbs, k=10, base=None, device="cuda"):
+        import torch
+        self.torch = torch
+        dev = torch.device(device)
+        self.n = len(sources)
+        q = np.ascontiguousarray(np.concatenate(queries) if queries else np.zeros((0, 3)), np.float32)
+        qstart = np.zeros(len(queries) + 1, np.uint64)
+        qstart[1:] = np.cumsum([x.shape[0] for x in queries])
+        qof = np.asarray(query_of, np.int64)
+        self.qn = np.array([queries[i].shape[0] for i in qof], np.uint32)
+        qoff = qstart[qof].astype(np.uint64)
+        self.out_off = np.zeros(self.n, np.uint64)
+        self.out_off[1:] = np.cumsum(self.qn.astype(np.uint64))[:-1]
+        s, so = _pack(sources)
+        c = np.ascontiguousarray(np.concatenate(rgbs), np.uint8)
+        self.ns = int(s.shape[0])
+        self.k = int(k)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+        self.q, self.qoff, self.qn_d = t(q), t(qoff.view(np.int64)), t(self.qn.view(np.int32))
+        self.src, self.rgb, self.soff = t(s), t(c), t(so.view(np.int32))
+        self.base = None if base is None else t(np.asarray(base, np.int32))
+        self.out_off_d = t(self.out_off.view(np.int64))
+        self.total = int(self.qn.sum())
+        self.yuv = torch.empty((max(self.total, 1), 3), dtype=torch.float32, device=dev)
+        self.status = torch.empty(max(self.n, 1), dtype=torch.int32, device=dev)
+        b = C.c_uint64(0)
+        L.check(L.lib().pvvc_knn_colors_workspace_size(self.n, self.ns, C.byref(b)), "pvvc_knn_colors_workspace_size")
+        self.ws = torch.empty(max(int(b.value), 256), dtype=torch.uint8, device=dev)
+        self.dev = dev
+
+    def run(self, stream=None):
+        """Launch pvvc_knn_colors_batch (stream-ordered, no sync)."""
+        sp = stream if stream is not None else self.torch.cuda.current_stream(self.dev).cuda_stream
+        L.check(L.lib().pvvc_knn_colors_batch(self.n, self.q.data_ptr(), self.qoff.data_ptr(), self.qn_d.data_ptr(),
+                                              self.src.data_ptr(), self.rgb.data_ptr(), self.soff.data_ptr(), self.k,
+                                              None if self.base is None else self.base.data_ptr(), self.yuv.data_ptr(),
+                                              self.out_off_d.data_ptr(), self.status.data_ptr(), self.ws.data_ptr(),
+                                              self.ws.numel(), self.ns, sp), "pvvc_knn_colors_batch")
+
+    def results(self):
+        """Per pair its YUV [n,3] (numpy) and the status array."""
+        self.torch.cuda.synchronize(self.dev)
+        y = self.yuv.cpu().numpy()
+        return [y[int(a):int(a) + int(m)] for a, m in zip(self.out_off, self.qn)], self.status.cpu().numpy()[:self.n]
+
+
 def rotation_error_deg(A: np.ndarray, B: np.ndarray) -> np.ndarray:
     """Angle of A[:3,:3] B[:3,:3]^T per pair, degrees."""
     R = np.einsum("nij,nkj->nik", A[:, :3, :3].astype(np.float64), B[:, :3, :3].astype(np.float64))

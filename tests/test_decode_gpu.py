@@ -256,17 +256,18 @@ def test_rlgr_golden_vectors_through_gpu_decode(pvvc_lib, oracle, torch):
     assert rgb_matches(rgb, orgb, oyuv).all()
 
 
-def test_host_call_decodes_gops_in_one_plan_identically(pvvc_lib, torch):
+@pytest.mark.parametrize("nframes", [12, 28])
+def test_host_call_decodes_gops_in_one_plan_identically(pvvc_lib, torch, nframes):
     """pvvc_decode_frames_host with slots for one region per GoP decodes all
-    GoPs of a call in one plan; the bytes equal run-by-run decoding (a state
-    with one slot per patch), and so does the next call, which continues the
-    last GoP from the patch slots."""
-    s = pvvc_lib.Synth(pvvc_lib.config("tiny", nframes=12, gof=4, seed=21))
+    GoPs of a call in one plan (3 and 7 GoPs); the bytes equal run-by-run
+    decoding (a state with one slot per patch), and so does the next call,
+    which continues the last GoP from the patch slots."""
+    s = pvvc_lib.Synth(pvvc_lib.config("tiny", nframes=nframes, gof=4, seed=21))
     frames = s.frames()
     nidx = max(int(pvvc_lib.parse_frame(b).index.max()) + 1 for b in frames)
-    merged = pvvc_lib.Decoder(nslots=3 * nidx, max_leaves=4096)
+    merged = pvvc_lib.Decoder(nslots=(nframes // 4) * nidx, max_leaves=4096)
     serial = pvvc_lib.Decoder(nslots=nidx, max_leaves=4096)
-    for part in (frames[:11], frames[11:]):
+    for part in (frames[:nframes - 1], frames[nframes - 1:]):
         a = merged.decode_frames(part)
         b = serial.decode_frames(part)
         assert (a[2] == 0).all() and (b[2] == 0).all()
