@@ -64,6 +64,7 @@ def parse_args():
     ap.add_argument("--no-encode", dest="encode", action="store_false", help="skip the GPU encoder measurement")
     ap.add_argument("--learned-train-pairs", type=int, default=32768, help="pairs to train on when no weights are committed")
     ap.add_argument("--learned-train-epochs", type=int, default=8)
+    ap.add_argument("--no-knn", dest="knn", action="store_false", help="skip the GPU colour-interpolation measurement")
     ap.add_argument("--serve-streams", type=int, default=64, help="playback streams of the serving run (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="real-time length of the serving run")
     return ap.parse_args()
@@ -336,6 +337,7 @@ def run_ours(args):
         icp = measure_icp(args, torch, peak) if args.icp_pairs > 0 else None
         learned = measure_learned(args, torch, pvvc) if args.icp_pairs > 0 and args.learned else None
         encode = measure_encode(args, torch, pvvc, s, len(frames)) if args.encode else None
+        knn = measure_knn_colors(args, torch, pvvc, s) if args.knn else None
         serving = measure_serving(args, pvvc) if args.serve_streams > 0 and args.serve_seconds > 0 else None
         out = {"metric": "decoded Mpts/s (seq300, GoP 30, ~800k pts/frame)", "value": value, "unit": "Mpts/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -343,7 +345,7 @@ def run_ours(args):
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
                "clocks": clk.summary(), "gpu_launches": info["kernels"] * args.steps, "points_per_step": P * world,
                "plan": info, "autotune_ms": tune_ms, "icp": icp, "learned_icp": learned, "encode": encode,
-               "serving": serving}
+               "knn_colors": knn, "serving": serving}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
@@ -390,6 +392,79 @@ def measure_icp(args, torch, peak_gbs):
             "hbm_gbs_one_read": nbytes / (ms / 1e3) / 1e9, "hbm_frac_one_read": nbytes / (ms / 1e3) / 1e9 / peak_gbs,
             "cpu_baseline": {"value": ns / cdt, "unit": "patches/s", "cores": cores, "kind": "port",
                              "sample": f"first {ns} pairs, {cdt:.1f}s"}}
+
+
+def measure_knn_colors(args, torch, pvvc, synth):
+    """GoP encoder colour interpolation (pvvc_knn_colors_batch) on the first
+    GoP of the decode workload: every patch's geometry is the query cloud
+    (the fitting cloud), and each of the 30 frames brings a source patch --
+    the cloud moved by up to a voxel per axis, 10% of points dropped, RGB from
+    the frame's colours -- interpolated with k = 10 (the reference default)
+    and turned into residuals against frame 0.  CPU baseline: the oracle's
+    grid k-NN restatement on a bounded sample of pairs, all host cores."""
+    from pvvc.icp import KnnColorBatch
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import concurrent.futures as cf
+    t0 = time.time()
+    gof = 30
+    npat = synth.patch_count(0)
+
+    def one(p):
+        xyz, yuv, _ = synth.patch(0, p)
+        rng = np.random.default_rng(1000 + p)
+        srcs, cols = [], []
+        for f in range(min(gof, yuv.shape[0])):
+            keep = rng.random(xyz.shape[0]) > 0.1
+            keep[0] = True
+            srcs.append(np.round(xyz[keep] + rng.integers(-1, 2, (int(keep.sum()), 3))).astype(np.float32))
+            c = yuv[0][keep] if f == 0 else yuv[0][keep] + yuv[f][keep]
+            cols.append(np.clip(c, 0, 255).astype(np.uint8))
+        return xyz.astype(np.float32), srcs, cols
+
+    with cf.ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 4)) as ex:
+        parts = list(ex.map(one, range(npat)))
+    queries, query_of, sources, rgbs, base = [], [], [], [], []
+    for p, (xyz, srcs, cols) in enumerate(parts):
+        first = len(sources)
+        for f, (sp, cp) in enumerate(zip(srcs, cols)):
+            query_of.append(p)
+            sources.append(sp)
+            rgbs.append(cp)
+            base.append(-1 if f == 0 else first)
+        queries.append(xyz)
+    b = KnnColorBatch(queries, query_of, sources, rgbs, k=10, base=base)
+    setup = time.time() - t0
+    b.run()
+    _, st = b.results()
+    assert (st == 0).all()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    e0.record()
+    for _ in range(reps):
+        b.run()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    pts = int(b.qn.astype(np.int64).sum())
+    from oracle import Oracle
+    o = Oracle()
+    cores = os.cpu_count() or 1
+    ns = 0
+    c0 = time.perf_counter()
+    cpts = 0
+    while ns < len(sources) and time.perf_counter() - c0 < args.cpu_seconds / 4:
+        m = min(64, len(sources) - ns)
+        o.knn_colors_batch([queries[query_of[i]] for i in range(ns, ns + m)], sources[ns:ns + m], rgbs[ns:ns + m], 10,
+                           cores)
+        cpts += int(sum(queries[query_of[i]].shape[0] for i in range(ns, ns + m)))
+        ns += m
+    cdt = time.perf_counter() - c0
+    log(f"knn colors: {len(sources)} pairs, {pts} points in {ms:.2f} ms (setup {setup:.1f}s)")
+    return {"pairs": len(sources), "query_points": pts, "source_points": b.ns, "k": 10, "ms": ms,
+            "mpts_per_s": pts / (ms / 1e3) / 1e6,
+            "what": "k-NN colour interpolation of one GoP (30 frames x every patch) with frame-0 residuals",
+            "cpu_baseline": {"value": cpts / cdt / 1e6, "unit": "Mpts/s", "cores": cores, "kind": "port",
+                             "sample": f"first {ns} pairs (grid k-NN restatement), {cdt:.1f}s"}}
 
 
 def measure_learned(args, torch, pvvc):
