@@ -1081,6 +1081,25 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
                 }
                 // last internal level: a contiguous node range per warp
                 const int a = s_ls[H - 2], cnt = s_ls[H - 1] - a;
+                // the group's region (every lane's frame shares it) and plane
+                // stride, from lane 0, which always holds a slice
+                const uint64_t g_off = __shfl_sync(0xffffffffu, have ? w.coef_off : 0ull, 0);
+                const uint32_t g_n = __shfl_sync(0xffffffffu, have ? w.n : 0u, 0);
+                const float* const g_coef = coef + g_off;
+                // Node t+1's lines into L1 while node t is transformed: lane
+                // l < 21 takes coefficient line (plane l / 7, coded slot
+                // l % 7), lanes 21-23 the node's three level-signal lines.
+                auto prefetch_node = [&](const NodeRows& r, int t, int jnode) {
+                    const uint32_t nc = __popc(r.mask[t] & 0xFEu);
+                    const float* line = nullptr;
+                    if (lane < 21) {
+                        const uint32_t k = (uint32_t)lane % 7u, pl = (uint32_t)lane / 7u;
+                        if (k < nc) line = g_coef + ((size_t)pl * g_n + r.coff[t] + k) * 32;
+                    } else if (lane < 24) {
+                        line = gA + (size_t)jnode * 96 + (lane - 21) * 32;
+                    }
+                    if (line) asm volatile("prefetch.global.L1 [%0];" ::"l"(line));
+                };
                 const int per = (cnt + kGrpWarps - 1) / kGrpWarps;
                 const int j0 = min(cnt, wid * per), j1 = min(cnt, j0 + per);
                 uint32_t base = 0, staged = 0;
@@ -1101,7 +1120,9 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
                         for (int i = 0; i < 7; ++i) nr.ab[i][lane] = __ldg(ab + i);
                     }
                     __syncwarp();
+                    if (nn > 0) prefetch_node(nr, 0, jb);
                     for (int t = 0; t < nn; ++t) {
+                        if (t + 1 < nn) prefetch_node(nr, t + 1, jb + t + 1);
                         const uint32_t byte = nr.occ[t], cb = nr.cb[t];
                         const uint32_t k = __popc(byte);
                         if (staged + k > (uint32_t)kWarpLeaves) {
