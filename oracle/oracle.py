@@ -35,10 +35,9 @@ def build_oracle(force: bool = False) -> str:
 def build_reference() -> str | None:
     """Compile the reference's own sources against the shims, if the reference
     tree is present on this machine.  Returns the .so path or None."""
-    if os.path.exists(_REF_SO):
-        return _REF_SO
     if not os.path.isdir(os.path.join(REFERENCE_ROOT, "src")):
-        return None
+        return _REF_SO if os.path.exists(_REF_SO) else None
+    # make rebuilds only when a source or a shim changed
     r = subprocess.run(["make", "-s", "-C", _HERE, "ref", f"REF={REFERENCE_ROOT}"], capture_output=True, text=True)
     return _REF_SO if r.returncode == 0 and os.path.exists(_REF_SO) else None
 
@@ -344,11 +343,38 @@ class Reference:
         lib.ref_decoder_set_slice.argtypes = [C.c_void_p, C.c_uint8, C.c_int, C.c_int, C.c_uint64, C.c_uint8, _f32p, _u8p, C.c_size_t, _u8p, C.c_size_t]
         lib.ref_decoder_get_patch.restype = C.c_long
         lib.ref_decoder_get_patch.argtypes = [C.c_void_p, _f32p, _u8p, C.c_size_t]
+        lib.ref_gop_encode.restype = C.c_int
+        lib.ref_gop_encode.argtypes = [_f32p, C.c_size_t, C.c_int, C.POINTER(_f32p), C.POINTER(_u8p),
+                                       C.POINTER(C.c_size_t), C.c_int, C.c_int, C.c_int, _f32p, _u8p, C.c_size_t,
+                                       C.POINTER(C.c_size_t), _u8p, C.c_size_t, C.POINTER(C.c_size_t)]
         lib.ref_save_slice.restype = C.c_int
         lib.ref_save_slice.argtypes = [C.c_char_p, C.c_uint8, C.c_int, C.c_int, C.c_uint64, C.c_uint8, _f32p, _u8p, C.c_size_t, _u8p, C.c_size_t]
         lib.ref_change_slice_to_frame.restype = C.c_int
         lib.ref_change_slice_to_frame.argtypes = [C.c_char_p, C.c_char_p]
 
+
+    def gop_encode(self, fit_xyz, srcs, rgbs, k, qp_i, qp_p):
+        """GoPEncoding::Encode on one patch's GoP (ref_gop_encode): the
+        interpolated colours [nf,n,3] (later frames as residuals), the
+        geometry payload and the raw colour payload of every frame."""
+        fit = np.ascontiguousarray(fit_xyz, np.float32)
+        n, nf = fit.shape[0], len(srcs)
+        srcs = [np.ascontiguousarray(x, np.float32) for x in srcs]
+        rgbs = [np.ascontiguousarray(x, np.uint8) for x in rgbs]
+        sp = (_f32p * nf)(*[_ptr(x, _f32p) for x in srcs])
+        cp = (_u8p * nf)(*[_ptr(x, _u8p) for x in rgbs])
+        sn = (C.c_size_t * nf)(*[x.shape[0] for x in srcs])
+        cols = np.zeros((nf, n, 3), np.float32)
+        geo = np.zeros(64 + 4 * n, np.uint8)
+        pay = np.zeros(nf * (64 + 16 * n), np.uint8)
+        gl = C.c_size_t(0)
+        cl = (C.c_size_t * nf)()
+        rc = self.lib.ref_gop_encode(_ptr(fit, _f32p), n, nf, sp, cp, sn, k, qp_i, qp_p, _ptr(cols, _f32p),
+                                     _ptr(geo, _u8p), geo.size, C.byref(gl), _ptr(pay, _u8p), pay.size, cl)
+        if rc:
+            raise RuntimeError(f"ref_gop_encode {rc}")
+        off = np.concatenate([[0], np.cumsum(list(cl))]).astype(np.int64)
+        return cols, geo[:gl.value].tobytes(), [pay[off[f]:off[f + 1]].tobytes() for f in range(nf)]
     def rlgr_encode(self, sym) -> bytes:
         sym = np.ascontiguousarray(sym, np.int64)
         cap = 16 * sym.size + 64

@@ -17,4 +17,12 @@ struct PointXYZRGB {
 struct Normal {
     float normal_x, normal_y, normal_z, curvature;
 };
+struct PointNormal {
+    float x, y, z, normal_x, normal_y, normal_z, curvature;
+};
+struct PointXYZRGBNormal {
+    float x, y, z;
+    uint8_t r, g, b, a;
+    float normal_x, normal_y, normal_z, curvature;
+};
 }  // namespace pcl

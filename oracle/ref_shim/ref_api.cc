@@ -21,6 +21,21 @@
 #include "io/slice_io.h"
 #include "octree/octree.h"
 
+// GoPEncoding keeps its interpolated colours private: this test driver reads
+// them through a public view of the class declaration (the reference's
+// source is compiled unchanged).  Standard headers first, so that only the
+// reference's declarations see the redefinition.
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <mutex>
+#include <numeric>
+#include <queue>
+#include <thread>
+#define private public
+#include "patch/patch.h"
+#undef private
+
 using namespace vvc;
 
 namespace {
@@ -220,6 +235,83 @@ int ref_save_slice(const char* path, uint8_t type, int timestamp, int index, uin
         if (geo && gsz) s.geometry = std::make_shared<std::vector<uint8_t>>(geo, geo + gsz);
         if (col && csz) s.color = std::make_shared<std::vector<uint8_t>>(col, col + csz);
         return io::SaveSlice(s, path);
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+/* ---- GoPEncoding::Encode (src/patch/GoP_encoding.cc:97-210) on one patch's
+ * GoP: the fitting cloud (n points; its colours are not used) and nf source
+ * patches (xyz + rgb).  k = patch.interpolation_num.  Writes the interpolated
+ * colours patch_colors_ (nf x n x YUV; later frames as residuals), the
+ * geometry payload of slice 0 and each slice's colour payload, zstd undone
+ * where the encoder kept the compressed form.  Returns 0, or -1 / -2. */
+int ref_gop_encode(const float* fit_xyz, size_t n, int nf, const float* const* src_xyz, const uint8_t* const* src_rgb,
+                   const size_t* src_n, int k, int qp_i, int qp_p, float* colors_out, uint8_t* geo_out, size_t geo_cap,
+                   size_t* geo_len, uint8_t* col_out, size_t col_cap, size_t* col_len) {
+    try {
+        auto prm = std::make_shared<common::PVVCParam_t>();
+        prm->octree.resolution = 1.0f;
+        prm->zstd_level = 1;
+        prm->thread_num = 1;
+        prm->patch.interpolation_num = k;
+        prm->slice.qp_i = (uint8_t)qp_i;
+        prm->slice.qp_p = (uint8_t)qp_p;
+        patch::GoPEncoding enc;
+        enc.SetParams(prm);
+        pcl::PointCloud<pcl::PointXYZRGB>::Ptr fit(new pcl::PointCloud<pcl::PointXYZRGB>());
+        fit->resize(n);
+        for (size_t i = 0; i < n; ++i) {
+            (*fit)[i].x = fit_xyz[3 * i];
+            (*fit)[i].y = fit_xyz[3 * i + 1];
+            (*fit)[i].z = fit_xyz[3 * i + 2];
+        }
+        enc.SetFittingCloud(fit);
+        std::vector<common::Patch> pats(nf);
+        for (int f = 0; f < nf; ++f) {
+            pats[f].cloud.reset(new pcl::PointCloud<pcl::PointXYZRGB>());
+            pats[f].cloud->resize(src_n[f]);
+            for (size_t i = 0; i < src_n[f]; ++i) {
+                pcl::PointXYZRGB& q = (*pats[f].cloud)[i];
+                q.x = src_xyz[f][3 * i];
+                q.y = src_xyz[f][3 * i + 1];
+                q.z = src_xyz[f][3 * i + 2];
+                q.r = src_rgb[f][3 * i];
+                q.g = src_rgb[f][3 * i + 1];
+                q.b = src_rgb[f][3 * i + 2];
+            }
+            pats[f].timestamp = f;
+            pats[f].index = 0;
+        }
+        enc.SetSourcePatches(pats);
+        enc.Encode();
+        for (int f = 0; f < nf; ++f)
+            for (size_t i = 0; i < n; ++i) {
+                const common::ColorYUV& c = enc.patch_colors_[f]->at(i);
+                colors_out[(f * n + i) * 3] = c.y;
+                colors_out[(f * n + i) * 3 + 1] = c.u;
+                colors_out[(f * n + i) * 3 + 2] = c.v;
+            }
+        auto raw = [](uint8_t type, uint8_t bit, const std::shared_ptr<std::vector<uint8_t>>& b) {
+            if (!(type & bit)) return *b;
+            common::ZstdDecoder dec;
+            dec.Decode(b);
+            return *dec.GetResult();
+        };
+        std::vector<common::Slice> res = enc.GetResults();
+        const std::vector<uint8_t> geo = raw(res[0].type, 0x08, res[0].geometry);
+        if (geo.size() > geo_cap) return -2;
+        std::memcpy(geo_out, geo.data(), geo.size());
+        *geo_len = geo.size();
+        size_t off = 0;
+        for (int f = 0; f < nf; ++f) {
+            const std::vector<uint8_t> c = raw(res[f].type, 0x10, res[f].color);
+            if (off + c.size() > col_cap) return -2;
+            std::memcpy(col_out + off, c.data(), c.size());
+            col_len[f] = c.size();
+            off += c.size();
+        }
+        return 0;
     } catch (const common::Exception&) {
         return -1;
     }

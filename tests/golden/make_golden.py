@@ -17,6 +17,14 @@ It compiles the reference's sources against the oracle's shim headers
   gop/expected.npz per frame: InvertRAHTOctree::SetSlice/GetPatch output
                    (src/octree/invert_raht_octree.cc:22-120) transformed as
                    pvvc_decompression.cc:141-150 (float32, left to right)
+  gop_encode.npz   GoPEncoding::Encode (src/patch/GoP_encoding.cc:97-210)
+                   on 4 patches x 3 frames: its k-NN colour interpolation
+                   (k = 10; patch_colors_, later frames as residuals), the
+                   geometry payload and each frame's colour payload.  The
+                   k-d tree is the shim's exact search (lower index first
+                   among equal distances).
+
+`python tests/golden/make_golden.py gop_encode` writes only gop_encode.npz.
 
 Patches: 4 from the seeded synthetic surface generator plus 4 edge cases
 (a single point, two distant points, a full 8^3 cube, and points that share
@@ -137,8 +145,48 @@ def edge_patches(rng):
     return pats
 
 
+def make_gop_encode(ref: Reference, seed: int = 41):
+    """Fitting clouds from the synthetic generator; each frame's source patch
+    is the cloud moved by up to a voxel per axis with 10% of points dropped,
+    integer coordinates (many equal distances), random RGB."""
+    import pvvc
+    s = pvvc.Synth(pvvc.config("gof8", nframes=3, gof=3, seed=seed))
+    rng = np.random.default_rng(seed)
+    out = {}
+    fits, srcs, rgbs, cols, geos, pays = [], [], [], [], [], []
+    for p in range(s.patch_count(0)):
+        xyz = s.patch(0, p)[0].astype(np.float32)
+        if xyz.shape[0] > 1200:
+            continue
+        ss, cc = [], []
+        for f in range(3):
+            keep = rng.random(xyz.shape[0]) > 0.1
+            keep[0] = True
+            ss.append(np.round(xyz[keep] + rng.integers(-1, 2, (int(keep.sum()), 3))).astype(np.float32))
+            cc.append(rng.integers(0, 256, (int(keep.sum()), 3)).astype(np.uint8))
+        c, g, pl = ref.gop_encode(xyz, ss, cc, 10, QP_I, QP_P)
+        fits.append(xyz)
+        srcs += ss
+        rgbs += cc
+        cols.append(c.reshape(-1, 3))
+        geos.append(np.frombuffer(g, np.uint8))
+        pays += [np.frombuffer(x, np.uint8) for x in pl]
+        if len(fits) == 4:
+            break
+    cat = lambda xs: np.concatenate(xs) if xs else np.zeros(0)
+    off = lambda xs: np.concatenate([[0], np.cumsum([len(x) for x in xs])]).astype(np.int64)
+    np.savez_compressed(os.path.join(HERE, "gop_encode.npz"), k=10, qp_i=QP_I, qp_p=QP_P, nframes=3,
+                        fit=cat(fits), fit_off=off(fits), src=cat(srcs), src_off=off(srcs), rgb=cat(rgbs),
+                        colors=cat(cols), geo=cat(geos), geo_off=off(geos), pay=cat(pays), pay_off=off(pays))
+
+
 def main():
     ref = Reference()
+    if sys.argv[1:] == ["gop_encode"]:
+        make_gop_encode(ref)
+        print("gop_encode.npz written to", HERE)
+        return
+    make_gop_encode(ref)
     rng = np.random.default_rng(2024)
     make_rlgr(ref, rng)
 

@@ -66,3 +66,37 @@ def test_oracle_knn_colors_known_answers(oracle):
     assert np.isfinite(oracle.knn_colors(src, src, rgb, 16)).all()
     with pytest.raises(RuntimeError):
         oracle.knn_colors(src, src[:0], rgb[:0], 4)
+
+
+def _golden():
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "gop_encode.npz"))
+    nf = int(z["nframes"])
+    fo, so, go, po = z["fit_off"], z["src_off"], z["geo_off"], z["pay_off"]
+    pats = []
+    for p in range(len(fo) - 1):
+        fit = z["fit"][fo[p]:fo[p + 1]].astype(np.float32)
+        n = fit.shape[0]
+        srcs = [z["src"][so[p * nf + f]:so[p * nf + f + 1]].astype(np.float32) for f in range(nf)]
+        rgbs = [z["rgb"][so[p * nf + f]:so[p * nf + f + 1]].astype(np.uint8) for f in range(nf)]
+        base = int(sum(fo[q + 1] - fo[q] for q in range(p))) * nf
+        cols = z["colors"][base:base + nf * n].reshape(nf, n, 3).astype(np.float32)
+        geo = z["geo"][go[p]:go[p + 1]].tobytes()
+        pays = [z["pay"][po[p * nf + f]:po[p * nf + f + 1]].tobytes() for f in range(nf)]
+        pats.append((fit, srcs, rgbs, cols, geo, pays))
+    return int(z["k"]), [int(z["qp_i"])] + [int(z["qp_p"])] * (nf - 1), pats
+
+
+def test_oracle_and_host_encoder_match_reference_gop_encoding(oracle, pvvc_lib):
+    """Pinned against the reference's own GoPEncoding::Encode (golden
+    fixture from tests/golden/make_golden.py, its k-d tree the shim's exact
+    search): the interpolated colours bit for bit, and the host encoder's
+    geometry and colour payloads byte for byte."""
+    k, qps, pats = _golden()
+    for fit, srcs, rgbs, cols, geo, pays in pats:
+        mine = np.stack([oracle.knn_colors(fit, s, c, k) for s, c in zip(srcs, rgbs)])
+        mine[1:] = (mine[1:] - mine[0]).astype(np.float32)  # ColorYUV::operator-= (GoP_encoding.cc:144-148)
+        assert np.array_equal(mine.view(np.uint32), cols.view(np.uint32))
+        g, _, cp = pvvc_lib.encode_patch_gop(fit, mine, qps)
+        assert g == geo
+        assert all(a == b for a, b in zip(cp, pays))

@@ -94,3 +94,29 @@ def test_knn_colors_gpu_small_empty_and_bad_arguments(pvvc_lib, oracle, torch):
     for k in (0, 17):
         with pytest.raises(pvvc_lib.PvvcError):
             KnnColorBatch([q], [0], [small], [c3], k=k).run()
+
+
+def test_knn_colors_gpu_equal_reference_gop_encoding(pvvc_lib, torch):
+    """The GPU's colours equal the reference GoPEncoding::Encode's
+    patch_colors_ (golden fixture), residuals included, bit for bit."""
+    from pvvc.icp import KnnColorBatch
+    from test_knn_colors import _golden
+    k, _, pats = _golden()
+    queries, query_of, sources, rgbs, base = [], [], [], [], []
+    for p, (fit, srcs, rg, _, _, _) in enumerate(pats):
+        first = len(sources)
+        for f, (s, c) in enumerate(zip(srcs, rg)):
+            query_of.append(p)
+            sources.append(s)
+            rgbs.append(c)
+            base.append(-1 if f == 0 else first)
+        queries.append(fit)
+    b = KnnColorBatch(queries, query_of, sources, rgbs, k=k, base=base)
+    b.run()
+    got, st = b.results()
+    assert (st == 0).all()
+    i = 0
+    for fit, srcs, _, cols, _, _ in pats:
+        for f in range(len(srcs)):
+            assert np.array_equal(got[i].view(np.uint32), cols[f].view(np.uint32)), (i, f)
+            i += 1
