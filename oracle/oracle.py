@@ -343,6 +343,8 @@ class Reference:
         lib.ref_decoder_set_slice.argtypes = [C.c_void_p, C.c_uint8, C.c_int, C.c_int, C.c_uint64, C.c_uint8, _f32p, _u8p, C.c_size_t, _u8p, C.c_size_t]
         lib.ref_decoder_get_patch.restype = C.c_long
         lib.ref_decoder_get_patch.argtypes = [C.c_void_p, _f32p, _u8p, C.c_size_t]
+        lib.ref_cloud_mse.restype = C.c_float
+        lib.ref_cloud_mse.argtypes = [_f32p, C.c_size_t, _f32p, C.c_size_t]
         lib.ref_gop_encode.restype = C.c_int
         lib.ref_gop_encode.argtypes = [_f32p, C.c_size_t, C.c_int, C.POINTER(_f32p), C.POINTER(_u8p),
                                        C.POINTER(C.c_size_t), C.c_int, C.c_int, C.c_int, _f32p, _u8p, C.c_size_t,
@@ -352,6 +354,12 @@ class Reference:
         lib.ref_change_slice_to_frame.restype = C.c_int
         lib.ref_change_slice_to_frame.argtypes = [C.c_char_p, C.c_char_p]
 
+
+    def cloud_mse(self, a, b) -> float:
+        """ICPBase::CloudMSE of cloud a (transformed source) against b."""
+        a = np.ascontiguousarray(a, np.float32)
+        b = np.ascontiguousarray(b, np.float32)
+        return float(self.lib.ref_cloud_mse(_ptr(a, _f32p), a.shape[0], _ptr(b, _f32p), b.shape[0]))
 
     def gop_encode(self, fit_xyz, srcs, rgbs, k, qp_i, qp_p):
         """GoPEncoding::Encode on one patch's GoP (ref_gop_encode): the

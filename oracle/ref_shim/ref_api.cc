@@ -317,6 +317,38 @@ int ref_gop_encode(const float* fit_xyz, size_t n, int nf, const float* const* s
     }
 }
 
+/* ---- ICPBase::CloudMSE (src/registration/registration_base.cc:114-158) of
+ * cloud a (the transformed source) against cloud b (the target); a derived
+ * class with an empty Align reaches the protected result cloud.  Returns the
+ * MSE, or -1 on an empty cloud. */
+namespace {
+struct CloudMSEProbe : registration::ICPBase {
+    void Align() override {}
+    void SetResult(pcl::PointCloud<pcl::PointXYZRGB>::Ptr c) { result_cloud_ = c; }
+};
+pcl::PointCloud<pcl::PointXYZRGB>::Ptr make_cloud(const float* xyz, size_t n) {
+    pcl::PointCloud<pcl::PointXYZRGB>::Ptr c(new pcl::PointCloud<pcl::PointXYZRGB>());
+    c->resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        (*c)[i].x = xyz[3 * i];
+        (*c)[i].y = xyz[3 * i + 1];
+        (*c)[i].z = xyz[3 * i + 2];
+    }
+    return c;
+}
+}  // namespace
+
+float ref_cloud_mse(const float* a, size_t na, const float* b, size_t nb) {
+    try {
+        CloudMSEProbe r;
+        r.SetResult(make_cloud(a, na));
+        r.SetTargetCloud(make_cloud(b, nb));
+        return r.CloudMSE();
+    } catch (const common::Exception&) {
+        return -1.0f;
+    }
+}
+
 int ref_change_slice_to_frame(const char* dir, const char* out_name) {
     try {
         io::ChangeSliceToFrame(dir, out_name);

@@ -24,7 +24,12 @@ It compiles the reference's sources against the oracle's shim headers
                    k-d tree is the shim's exact search (lower index first
                    among equal distances).
 
-`python tests/golden/make_golden.py gop_encode` writes only gop_encode.npz.
+  cloud_mse.npz    ICPBase::CloudMSE (src/registration/registration_base.cc:
+                   114-158) of 6 cloud pairs (its k-d tree the shim's exact
+                   search; the sums in float, in point order).
+
+`python tests/golden/make_golden.py gop_encode` (or `cloud_mse`) writes only
+that fixture.
 
 Patches: 4 from the seeded synthetic surface generator plus 4 edge cases
 (a single point, two distant points, a full 8^3 cube, and points that share
@@ -180,13 +185,37 @@ def make_gop_encode(ref: Reference, seed: int = 41):
                         colors=cat(cols), geo=cat(geos), geo_off=off(geos), pay=cat(pays), pay_off=off(pays))
 
 
+def make_cloud_mse(ref: Reference, seed: int = 43):
+    """Voxel clouds against each other, and synthetic patches against a
+    rotated, shifted and jittered copy (the registration's use)."""
+    import pvvc
+    rng = np.random.default_rng(seed)
+    a_list, b_list = [], []
+    for _ in range(3):
+        a_list.append(rng.integers(0, 40, (int(rng.integers(50, 900)), 3)).astype(np.float32))
+        b_list.append(rng.integers(0, 40, (int(rng.integers(50, 900)), 3)).astype(np.float32))
+    s = pvvc.Synth(pvvc.config("gof8", nframes=1, gof=1, seed=seed))
+    for p in range(3):
+        x = s.patch(0, p)[0].astype(np.float32)
+        R = rot(rng.normal(size=3), 5.0)
+        y = ((x - x.mean(0)) @ R.T + x.mean(0) + rng.uniform(-2, 2, 3) + rng.normal(0, 0.5, x.shape)).astype(np.float32)
+        a_list.append(x)
+        b_list.append(y)
+    mse = np.array([ref.cloud_mse(a, b) for a, b in zip(a_list, b_list)], np.float32)
+    off = lambda xs: np.concatenate([[0], np.cumsum([len(x) for x in xs])]).astype(np.int64)
+    np.savez_compressed(os.path.join(HERE, "cloud_mse.npz"), a=np.concatenate(a_list), a_off=off(a_list),
+                        b=np.concatenate(b_list), b_off=off(b_list), mse=mse)
+
+
 def main():
     ref = Reference()
-    if sys.argv[1:] == ["gop_encode"]:
-        make_gop_encode(ref)
-        print("gop_encode.npz written to", HERE)
+    one = {"gop_encode": make_gop_encode, "cloud_mse": make_cloud_mse}
+    if len(sys.argv) == 2 and sys.argv[1] in one:
+        one[sys.argv[1]](ref)
+        print(sys.argv[1] + ".npz written to", HERE)
         return
     make_gop_encode(ref)
+    make_cloud_mse(ref)
     rng = np.random.default_rng(2024)
     make_rlgr(ref, rng)
 

@@ -45,6 +45,36 @@ def test_oracle_cloud_mse_identity_is_zero(oracle):
     assert abs(oracle.cloud_mse(a, b) - 3.0) < 1e-5 or oracle.cloud_mse(a, b) <= 3.0
 
 
+CLOUD_MSE_RTOL = 1e-5  # the reference sums float distances in point order; the oracle (double) and GPU (compensated) do not
+
+
+def _cloud_mse_golden():
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "cloud_mse.npz"))
+    ao, bo = z["a_off"], z["b_off"]
+    return [(z["a"][ao[i]:ao[i + 1]], z["b"][bo[i]:bo[i + 1]], float(z["mse"][i])) for i in range(len(z["mse"]))]
+
+
+def test_oracle_cloud_mse_matches_reference(oracle):
+    """Pinned against the reference's own ICPBase::CloudMSE (golden fixture
+    from tests/golden/make_golden.py)."""
+    for a, b, want in _cloud_mse_golden():
+        got = oracle.cloud_mse(a, b)
+        assert abs(got - want) <= CLOUD_MSE_RTOL * want, (got, want)
+
+
+@pytest.mark.gpu
+def test_gpu_cloud_mse_matches_reference(pvvc_lib):
+    import torch
+    from pvvc.icp import IcpBatch, Pairs
+    cases = _cloud_mse_golden()
+    b = IcpBatch(Pairs([c[0] for c in cases], [c[1] for c in cases], np.repeat(np.eye(4)[None], len(cases), 0)))
+    T = torch.from_numpy(np.tile(np.eye(4, dtype=np.float32).reshape(16), (len(cases), 1))).cuda()
+    got = b.cloud_mse(T)
+    for i, (_, _, want) in enumerate(cases):
+        assert abs(got[i] - want) <= CLOUD_MSE_RTOL * want, (i, got[i], want)
+
+
 @pytest.mark.gpu
 def test_gpu_icp_matches_oracle(pvvc_lib, oracle):
     import torch
