@@ -761,11 +761,12 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     StageClock clk;
     for (double& v : g_stage_ms) v = 0;
     // parse (io::LoadFrame) and inflate zstd on the host, frames in parallel
-    std::vector<Frame> frames(nframes);
+    // the payloads stay in the caller's bytes until they are packed
+    std::vector<FrameView> frames(nframes);
     std::vector<int> prc(nframes, PVVC_OK);
     parallel_for(nframes, threads, [&](int f) {
-        prc[f] = parse_frame(frame_bytes[f], frame_len[f], &frames[f]);
-        if (!prc[f]) prc[f] = frame_inflate(&frames[f]);
+        prc[f] = parse_frame_view(frame_bytes[f], frame_len[f], &frames[f]);
+        if (!prc[f]) prc[f] = frame_view_inflate(&frames[f]);
     });
     for (int r : prc)
         if (r) return r;
@@ -793,8 +794,8 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
                 qp[k] = fr.qp[i];
                 size[k] = fr.size[i];
                 std::memcpy(&mv[16ull * k], &fr.mv[16 * i], 64);
-                gsz[k] = (uint32_t)fr.geometry[i].size();
-                csz[k] = (uint32_t)fr.color[i].size();
+                gsz[k] = fr.gsz[i];
+                csz[k] = fr.csz[i];
                 goff[k] = bytes;
                 bytes = align_up(bytes + gsz[k], 4);
                 coff[k] = bytes;
@@ -808,16 +809,13 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (st->h_payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     uint8_t* hp = static_cast<uint8_t*>(st->h_payload.p);
     parallel_for(nframes, threads, [&](int f) {
-        Frame& fr = frames[f];
+        FrameView& fr = frames[f];
         for (size_t i = 0; i < fr.count(); ++i) {
             const int32_t k = ffirst[f] + (int32_t)i;
-            if (gsz[k]) std::memcpy(hp + goff[k], fr.geometry[i].data(), gsz[k]);
-            if (csz[k]) std::memcpy(hp + coff[k], fr.color[i].data(), csz[k]);
+            if (gsz[k]) std::memcpy(hp + goff[k], fr.geo[i], gsz[k]);
+            if (csz[k]) std::memcpy(hp + coff[k], fr.col[i], csz[k]);
         }
-        // the payload bytes are packed: free this frame's per-slice buffers
-        // here, in parallel, rather than all of them on return
-        std::vector<std::vector<uint8_t>>().swap(fr.geometry);
-        std::vector<std::vector<uint8_t>>().swap(fr.color);
+        std::vector<std::vector<uint8_t>>().swap(fr.owned);  // inflated payloads, now packed
     });
     std::memset(hp + bytes, 0, 16);  // the decoder reads whole 16-byte blocks
     // Intra slices of different frames of one call may hit the same patch

@@ -234,6 +234,69 @@ int zstd_compress(const uint8_t* src, size_t n, int level, std::vector<uint8_t>*
     return PVVC_OK;
 }
 
+int parse_frame_view(const uint8_t* p, size_t len, FrameView* f) {
+    Reader r{p, len};
+    f->timestamp = r.get<int32_t>();
+    uint32_t n = r.get<uint32_t>();
+    if (!r.ok) return PVVC_ERR_FORMAT;
+    if (static_cast<uint64_t>(n) * 82ull > len) return PVVC_ERR_FORMAT;
+    f->index.resize(n);
+    f->type.resize(n);
+    f->size.resize(n);
+    f->qp.resize(n);
+    f->mv.resize(16ull * n);
+    f->geo.assign(n, nullptr);
+    f->col.assign(n, nullptr);
+    f->gsz.assign(n, 0);
+    f->csz.assign(n, 0);
+    f->owned.clear();
+    for (uint32_t i = 0; i < n; ++i) f->index[i] = r.get<int32_t>();
+    for (uint32_t i = 0; i < n; ++i) f->type[i] = r.get<uint8_t>();
+    for (uint32_t i = 0; i < n; ++i) f->size[i] = r.get<uint32_t>();
+    for (uint32_t i = 0; i < n; ++i) f->qp[i] = r.get<uint8_t>();
+    for (uint64_t i = 0; i < 16ull * n; ++i) f->mv[i] = r.get<float>();
+    auto span = [&](uint32_t sz, const uint8_t** at) {
+        if (sz > len - r.pos || r.pos > len) return false;
+        *at = p + r.pos;
+        r.pos += sz;
+        return true;
+    };
+    for (uint32_t i = 0; i < n; ++i) f->gsz[i] = r.get<uint32_t>();
+    if (!r.ok) return PVVC_ERR_FORMAT;
+    for (uint32_t i = 0; i < n; ++i)
+        if (f->gsz[i] && !span(f->gsz[i], &f->geo[i])) return PVVC_ERR_FORMAT;
+    for (uint32_t i = 0; i < n; ++i) f->csz[i] = r.get<uint32_t>();
+    if (!r.ok) return PVVC_ERR_FORMAT;
+    for (uint32_t i = 0; i < n; ++i)
+        if (f->csz[i] && !span(f->csz[i], &f->col[i])) return PVVC_ERR_FORMAT;
+    return PVVC_OK;
+}
+
+int frame_view_inflate(FrameView* f) {
+    auto inflate = [&](const uint8_t** at, uint32_t* sz) {
+        std::vector<uint8_t> t;
+        const int s = zstd_decompress(*at, *sz, &t);
+        if (s) return s;
+        if (t.size() > 0xFFFFFFFFull) return (int)PVVC_ERR_ZSTD;
+        f->owned.emplace_back(std::move(t));  // moving keeps the buffer where it is
+        *at = f->owned.back().data();
+        *sz = (uint32_t)f->owned.back().size();
+        return (int)PVVC_OK;
+    };
+    for (size_t i = 0; i < f->count(); ++i) {
+        if ((f->type[i] & kTypeGeoZstd) && f->gsz[i]) {
+            const int s = inflate(&f->geo[i], &f->gsz[i]);
+            if (s) return s;
+        }
+        if ((f->type[i] & kTypeColorZstd) && f->csz[i]) {
+            const int s = inflate(&f->col[i], &f->csz[i]);
+            if (s) return s;
+        }
+        f->type[i] &= static_cast<uint8_t>(~(kTypeGeoZstd | kTypeColorZstd));
+    }
+    return PVVC_OK;
+}
+
 int frame_inflate(Frame* f) {
     for (size_t i = 0; i < f->count(); ++i) {
         if ((f->type[i] & kTypeGeoZstd) && !f->geometry[i].empty()) {

@@ -52,12 +52,32 @@ struct Frame {
     size_t count() const { return index.size(); }
 };
 
+// A parsed .frame whose slice payloads point into the parsed bytes (no
+// copies); payloads inflated from zstd live in `owned` and point there.
+// Valid while those bytes live.
+struct FrameView {
+    int32_t timestamp = -1;
+    std::vector<int32_t> index;
+    std::vector<uint8_t> type;
+    std::vector<uint32_t> size;
+    std::vector<uint8_t> qp;
+    std::vector<float> mv;
+    std::vector<const uint8_t*> geo, col;
+    std::vector<uint32_t> gsz, csz;
+    std::vector<std::vector<uint8_t>> owned;
+    size_t count() const { return index.size(); }
+};
+
 // Serialise / parse.  Parsers return 0 or a PVVC_ERR_* status and never read
 // past `len`.
 std::vector<uint8_t> write_slice(const Slice& s);
 int parse_slice(const uint8_t* p, size_t len, Slice* out);
 std::vector<uint8_t> write_frame(const Frame& f);
 int parse_frame(const uint8_t* p, size_t len, Frame* out);
+// parse_frame's checks, the payloads left in place
+int parse_frame_view(const uint8_t* p, size_t len, FrameView* out);
+// zstd payloads of a view inflated into its `owned` buffers, flags cleared
+int frame_view_inflate(FrameView* f);
 
 // Frame from slices sorted by patch index (ChangeSliceToFrame, slice_io.cc:208-322).
 Frame frame_from_slices(std::vector<Slice> slices);
