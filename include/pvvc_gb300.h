@@ -185,10 +185,10 @@ int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* cons
                             int32_t* status_host, int32_t status_cap, void* stream);
 /* Wall-clock milliseconds of the stages of the calling thread's last
  * pvvc_decode_frames_host (no counterpart in the reference):
- * out[0] parse + inflate, out[1] payload packing and the batch description,
- * out[2] planning (host) and plan upload, out[3] H2D + decode + D2H up to the
- * final stream synchronisation.  Fills min(n, 4) values; zeros before any
- * call. */
+ * out[0] parse + inflate, out[1] the batch description and the split into
+ * runs, out[2] planning (host) and plan upload, with the payload packed into
+ * pinned memory beside it, out[3] H2D + decode + D2H up to the final stream
+ * synchronisation.  Fills min(n, 4) values; zeros before any call. */
 int pvvc_host_stage_times(double* out, int32_t n);
 
 /* ---- reference-signature shim --------------------------------------------

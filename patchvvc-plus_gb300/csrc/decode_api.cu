@@ -808,16 +808,34 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (pts > cap_points || (status_host && status_cap < nsl)) return PVVC_ERR_CAPACITY;
     if (st->h_payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     uint8_t* hp = static_cast<uint8_t*>(st->h_payload.p);
-    parallel_for(nframes, threads, [&](int f) {
-        FrameView& fr = frames[f];
-        for (size_t i = 0; i < fr.count(); ++i) {
-            const int32_t k = ffirst[f] + (int32_t)i;
-            if (gsz[k]) std::memcpy(hp + goff[k], fr.geo[i], gsz[k]);
-            if (csz[k]) std::memcpy(hp + coff[k], fr.col[i], csz[k]);
-        }
-        std::vector<std::vector<uint8_t>>().swap(fr.owned);  // inflated payloads, now packed
-    });
     std::memset(hp + bytes, 0, 16);  // the decoder reads whole 16-byte blocks
+    // The payload bytes go into pinned memory on helper threads while this
+    // thread splits the call into runs and builds the first plan; the copy
+    // to the device waits for them.
+    std::thread packer([&] {
+        parallel_for(nframes, std::max(1, threads / 2), [&](int f) {
+            FrameView& fr = frames[f];
+            for (size_t i = 0; i < fr.count(); ++i) {
+                const int32_t k = ffirst[f] + (int32_t)i;
+                if (gsz[k]) std::memcpy(hp + goff[k], fr.geo[i], gsz[k]);
+                if (csz[k]) std::memcpy(hp + coff[k], fr.col[i], csz[k]);
+            }
+            std::vector<std::vector<uint8_t>>().swap(fr.owned);  // inflated payloads, now packed
+        });
+    });
+    struct JoinOnExit {
+        std::thread& t;
+        ~JoinOnExit() {
+            if (t.joinable()) t.join();
+        }
+    } join_packer{packer};
+    bool sent = false;
+    auto send_payload = [&]() -> bool {  // once: the packed payload to the device
+        if (sent) return true;
+        sent = true;
+        packer.join();
+        return !bytes || cudaMemcpyAsync(st->payload.p, hp, bytes + 16, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    };
     // Intra slices of different frames of one call may hit the same patch
     // index (a new GoP).  Split the call into runs of frames without a
     // repeated intra index.
@@ -876,8 +894,6 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
-    if (bytes && cudaMemcpyAsync(st->payload.p, hp, bytes + 16, cudaMemcpyHostToDevice, s) != cudaSuccess)
-        return PVVC_ERR_CUDA;
     int rc = PVVC_OK;
     const std::vector<int32_t> one_run{0, nsl};
     const std::vector<int32_t>& runs = merge ? one_run : bounds;
@@ -890,6 +906,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         rc = build_plan(&d, &st->plan, nullptr, nullptr);
         if (rc) break;
         if (st->ws.ensure(st->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
+        if (!send_payload()) return PVVC_ERR_CUDA;
         g_stage_ms[2] += clk.lap();
         rc = run_decode(&st->plan, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
                         static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
