@@ -3,17 +3,21 @@
 //
 //   C[M,N] = epilogue( A[M,K] . B[N,K]^T )     A, B bf16, K contiguous
 //
-// One CTA computes one 128 x BN tile of C (BN = 64, 128 or 256) over a
-// range of K (split-K over gridDim.z).  Four warps:
+// Persistent CTAs (one per SM for BN = 256) walk the 128 x BN tiles of C
+// (BN = 64, 128 or 256; split-K over a third tile index).  Six warps:
 //   warp 0, lane 0   TMA producer: 128x64 A and BNx64 B tiles (128-byte
-//                    swizzle) into a 4-stage shared-memory ring, completion
-//                    counted on the stage's `full` mbarrier
+//                    swizzle) into a 4-stage shared-memory ring that runs on
+//                    across tiles, completion counted on the stage's `full`
+//                    mbarrier
 //   warp 1, lane 0   MMA issuer: tcgen05.mma kind::f16 (M=128, N=BN, K=16)
-//                    four per stage into an FP32 accumulator in tensor
-//                    memory; tcgen05.commit frees the stage (`empty`) and,
-//                    after the last stage, signals `done`
-//   warps 0-3        epilogue: tcgen05.ld of the warp's 32 accumulator lanes
-//                    (one C row per thread), bias / ReLU / mask, store
+//                    four per stage into one of two FP32 accumulators in
+//                    tensor memory (2*BN columns); tcgen05.commit frees the
+//                    stage (`empty`) and, after a tile's last stage, marks
+//                    its accumulator full
+//   warps 2-5        epilogue: tcgen05.ld of the warp's 32 accumulator lanes
+//                    (one C row per thread), bias / ReLU / mask, store; then
+//                    the accumulator is released to the MMA issuer
+// so a tile's loads and MMAs overlap the previous tile's stores.
 // Every mbarrier wait is bounded; a wait that gives up sets the device error
 // word (read by pvvc_device_error_take) and the CTA skips the rest of its
 // work instead of hanging.
@@ -21,6 +25,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 
@@ -99,6 +104,10 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b
         : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
@@ -128,149 +137,185 @@ struct EpiArgs {
     int64_t ldaux;
 };
 
-// Shared memory of a CTA: `stages` (1..kStages) A and B tiles, 1024-byte
-// aligned as the 128-byte swizzle wants, then the barriers.  A GEMM with
-// fewer K blocks than kStages gets a shorter ring, so that more CTAs fit on
-// an SM (the network's GEMMs have K of 64..512).
 constexpr int kTileA = kBM * kBK * 2;  // 16 KB
+
+// Epilogue of one 128 x BN tile: this thread's accumulator row (TMEM lane
+// `tl`'s columns) through bias / ReLU / mask into C row `row`.  A warp
+// instruction (tcgen05.ld): every lane of the warp calls it.
+template <int BN, int EPI>
+__device__ __forceinline__ void epilogue_row(uint32_t tl, int row, int M, int n0, const EpiArgs& ep) {
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tl + c0, v);
+        if (row >= M) continue;
+        const int col = n0 + c0;
+        if (EPI == PVVC_GEMM_BIAS_RELU_BF16 || EPI == PVVC_GEMM_MASK_BF16) {
+            __nv_bfloat16* out = static_cast<__nv_bfloat16*>(ep.C) + (int64_t)row * ep.ldc + col;
+            if (EPI == PVVC_GEMM_BIAS_RELU_BF16) {
+#pragma unroll
+                for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + (ep.bias ? ep.bias[col + j] : 0.f), 0.f);
+            } else {
+                const uint4* ax = reinterpret_cast<const uint4*>(ep.aux + (int64_t)row * ep.ldaux + col);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const uint4 w = ax[q];
+                    const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&w);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        if (!(__bfloat162float(h[j]) > 0.f)) v[q * 8 + j] = 0.f;
+                }
+            }
+            uint4* o4 = reinterpret_cast<uint4*>(out);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                __nv_bfloat162 p[4];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) p[j] = __floats2bfloat162_rn(v[q * 8 + 2 * j], v[q * 8 + 2 * j + 1]);
+                o4[q] = *reinterpret_cast<uint4*>(p);
+            }
+        } else {
+            float* out = static_cast<float*>(ep.C) + (int64_t)row * ep.ldc + col;
+            if (EPI == PVVC_GEMM_F32) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    float4 f;
+                    f.x = v[4 * q] + (ep.bias ? ep.bias[col + 4 * q] : 0.f);
+                    f.y = v[4 * q + 1] + (ep.bias ? ep.bias[col + 4 * q + 1] : 0.f);
+                    f.z = v[4 * q + 2] + (ep.bias ? ep.bias[col + 4 * q + 2] : 0.f);
+                    f.w = v[4 * q + 3] + (ep.bias ? ep.bias[col + 4 * q + 3] : 0.f);
+                    reinterpret_cast<float4*>(out)[q] = f;
+                }
+            } else {  // PVVC_GEMM_F32_ACCUM
+#pragma unroll
+                for (int j = 0; j < 32; ++j) atomicAdd(out + j, v[j]);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent form: gridDim.x CTAs (one per SM for BN = 256) walk the tiles
+// t = blockIdx.x, blockIdx.x + gridDim.x, ... (m-tile fastest, then n-tile,
+// then the K split).  Six warps:
+//   warp 0, lane 0   TMA producer; its kStages ring runs on across tiles
+//   warp 1           allocates 2*BN TMEM columns (two accumulators); lane 0
+//                    issues tile u's MMAs into accumulator u & 1 once the
+//                    epilogue has released it (acc_empty), then commits
+//                    acc_full
+//   warps 2-5        epilogue: warp w drains TMEM lanes 32*(w % 4).. of the
+//                    full accumulator, stores its rows, releases it
+// so the loads and MMAs of the next tile run while a tile's rows are stored.
 template <int BN>
-struct GemmBars {
-    uint64_t full[kStages], empty[kStages], done;
+struct PersistBars {
+    uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2];
     uint32_t tmem_base;
 };
 template <int BN>
-__host__ __device__ constexpr size_t gemm_smem_bytes(int stages) {
-    return 1024 + (size_t)stages * (kTileA + BN * kBK * 2) + sizeof(GemmBars<BN>);
+__host__ __device__ constexpr size_t persist_smem_bytes() {
+    return 1024 + (size_t)kStages * (kTileA + BN * kBK * 2) + sizeof(PersistBars<BN>);
 }
-template <int BN>
-struct GemmSmem {
-    uint8_t* base;
-    int stages;
-    __device__ __forceinline__ void* a(int s) const { return base + (size_t)s * kTileA; }
-    __device__ __forceinline__ void* b(int s) const { return base + (size_t)stages * kTileA + (size_t)s * BN * kBK * 2; }
-    __device__ __forceinline__ GemmBars<BN>& bars() const {
-        return *reinterpret_cast<GemmBars<BN>*>(base + (size_t)stages * (kTileA + BN * kBK * 2));
-    }
-};
+constexpr int kPersistThreads = 192;
 
 template <int BN, int EPI>
-__global__ void __launch_bounds__(128, 1)
-    k_gemm_bf16_tn(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M, int K,
-                   int kb_per_split, int stages, EpiArgs ep) {
+__global__ void __launch_bounds__(kPersistThreads, 1)
+    k_gemm_bf16_tn_persist(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int M,
+                           int K, int mtiles, int ntiles, int splits, int kb_per_split, EpiArgs ep) {
     extern __shared__ uint8_t smem_raw[];
-    const GemmSmem<BN> L{reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023)),
-                         stages};
-    GemmBars<BN>& sm = L.bars();
+    uint8_t* const base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    PersistBars<BN>& sm = *reinterpret_cast<PersistBars<BN>*>(base + (size_t)kStages * (kTileA + BN * kBK * 2));
+    auto tile_a = [&](uint32_t st) { return base + (size_t)st * kTileA; };
+    auto tile_b = [&](uint32_t st) { return base + (size_t)kStages * kTileA + (size_t)st * BN * kBK * 2; };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
     const int nkb = K / kBK;
-    const int kb0 = blockIdx.z * kb_per_split;
-    const int kb1 = min(nkb, kb0 + kb_per_split);
-    if (kb0 >= kb1) return;  // uniform over the CTA
-
+    const int ntiles_all = mtiles * ntiles * splits;
+    auto tile_of = [&](int t, int& m0, int& n0, int& kb0, int& kb1) {
+        const int mt = t % mtiles, r = t / mtiles;
+        m0 = mt * kBM;
+        n0 = (r % ntiles) * BN;
+        kb0 = (r / ntiles) * kb_per_split;
+        kb1 = min(nkb, kb0 + kb_per_split);
+    };
     if (threadIdx.x == 0) {
-        for (int s = 0; s < stages; ++s) {
-            mbar_init(&sm.full[s], 1);
-            mbar_init(&sm.empty[s], 1);
+        for (int st = 0; st < kStages; ++st) {
+            mbar_init(&sm.full[st], 1);
+            mbar_init(&sm.empty[st], 1);
         }
-        mbar_init(&sm.done, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&sm.acc_full[b], 1);
+            mbar_init(&sm.acc_empty[b], 4);  // one arrive per epilogue warp
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
-    if (warp == 0) {  // the whole warp allocates BN accumulator columns
+    if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
-                     "r"(BN));
+                     "r"(2 * BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = sm.tmem_base;
-    bool ok = true;
-
-    if (threadIdx.x == 0) {  // producer
-        for (int kb = kb0; kb < kb1 && ok; ++kb) {
-            const int i = kb - kb0, s = i % stages;
-            if (!(ok = mbar_wait(&sm.empty[s], ((i / stages) & 1) ^ 1, 1))) break;
-            mbar_expect_tx(&sm.full[s], (kBM + BN) * kBK * 2);
-            tma_load_2d(L.a(s), &map_a, &sm.full[s], kb * kBK, m0);
-            tma_load_2d(L.b(s), &map_b, &sm.full[s], kb * kBK, n0);
-        }
-    } else if (threadIdx.x == 32) {  // MMA issuer
-        constexpr uint32_t idesc = idesc_bf16(kBM, BN);
-        for (int kb = kb0; kb < kb1 && ok; ++kb) {
-            const int i = kb - kb0, s = i % stages;
-            if (!(ok = mbar_wait(&sm.full[s], (i / stages) & 1, 2))) break;
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint64_t da = smem_desc_sw128(smem_u32(L.a(s)));
-            const uint64_t db = smem_desc_sw128(smem_u32(L.b(s)));
-#pragma unroll
-            for (int k = 0; k < kBK / 16; ++k)  // +32 bytes per K=16 step inside the swizzle row
-                mma_bf16(tmem, da + 2 * k, db + 2 * k, idesc, (i > 0 || k > 0) ? 1u : 0u);
-            mma_commit(&sm.empty[s]);
-        }
-        mma_commit(&sm.done);  // fires when every MMA issued above has completed
-    }
-    __syncwarp();
-    // epilogue: all four warps
-    // warp-uniform: tcgen05.ld below is a .sync.aligned warp instruction
-    const bool done_ok = __all_sync(0xffffffffu, mbar_wait(&sm.done, 0, 3));
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (done_ok) {
-        const int row = m0 + warp * 32 + lane;
-        const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 32) {
-            float v[32];
-            tmem_ld32(tl + c0, v);
-            if (row >= M) continue;
-            const int col = n0 + c0;
-            if (EPI == PVVC_GEMM_BIAS_RELU_BF16 || EPI == PVVC_GEMM_MASK_BF16) {
-                __nv_bfloat16* out = static_cast<__nv_bfloat16*>(ep.C) + (int64_t)row * ep.ldc + col;
-                if (EPI == PVVC_GEMM_BIAS_RELU_BF16) {
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + (ep.bias ? ep.bias[col + j] : 0.f), 0.f);
-                } else {
-                    const uint4* ax = reinterpret_cast<const uint4*>(ep.aux + (int64_t)row * ep.ldaux + col);
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint4 w = ax[q];
-                        const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&w);
-#pragma unroll
-                        for (int j = 0; j < 8; ++j)
-                            if (!(__bfloat162float(h[j]) > 0.f)) v[q * 8 + j] = 0.f;
-                    }
-                }
-                uint4* o4 = reinterpret_cast<uint4*>(out);
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    __nv_bfloat162 p[4];
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) p[j] = __floats2bfloat162_rn(v[q * 8 + 2 * j], v[q * 8 + 2 * j + 1]);
-                    o4[q] = *reinterpret_cast<uint4*>(p);
-                }
-            } else {
-                float* out = static_cast<float*>(ep.C) + (int64_t)row * ep.ldc + col;
-                if (EPI == PVVC_GEMM_F32) {
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) {
-                        float4 f;
-                        f.x = v[4 * q] + (ep.bias ? ep.bias[col + 4 * q] : 0.f);
-                        f.y = v[4 * q + 1] + (ep.bias ? ep.bias[col + 4 * q + 1] : 0.f);
-                        f.z = v[4 * q + 2] + (ep.bias ? ep.bias[col + 4 * q + 2] : 0.f);
-                        f.w = v[4 * q + 3] + (ep.bias ? ep.bias[col + 4 * q + 3] : 0.f);
-                        reinterpret_cast<float4*>(out)[q] = f;
-                    }
-                } else {  // PVVC_GEMM_F32_ACCUM
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) atomicAdd(out + j, v[j]);
+    int m0, n0, kb0, kb1;
+    if (warp == 0) {
+        if (lane == 0) {  // producer
+            bool ok = true;
+            uint32_t it = 0;
+            for (int t = blockIdx.x; t < ntiles_all && ok; t += gridDim.x) {
+                tile_of(t, m0, n0, kb0, kb1);
+                for (int kb = kb0; kb < kb1; ++kb, ++it) {
+                    const uint32_t st = it % kStages, ph = (it / kStages) & 1;
+                    if (!(ok = mbar_wait(&sm.empty[st], ph ^ 1, 1))) break;
+                    mbar_expect_tx(&sm.full[st], (kBM + BN) * kBK * 2);
+                    tma_load_2d(tile_a(st), &map_a, &sm.full[st], kb * kBK, m0);
+                    tma_load_2d(tile_b(st), &map_b, &sm.full[st], kb * kBK, n0);
                 }
             }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            constexpr uint32_t idesc = idesc_bf16(kBM, BN);
+            bool ok = true;
+            uint32_t it = 0, u = 0;
+            for (int t = blockIdx.x; t < ntiles_all && ok; t += gridDim.x, ++u) {
+                tile_of(t, m0, n0, kb0, kb1);
+                const uint32_t b = u & 1, use = u >> 1;
+                if (!(ok = mbar_wait(&sm.acc_empty[b], (use & 1) ^ 1, 4))) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc = tmem + b * BN;
+                for (int kb = kb0; kb < kb1; ++kb, ++it) {
+                    const uint32_t st = it % kStages, ph = (it / kStages) & 1;
+                    if (!(ok = mbar_wait(&sm.full[st], ph, 2))) break;
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint64_t da = smem_desc_sw128(smem_u32(tile_a(st)));
+                    const uint64_t db = smem_desc_sw128(smem_u32(tile_b(st)));
+#pragma unroll
+                    for (int k = 0; k < kBK / 16; ++k)  // +32 bytes per K=16 step inside the swizzle row
+                        mma_bf16(acc, da + 2 * k, db + 2 * k, idesc, (kb > kb0 || k > 0) ? 1u : 0u);
+                    mma_commit(&sm.empty[st]);
+                }
+                if (ok) mma_commit(&sm.acc_full[b]);  // fires when the tile's MMAs have completed
+            }
+        }
+    } else {  // epilogue warps 2..5
+        const int q = warp & 3;  // the TMEM lane quarter this warp may read
+        uint32_t u = 0;
+        for (int t = blockIdx.x; t < ntiles_all; t += gridDim.x, ++u) {
+            tile_of(t, m0, n0, kb0, kb1);
+            const uint32_t b = u & 1, use = u >> 1;
+            // warp-uniform: tcgen05.ld in the epilogue is a .sync.aligned warp instruction
+            if (!__all_sync(0xffffffffu, mbar_wait(&sm.acc_full[b], use & 1, 3))) break;
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            epilogue_row<BN, EPI>(tmem + b * BN + ((uint32_t)(q * 32) << 16), m0 + q * 32 + lane, M, n0, ep);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.acc_empty[b]);
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+    if (warp == 1) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN));
 }
 
 // ---- host ----------------------------------------------------------------
@@ -307,19 +352,34 @@ bool make_map(CUtensorMap* m, const void* base, int64_t rows, int64_t K, int64_t
 template <int BN, int EPI>
 cudaError_t launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int K, int splits, const EpiArgs& ep,
                       cudaStream_t s) {
+    // once per instantiation: the shared-memory opt-in and how many CTAs fit
+    // on an SM (two accumulators of BN columns each must fit the 512 TMEM
+    // columns of all resident CTAs)
     static std::once_flag once;
     static cudaError_t attr = cudaSuccess;
+    static int per_sm = 1;
     std::call_once(once, [&] {
-        attr = cudaFuncSetAttribute(k_gemm_bf16_tn<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)gemm_smem_bytes<BN>(kStages));
+        attr = cudaFuncSetAttribute(k_gemm_bf16_tn_persist<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)persist_smem_bytes<BN>());
+        int occ = 0;
+        if (attr == cudaSuccess)
+            attr = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_gemm_bf16_tn_persist<BN, EPI>, kPersistThreads,
+                                                                 persist_smem_bytes<BN>());
+        per_sm = std::max(1, std::min(occ, 512 / (2 * BN)));
     });
     if (attr != cudaSuccess) return attr;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
     const int nkb = K / kBK;
     const int per = (nkb + splits - 1) / splits;
     const int z = (nkb + per - 1) / per;
-    const int stages = per < kStages ? per : kStages;  // K blocks one CTA walks
-    dim3 grid((M + kBM - 1) / kBM, N / BN, z);
-    k_gemm_bf16_tn<BN, EPI><<<grid, 128, gemm_smem_bytes<BN>(stages), s>>>(ma, mb, M, K, per, stages, ep);
+    const int mtiles = (M + kBM - 1) / kBM, ntiles = N / BN;
+    const long long tiles = (long long)mtiles * ntiles * z;
+    const int grid = (int)std::min<long long>(tiles, (long long)sms * per_sm);
+    k_gemm_bf16_tn_persist<BN, EPI><<<grid, kPersistThreads, persist_smem_bytes<BN>(), s>>>(ma, mb, M, K, mtiles, ntiles, z,
+                                                                                            per, ep);
     return cudaGetLastError();
 }
 
