@@ -6,7 +6,7 @@
 // Persistent CTAs (one per SM for BN = 256) walk the 128 x BN tiles of C
 // (BN = 64, 128 or 256; split-K over a third tile index).  Six warps:
 //   warp 0, lane 0   TMA producer: 128x64 A and BNx64 B tiles (128-byte
-//                    swizzle) into a 4-stage shared-memory ring that runs on
+//                    swizzle) into a 3- to 7-stage shared-memory ring that runs on
 //                    across tiles, completion counted on the stage's `full`
 //                    mbarrier
 //   warp 1, lane 0   MMA issuer: tcgen05.mma kind::f16 (M=128, N=BN, K=16)
@@ -14,9 +14,10 @@
 //                    tensor memory (2*BN columns); tcgen05.commit frees the
 //                    stage (`empty`) and, after a tile's last stage, marks
 //                    its accumulator full
-//   warps 2-5        epilogue: tcgen05.ld of the warp's 32 accumulator lanes
-//                    (one C row per thread), bias / ReLU / mask, store; then
-//                    the accumulator is released to the MMA issuer
+//   warps 2-9        epilogue: two warps per 32-lane TMEM quarter, each with
+//                    half the columns: tcgen05.ld (one C row per thread),
+//                    bias / ReLU / mask, store; then the accumulator is
+//                    released to the MMA issuer
 // so a tile's loads and MMAs overlap the previous tile's stores.
 // Every mbarrier wait is bounded; a wait that gives up sets the device error
 // word (read by pvvc_device_error_take) and the CTA skips the rest of its
@@ -34,7 +35,7 @@
 namespace pvvc {
 namespace {
 
-constexpr int kBM = 128, kBK = 64, kStages = 4;
+constexpr int kBM = 128, kBK = 64, kStages = 8;  // kStages: the most ring stages of any tile width
 constexpr uint32_t kSpinLimit = 1u << 26;  // ~seconds of try_wait polling
 
 __device__ int g_tc_error;  // nonzero: a bounded wait gave up (first code wins)
@@ -143,9 +144,9 @@ constexpr int kTileA = kBM * kBK * 2;  // 16 KB
 // `tl`'s columns) through bias / ReLU / mask into C row `row`.  A warp
 // instruction (tcgen05.ld): every lane of the warp calls it.
 template <int BN, int EPI>
-__device__ __forceinline__ void epilogue_row(uint32_t tl, int row, int M, int n0, const EpiArgs& ep) {
+__device__ __forceinline__ void epilogue_row(uint32_t tl, int row, int M, int n0, int cbeg, int cend, const EpiArgs& ep) {
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
+    for (int c0 = cbeg; c0 < cend; c0 += 32) {
         float v[32];
         tmem_ld32(tl + c0, v);
         if (row >= M) continue;
@@ -194,28 +195,88 @@ __device__ __forceinline__ void epilogue_row(uint32_t tl, int row, int M, int n0
     }
 }
 
+// Epilogue of one warp's 32 rows (row0 + lane) of a bf16 tile: 64 columns at
+// a time go through the warp's shared-memory buffer (32 rows x 8 chunks of
+// 16 bytes, chunk j of row r at j ^ (r & 7), so that neither the row-wise
+// writes nor the column-wise reads conflict), then out as full 128-byte row
+// segments, four rows per store instruction.  Other epilogues store by row.
+template <int BN, int EPI>
+__device__ __forceinline__ void epilogue_warp(uint32_t tl, int row0, int M, int n0, int cbeg, int cend, const EpiArgs& ep,
+                                              uint4* stage) {
+    const int lane = threadIdx.x & 31, row = row0 + lane;
+    if constexpr (EPI == PVVC_GEMM_BIAS_RELU_BF16 || EPI == PVVC_GEMM_MASK_BF16) {
+#pragma unroll 1
+        for (int c0 = cbeg; c0 < cend; c0 += 64) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float v[32];
+                tmem_ld32(tl + c0 + 32 * h, v);
+                const int col = n0 + c0 + 32 * h;
+                if (EPI == PVVC_GEMM_BIAS_RELU_BF16) {
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + (ep.bias ? ep.bias[col + j] : 0.f), 0.f);
+                } else if (row < M) {
+                    const uint4* ax = reinterpret_cast<const uint4*>(ep.aux + (int64_t)row * ep.ldaux + col);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        const uint4 w = ax[q];
+                        const __nv_bfloat16* hb = reinterpret_cast<const __nv_bfloat16*>(&w);
+#pragma unroll
+                        for (int j = 0; j < 8; ++j)
+                            if (!(__bfloat162float(hb[j]) > 0.f)) v[q * 8 + j] = 0.f;
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    __nv_bfloat162 pk[4];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) pk[j] = __floats2bfloat162_rn(v[q * 8 + 2 * j], v[q * 8 + 2 * j + 1]);
+                    stage[lane * 8 + ((4 * h + q) ^ (lane & 7))] = *reinterpret_cast<uint4*>(pk);
+                }
+            }
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int r = i * 4 + (lane >> 3), ch = lane & 7;
+                const uint4 val = stage[r * 8 + (ch ^ (r & 7))];
+                if (row0 + r < M)
+                    *reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(ep.C) + (int64_t)(row0 + r) * ep.ldc + n0 + c0 +
+                                              ch * 8) = val;
+            }
+            __syncwarp();
+        }
+    } else {
+        epilogue_row<BN, EPI>(tl, row, M, n0, cbeg, cend, ep);
+    }
+}
+
 // ---------------------------------------------------------------------------
-// Persistent form: gridDim.x CTAs (one per SM for BN = 256) walk the tiles
-// t = blockIdx.x, blockIdx.x + gridDim.x, ... (m-tile fastest, then n-tile,
-// then the K split).  Six warps:
-//   warp 0, lane 0   TMA producer; its kStages ring runs on across tiles
-//   warp 1           allocates 2*BN TMEM columns (two accumulators); lane 0
-//                    issues tile u's MMAs into accumulator u & 1 once the
-//                    epilogue has released it (acc_empty), then commits
-//                    acc_full
-//   warps 2-5        epilogue: warp w drains TMEM lanes 32*(w % 4).. of the
-//                    full accumulator, stores its rows, releases it
-// so the loads and MMAs of the next tile run while a tile's rows are stored.
+// The persistent kernel (roles in the file header).  CTA c takes tiles c,
+// c + gridDim.x, ... (m-tile fastest, then n-tile, then the K split); its
+// accumulator u & 1 holds its u-th tile.
+// ring depth: as many stages as fit beside the eight staging buffers, so
+// that narrow tiles (whose GEMMs are long K loops) keep more bytes in flight
+template <int BN>
+__host__ __device__ constexpr int persist_stages() {
+    return BN == 256 ? 3 : (BN == 128 ? 5 : 7);
+}
 template <int BN>
 struct PersistBars {
     uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2];
     uint32_t tmem_base;
 };
+constexpr int kStageChunks = 32 * 8;  // one epilogue warp's staging buffer, 16-byte chunks
+constexpr int kEpiWarps = 8;          // two per TMEM lane quarter, each draining half the columns
+template <int BN>
+__host__ __device__ constexpr size_t persist_bars_bytes() {
+    return (sizeof(PersistBars<BN>) + 15) / 16 * 16;
+}
 template <int BN>
 __host__ __device__ constexpr size_t persist_smem_bytes() {
-    return 1024 + (size_t)kStages * (kTileA + BN * kBK * 2) + sizeof(PersistBars<BN>);
+    return 1024 + (size_t)persist_stages<BN>() * (kTileA + BN * kBK * 2) + persist_bars_bytes<BN>() +
+           kEpiWarps * kStageChunks * 16;
 }
-constexpr int kPersistThreads = 192;
+constexpr int kPersistThreads = 64 + 32 * kEpiWarps;
 
 template <int BN, int EPI>
 __global__ void __launch_bounds__(kPersistThreads, 1)
@@ -223,9 +284,11 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
                            int K, int mtiles, int ntiles, int splits, int kb_per_split, EpiArgs ep) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* const base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    PersistBars<BN>& sm = *reinterpret_cast<PersistBars<BN>*>(base + (size_t)kStages * (kTileA + BN * kBK * 2));
+    constexpr int S = persist_stages<BN>();
+    PersistBars<BN>& sm = *reinterpret_cast<PersistBars<BN>*>(base + (size_t)S * (kTileA + BN * kBK * 2));
+    uint4* const stage = reinterpret_cast<uint4*>(reinterpret_cast<uint8_t*>(&sm) + persist_bars_bytes<BN>());
     auto tile_a = [&](uint32_t st) { return base + (size_t)st * kTileA; };
-    auto tile_b = [&](uint32_t st) { return base + (size_t)kStages * kTileA + (size_t)st * BN * kBK * 2; };
+    auto tile_b = [&](uint32_t st) { return base + (size_t)S * kTileA + (size_t)st * BN * kBK * 2; };
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int nkb = K / kBK;
     const int ntiles_all = mtiles * ntiles * splits;
@@ -237,13 +300,13 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
         kb1 = min(nkb, kb0 + kb_per_split);
     };
     if (threadIdx.x == 0) {
-        for (int st = 0; st < kStages; ++st) {
+        for (int st = 0; st < S; ++st) {
             mbar_init(&sm.full[st], 1);
             mbar_init(&sm.empty[st], 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&sm.acc_full[b], 1);
-            mbar_init(&sm.acc_empty[b], 4);  // one arrive per epilogue warp
+            mbar_init(&sm.acc_empty[b], kEpiWarps);  // one arrive per epilogue warp
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -265,7 +328,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
             for (int t = blockIdx.x; t < ntiles_all && ok; t += gridDim.x) {
                 tile_of(t, m0, n0, kb0, kb1);
                 for (int kb = kb0; kb < kb1; ++kb, ++it) {
-                    const uint32_t st = it % kStages, ph = (it / kStages) & 1;
+                    const uint32_t st = it % S, ph = (it / S) & 1;
                     if (!(ok = mbar_wait(&sm.empty[st], ph ^ 1, 1))) break;
                     mbar_expect_tx(&sm.full[st], (kBM + BN) * kBK * 2);
                     tma_load_2d(tile_a(st), &map_a, &sm.full[st], kb * kBK, m0);
@@ -285,7 +348,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 const uint32_t acc = tmem + b * BN;
                 for (int kb = kb0; kb < kb1; ++kb, ++it) {
-                    const uint32_t st = it % kStages, ph = (it / kStages) & 1;
+                    const uint32_t st = it % S, ph = (it / S) & 1;
                     if (!(ok = mbar_wait(&sm.full[st], ph, 2))) break;
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                     const uint64_t da = smem_desc_sw128(smem_u32(tile_a(st)));
@@ -298,8 +361,11 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
                 if (ok) mma_commit(&sm.acc_full[b]);  // fires when the tile's MMAs have completed
             }
         }
-    } else {  // epilogue warps 2..5
+    } else {  // epilogue warps 2..9
         const int q = warp & 3;  // the TMEM lane quarter this warp may read
+        const int half = (warp - 2) >> 2;
+        // its half of the columns (BN = 64: the first warp of each quarter takes all)
+        const int cbeg = BN >= 128 ? half * (BN / 2) : 0, cend = BN >= 128 ? cbeg + BN / 2 : (half ? 0 : BN);
         uint32_t u = 0;
         for (int t = blockIdx.x; t < ntiles_all; t += gridDim.x, ++u) {
             tile_of(t, m0, n0, kb0, kb1);
@@ -307,7 +373,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
             // warp-uniform: tcgen05.ld in the epilogue is a .sync.aligned warp instruction
             if (!__all_sync(0xffffffffu, mbar_wait(&sm.acc_full[b], use & 1, 3))) break;
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            epilogue_row<BN, EPI>(tmem + b * BN + ((uint32_t)(q * 32) << 16), m0 + q * 32 + lane, M, n0, ep);
+            epilogue_warp<BN, EPI>(tmem + b * BN + ((uint32_t)(q * 32) << 16), m0 + q * 32, M, n0, cbeg, cend, ep,
+                                   stage + (warp - 2) * kStageChunks);
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(&sm.acc_empty[b]);
