@@ -252,6 +252,69 @@ __global__ void k_transpose(const __nv_bfloat16* __restrict__ in, int64_t R, int
     }
 }
 
+// out[C,R] = in[R,C]^T for even R and C: 64x64 tiles, each thread moving
+// bf16 pairs, so that a warp reads and writes 128 contiguous bytes per row.
+// part (optional): the tile's column sums, part[blockIdx.y * C + c], for
+// k_colsum_parts.
+__global__ void __launch_bounds__(256) k_transpose_pairs(const __nv_bfloat16* __restrict__ in, int64_t R, int64_t C,
+                                                         __nv_bfloat16* __restrict__ out, float* __restrict__ part) {
+    __shared__ __nv_bfloat16 t[64][66];  // odd word stride: column reads spread over the banks
+    __shared__ float red[8][64];
+    const int64_t r0 = blockIdx.y * 64ll, c0 = blockIdx.x * 64ll;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    float s0 = 0.f, s1 = 0.f;
+    for (int i = ty; i < 64; i += 8) {
+        const int64_t r = r0 + i, c = c0 + 2 * tx;
+        __nv_bfloat162 v = __floats2bfloat162_rn(0.f, 0.f);
+        if (r < R && c < C) v = *reinterpret_cast<const __nv_bfloat162*>(in + r * C + c);
+        t[i][2 * tx] = v.x;
+        t[i][2 * tx + 1] = v.y;
+        s0 += __bfloat162float(v.x);
+        s1 += __bfloat162float(v.y);
+    }
+    if (part) {
+        red[ty][2 * tx] = s0;
+        red[ty][2 * tx + 1] = s1;
+    }
+    __syncthreads();
+    if (part && ty == 0) {
+        for (int h = 0; h < 2; ++h) {
+            const int64_t c = c0 + 2 * tx + h;
+            float a = 0.f;
+            for (int y = 0; y < 8; ++y) a += red[y][2 * tx + h];
+            if (c < C) part[blockIdx.y * C + c] = a;
+        }
+    }
+    for (int i = ty; i < 64; i += 8) {
+        const int64_t c = c0 + i, r = r0 + 2 * tx;
+        if (c < C && r < R) {
+            __nv_bfloat162 v;
+            v.x = t[2 * tx][i];
+            v.y = t[2 * tx + 1][i];
+            *reinterpret_cast<__nv_bfloat162*>(out + c * R + r) = v;
+        }
+    }
+}
+
+// g[c] += sum over r of part[r * C + c]: 32 columns x 8 row phases per
+// block, `rows_per_block` rows per block, one atomic per column per block
+__global__ void __launch_bounds__(256) k_colsum_parts(const float* __restrict__ part, int64_t nrows, int C,
+                                                      int64_t rows_per_block, float* __restrict__ g) {
+    __shared__ float red[8][32];
+    const int c = blockIdx.x * 32 + threadIdx.x;
+    const int64_t r0 = blockIdx.y * rows_per_block, r1 = min(nrows, r0 + rows_per_block);
+    float a = 0.f;
+    if (c < C)
+        for (int64_t r = r0 + threadIdx.y; r < r1; r += 8) a += part[r * C + c];
+    red[threadIdx.y][threadIdx.x] = a;
+    __syncthreads();
+    if (threadIdx.y == 0 && c < C) {
+        float t = 0.f;
+        for (int y = 0; y < 8; ++y) t += red[y][threadIdx.x];
+        atomicAdd(g + c, t);
+    }
+}
+
 // g[c] += sum over rows of in[r, c] (bf16 in, fp32 partial sums per block)
 __global__ void k_colsum(const __nv_bfloat16* __restrict__ in, int64_t R, int C, int64_t rows_per_block,
                          float* __restrict__ g) {
@@ -272,11 +335,13 @@ __device__ __forceinline__ float pooled_grad(const float* dh0, const __nv_bfloat
 }
 
 // dW3[n, :] = sum over clouds of g(c, n) X2[argmax(c, n), :];  db3[n] = sum g.
-// One channel per block, one input feature per thread.  Clouds go in chunks:
-// the chunk's gradients and argmax rows are staged in shared memory by
-// independent loads, then the X2 rows are gathered kGather at a time, so the
-// loads overlap; the sums still run over the clouds in order.
+// One channel and one of kPoolParts cloud ranges per block, one input
+// feature per thread; the ranges' sums are combined by atomics.  Clouds go
+// in chunks: the chunk's gradients and argmax rows are staged in shared
+// memory by independent loads, then the X2 rows are gathered kGather at a
+// time, so the loads overlap.
 constexpr int kPoolChunk = 1024;
+constexpr int kPoolParts = 4;  // cloud ranges per channel (k_pool_bwd_w3's grid.y)
 constexpr int kGather = 8;
 __global__ void __launch_bounds__(kD2) k_pool_bwd_w3(int nclouds, const float* __restrict__ dh0,
                                                     const __nv_bfloat16* __restrict__ h0, const int32_t* __restrict__ amax,
@@ -285,9 +350,12 @@ __global__ void __launch_bounds__(kD2) k_pool_bwd_w3(int nclouds, const float* _
     __shared__ float s_g[kPoolChunk];
     __shared__ int32_t s_row[kPoolChunk];  // argmax row within the cloud
     const int n = blockIdx.x, k = threadIdx.x;
+    // this block's share of the clouds: gridDim.y parts, combined by atomics
+    const int per = (nclouds + gridDim.y - 1) / gridDim.y;
+    const int cbeg = blockIdx.y * per, cend = min(nclouds, cbeg + per);
     float acc = 0.f, accb = 0.f;
-    for (int c0 = 0; c0 < nclouds; c0 += kPoolChunk) {
-        const int cn = min(kPoolChunk, nclouds - c0);
+    for (int c0 = cbeg; c0 < cend; c0 += kPoolChunk) {
+        const int cn = min(kPoolChunk, cend - c0);
         __syncthreads();
         for (int i = k; i < cn; i += kD2) {
             s_g[i] = pooled_grad(dh0, h0, c0 + i, n);
@@ -314,8 +382,8 @@ __global__ void __launch_bounds__(kD2) k_pool_bwd_w3(int nclouds, const float* _
             }
         }
     }
-    gw3[n * kD2 + k] += acc;
-    if (k == 0) gb3[n] += accb;
+    atomicAdd(gw3 + n * kD2 + k, acc);
+    if (k == 0) atomicAdd(gb3 + n, accb);
 }
 
 // dY2 = (sum over channels n of g(c, n) W3[n, :] scattered to row argmax(c, n))
@@ -323,11 +391,11 @@ __global__ void __launch_bounds__(kD2) k_pool_bwd_w3(int nclouds, const float* _
 // channels with a gradient are bucketed by their argmax row (a stable
 // counting sort: channel order kept within a row); then each row's 128
 // outputs are summed over its bucket in channel order and written at once,
-// zero rows included.
+// zero rows included, as column pairs (four rows per pass).
 __global__ void __launch_bounds__(256) k_pool_bwd_x2(const float* __restrict__ dh0, const __nv_bfloat16* __restrict__ h0,
                                                     const int32_t* __restrict__ amax, const __nv_bfloat16* __restrict__ w3,
                                                     const __nv_bfloat16* __restrict__ x2, __nv_bfloat16* __restrict__ dy2) {
-    static_assert(kD3 == 256 && kP == 256 && kD2 == 128, "one thread per channel and per row, two rows per pass");
+    static_assert(kD3 == 256 && kP == 256 && kD2 == 128, "one thread per channel and per row; 64 column pairs x 4 rows per pass");
     __shared__ float s_g[kD3];
     __shared__ int32_t s_row[kD3];
     __shared__ int32_t s_start[kP + 1];  // bucket of row r: s_list[s_start[r] .. s_start[r + 1])
@@ -362,17 +430,22 @@ __global__ void __launch_bounds__(256) k_pool_bwd_x2(const float* __restrict__ d
         s_list[s_start[s_row[t]] + rank] = t;
     }
     __syncthreads();
-    const int k = t & (kD2 - 1), half = t >> 7;
+    // column pair kp of rows r0 + quarter: a warp moves 128 contiguous bytes
+    const int kp = t & (kD2 / 2 - 1), quarter = t >> 6;
     const int64_t base = (int64_t)c * kP;
-    for (int r0 = 0; r0 < kP; r0 += 2) {
-        const int row = r0 + half;
-        float acc = 0.f;
+    for (int r0 = 0; r0 < kP; r0 += 4) {
+        const int row = r0 + quarter;
+        float a0 = 0.f, a1 = 0.f;
         for (int j = s_start[row]; j < s_start[row + 1]; ++j) {
             const int n = s_list[j];
-            acc += s_g[n] * __bfloat162float(w3[n * kD2 + k]);
+            const __nv_bfloat162 w = *reinterpret_cast<const __nv_bfloat162*>(w3 + n * kD2 + 2 * kp);
+            a0 += s_g[n] * __bfloat162float(w.x);
+            a1 += s_g[n] * __bfloat162float(w.y);
         }
-        const int64_t idx = (base + row) * kD2 + k;
-        dy2[idx] = __float2bfloat16_rn(__bfloat162float(x2[idx]) > 0.f ? acc : 0.f);
+        const int64_t idx = (base + row) * kD2 + 2 * kp;
+        const __nv_bfloat162 xv = *reinterpret_cast<const __nv_bfloat162*>(x2 + idx);
+        *reinterpret_cast<__nv_bfloat162*>(dy2 + idx) = __floats2bfloat162_rn(__bfloat162float(xv.x) > 0.f ? a0 : 0.f,
+                                                                               __bfloat162float(xv.y) > 0.f ? a1 : 0.f);
     }
 }
 
@@ -383,6 +456,7 @@ __global__ void __launch_bounds__(256) k_bwd_w1(const __nv_bfloat16* __restrict_
     const int o = threadIdx.x & 63, ph = threadIdx.x >> 6;
     const int64_t r0 = blockIdx.x * rows_per_block, r1 = min(R, r0 + rows_per_block);
     float a0 = 0.f, a1 = 0.f, a2 = 0.f, ab = 0.f;
+#pragma unroll 4
     for (int64_t r = r0 + ph; r < r1; r += 4) {
         const float d = __bfloat162float(dy1[r * kD1 + o]);
         a0 += d * x0[3 * r];
@@ -481,6 +555,7 @@ struct pvvc_regnet {
     // activations and scratch for up to `cap` pairs
     int64_t cap = 0;
     DevBuf x0, x1, x2, y3, h0, amax, h1, h2, out, frame, y, dh2, dh1, dh0, dy2, dy1, ta, tb, loss, ids;
+    DevBuf part;  // column sums of dY2 per 64-row tile (the db2 reduction)
 };
 
 namespace {
@@ -503,7 +578,8 @@ int ensure_cap(pvvc_regnet* n, int64_t B) {
               n->dh1.ensure(2 * B * kH1) == cudaSuccess && n->dh0.ensure(4 * B * kH0) == cudaSuccess &&
               n->dy2.ensure(2 * M * kD2) == cudaSuccess && n->dy1.ensure(2 * M * kD1) == cudaSuccess &&
               n->ta.ensure(2 * M * kD2) == cudaSuccess && n->tb.ensure(2 * M * kD1 + 2 * B * kH0) == cudaSuccess &&
-              n->loss.ensure(16) == cudaSuccess && n->ids.ensure(4 * B) == cudaSuccess;
+              n->loss.ensure(16) == cudaSuccess && n->ids.ensure(4 * B) == cudaSuccess &&
+              n->part.ensure(4 * ((M + 63) / 64) * kD2) == cudaSuccess;
     if (!ok) return PVVC_ERR_NOMEM;
     n->cap = B;
     return PVVC_OK;
@@ -554,12 +630,29 @@ int forward_from_x1(pvvc_regnet* n, int64_t B, const float* y, float lambda_w, b
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }
 
-// dW += dY^T X over `rows` rows: transposes into scratch, then a split-K GEMM
+// dW += dY^T X over `rows` rows: transposes into scratch, then a split-K GEMM.
+// With gb and part (scratch of ceil(rows/64) * dout floats) and even sizes,
+// the transpose of dY also yields db += column sums of dY.
 int weight_grad(int64_t rows, int dout, int din, const __nv_bfloat16* dy, const __nv_bfloat16* x, __nv_bfloat16* dyT,
-                __nv_bfloat16* xT, float* gw, cudaStream_t s) {
-    dim3 blk(32, 8);
-    k_transpose<<<dim3((dout + 31) / 32, (unsigned)((rows + 31) / 32)), blk, 0, s>>>(dy, rows, dout, dyT);
-    k_transpose<<<dim3((din + 31) / 32, (unsigned)((rows + 31) / 32)), blk, 0, s>>>(x, rows, din, xT);
+                __nv_bfloat16* xT, float* gw, cudaStream_t s, float* gb = nullptr, float* part = nullptr) {
+    const bool pairs = rows % 2 == 0 && dout % 2 == 0 && din % 2 == 0;
+    auto transpose = [&](const __nv_bfloat16* in, int cols, __nv_bfloat16* out, float* prt) {
+        dim3 blk(32, 8);
+        if (pairs)
+            k_transpose_pairs<<<dim3((cols + 63) / 64, (unsigned)((rows + 63) / 64)), blk, 0, s>>>(in, rows, cols, out, prt);
+        else
+            k_transpose<<<dim3((cols + 31) / 32, (unsigned)((rows + 31) / 32)), blk, 0, s>>>(in, rows, cols, out);
+    };
+    const bool fused_db = gb && part && pairs;
+    transpose(dy, dout, dyT, fused_db ? part : nullptr);
+    if (fused_db) {
+        const int64_t nparts = (rows + 63) / 64, per = 128;
+        k_colsum_parts<<<dim3((dout + 31) / 32, (unsigned)((nparts + per - 1) / per)), dim3(32, 8), 0, s>>>(part, nparts, dout,
+                                                                                                         per, gb);
+    } else if (gb) {
+        k_colsum<<<(unsigned)((rows + 1023) / 1024), 128, 0, s>>>(dy, rows, dout, 1024, gb);
+    }
+    transpose(x, din, xT, nullptr);
     const int nkb = (int)(rows / 64);
     const int splits = std::max(1, std::min(nkb, 2 * sm_count() / std::max(1, (dout + 127) / 128)));
     return gemm_bf16(dout, din, (int32_t)rows, dyT, rows, xT, rows, gw, din, nullptr, nullptr, 0, PVVC_GEMM_F32_ACCUM,
@@ -584,18 +677,18 @@ int backward(pvvc_regnet* n, int64_t B, cudaStream_t s) {
                         1, s)))
         return rc;
     // max-pool + layer 3 (sparse): dW3, db3, dY2
-    k_pool_bwd_w3<<<kD3, kD2, 0, s>>>((int)(2 * B), F32(dh0), BF(h0), static_cast<int32_t*>(n->amax.p), BF(x2), g + kL.w3,
+    k_pool_bwd_w3<<<dim3(kD3, kPoolParts), kD2, 0, s>>>((int)(2 * B), F32(dh0), BF(h0), static_cast<int32_t*>(n->amax.p), BF(x2), g + kL.w3,
                                       g + kL.b3);
     k_pool_bwd_x2<<<(unsigned)(2 * B), 256, 0, s>>>(F32(dh0), BF(h0), static_cast<int32_t*>(n->amax.p),
                                                                             BF(w3b), BF(x2), BF(dy2));
     // layer 2: dW2, db2, dY1
-    if ((rc = weight_grad(M, kD2, kD1, BF(dy2), BF(x1), BF(ta), BF(tb), g + kL.w2, s))) return rc;
-    k_colsum<<<(unsigned)((M + 1023) / 1024), 128, 0, s>>>(BF(dy2), M, kD2, 1024, g + kL.b2);
+    if ((rc = weight_grad(M, kD2, kD1, BF(dy2), BF(x1), BF(ta), BF(tb), g + kL.w2, s, g + kL.b2, F32(part))))
+        return rc;
     if ((rc = gemm_bf16((int32_t)M, kD1, kD2, BF(dy2), kD2, BF(w2t), kD2, BF(dy1), kD1, nullptr, BF(x1), kD1,
                         PVVC_GEMM_MASK_BF16, 1, s)))
         return rc;
     // layer 1
-    k_bwd_w1<<<(unsigned)((M + 2047) / 2048), 256, 0, s>>>(BF(dy1), F32(x0), M, 2048, g + kL.w1, g + kL.b1);
+    k_bwd_w1<<<(unsigned)((M + 511) / 512), 256, 0, s>>>(BF(dy1), F32(x0), M, 512, g + kL.w1, g + kL.b1);
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }
 
