@@ -137,24 +137,48 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         w.qp = d->qp[i];
         for (int k = 0; k < 12; ++k) w.mv[k] = d->mv[16ull * i + k];
     };
+    // Chunks of the queue in parallel; each also sums its slices' fallback
+    // buffers (6 floats per point of a slice above kRahtWcap leaves) and
+    // its output extent, and the offsets follow from a prefix over chunks.
     constexpr int kFillChunk = 4096;
-    if (n < 2 * kFillChunk) {
-        for (int q = 0; q < n; ++q) fill(q);
-    } else {
-        parallel_for((n + kFillChunk - 1) / kFillChunk, host_threads(), [&](int c) {
-            for (int q = c * kFillChunk, e = std::min(n, q + kFillChunk); q < e; ++q) fill(q);
-        });
-    }
-    for (int q = 0; q < n; ++q) {  // fallback-buffer offsets and the output extent, in queue order
-        SliceWork& w = p->work[q];
-        if (w.n > (uint32_t)kRahtWcap) {
-            w.fb_off = fb;
-            fb += 6ull * w.n;
-        } else {
-            w.fb_off = ~0ull;
+    const int nch = (n + kFillChunk - 1) / kFillChunk;
+    std::vector<uint64_t> ch_fb(nch + 1, 0), ch_pts(nch, 0);
+    auto fill_chunk = [&](int c) {
+        uint64_t f = 0, m = 0;
+        for (int q = c * kFillChunk, e = std::min(n, q + kFillChunk); q < e; ++q) {
+            fill(q);
+            const SliceWork& w = p->work[q];
+            if (w.n > (uint32_t)kRahtWcap) f += 6ull * w.n;
+            m = std::max<uint64_t>(m, w.out_off + w.n);
         }
-        pts = std::max<uint64_t>(pts, w.out_off + w.n);
+        ch_fb[c + 1] = f;
+        ch_pts[c] = m;
+    };
+    if (nch < 2)
+        for (int c = 0; c < nch; ++c) fill_chunk(c);
+    else
+        parallel_for(nch, host_threads(), fill_chunk);
+    for (int c = 0; c < nch; ++c) {
+        ch_fb[c + 1] += ch_fb[c];
+        pts = std::max(pts, ch_pts[c]);
     }
+    fb = ch_fb[nch];
+    auto fb_chunk = [&](int c) {  // fallback-buffer offsets, in queue order from the chunk's base
+        uint64_t f = ch_fb[c];
+        for (int q = c * kFillChunk, e = std::min(n, q + kFillChunk); q < e; ++q) {
+            SliceWork& w = p->work[q];
+            if (w.n > (uint32_t)kRahtWcap) {
+                w.fb_off = f;
+                f += 6ull * w.n;
+            } else {
+                w.fb_off = ~0ull;
+            }
+        }
+    };
+    if (nch < 2)
+        for (int c = 0; c < nch; ++c) fb_chunk(c);
+    else
+        parallel_for(nch, host_threads(), fb_chunk);
     p->total_points = pts;
     // RLGR order: all slices by size, so that a warp decodes similar lengths.
     // The queue holds the intra slices, then the predictive ones, each run
@@ -187,37 +211,49 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     if (!intra.empty() && p->tree.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
     // inverse-RAHT schedule: slices grouped by slot (largest slots first)
     {
-        std::vector<std::vector<int32_t>> per;  // queue indices per slot, in queue order
-        std::vector<int32_t> slot_of;
-        std::vector<int32_t> where(max_slot + 1, -1);
+        // queue indices bucketed by slot (slots in order of first appearance,
+        // each bucket in queue order): a counting sort into one array
+        std::vector<int32_t> where(max_slot + 1, -1), slot_of, cnt_of;
+        std::vector<int32_t> bucket_of(n);
         for (int q2 = 0; q2 < n; ++q2) {
             const int32_t sl = p->work[q2].slot;
             if (where[sl] < 0) {
-                where[sl] = (int32_t)per.size();
-                per.emplace_back();
+                where[sl] = (int32_t)slot_of.size();
                 slot_of.push_back(sl);
+                cnt_of.push_back(0);
             }
-            per[where[sl]].push_back(q2);
+            bucket_of[q2] = where[sl];
+            ++cnt_of[where[sl]];
         }
-        std::vector<int32_t> ord(per.size());
+        const int nb = (int)slot_of.size();
+        std::vector<int32_t> bstart(nb + 1, 0), flat(n);
+        for (int b = 0; b < nb; ++b) bstart[b + 1] = bstart[b] + cnt_of[b];
+        {
+            std::vector<int32_t> at(bstart.begin(), bstart.end() - 1);
+            for (int q2 = 0; q2 < n; ++q2) flat[at[bucket_of[q2]]++] = q2;
+        }
+        std::vector<int32_t> ord(nb);
         std::iota(ord.begin(), ord.end(), 0);
-        std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) { return p->work[per[a][0]].n > p->work[per[b][0]].n; });
+        std::stable_sort(ord.begin(), ord.end(),
+                         [&](int32_t a, int32_t b) { return p->work[flat[bstart[a]]].n > p->work[flat[bstart[b]]].n; });
         std::vector<GroupDesc> ga, gb;
         std::vector<int32_t> items, la, lb;
+        items.reserve(n);
         for (int32_t si : ord) {
-            const auto& L = per[si];
+            const int32_t* L = flat.data() + bstart[si];  // the slot's queue indices
+            const size_t Ln = (size_t)(bstart[si + 1] - bstart[si]);
             const bool has_intra = !(p->work[L[0]].type & PVVC_TYPE_PREDICT);
-            for (size_t c0 = 0; c0 < L.size(); c0 += 32) {
-                const int cnt = (int)std::min<size_t>(32, L.size() - c0);
+            for (size_t c0 = 0; c0 < Ln; c0 += 32) {
+                const int cnt = (int)std::min<size_t>(32, Ln - c0);
                 const bool first = c0 == 0;
                 const bool phase_b = has_intra && !first;
                 if ((first && has_intra) || cnt >= p->tune.min_group) {
                     GroupDesc g{slot_of[si], (int32_t)items.size(), cnt, (first && has_intra) ? 1 : 0};
-                    items.insert(items.end(), L.begin() + c0, L.begin() + c0 + cnt);
+                    items.insert(items.end(), L + c0, L + c0 + cnt);
                     (phase_b ? gb : ga).push_back(g);
                 } else {
                     auto& dst = phase_b ? lb : la;
-                    dst.insert(dst.end(), L.begin() + c0, L.begin() + c0 + cnt);
+                    dst.insert(dst.end(), L + c0, L + c0 + cnt);
                 }
             }
         }
