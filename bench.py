@@ -190,8 +190,10 @@ def run_reference(args):
     s, frames = make_workload(args, 0)
     per = []
     cb = None
+    # each step a bounded sample; the whole run stays near 90 s of CPU work
+    per_step = max(0.5, min(args.cpu_seconds / 2, 90.0 / (args.warmup + args.steps)))
     for i in range(args.warmup + args.steps):
-        cb = cpu_baseline(frames, max(2.0, args.cpu_seconds / 2))
+        cb = cpu_baseline(frames, per_step)
         if i >= args.warmup:
             per.append(cb["value"])
     v = float(np.median(per))
