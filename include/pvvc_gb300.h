@@ -191,6 +191,36 @@ int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* cons
  * synchronisation.  Fills min(n, 4) values; zeros before any call. */
 int pvvc_host_stage_times(double* out, int32_t n);
 
+/* ---- zstd payloads on the GPU ----------------------------------------------
+ * Batched ZSTD_decompress for payloads that carry a zstd type bit.  Replaces
+ * the host zstd stage of the reference loader (ZstdDecoder::Decode,
+ * src/common/entropy_codec.cc:341-360, called from io::LoadFrame,
+ * src/cuda/common/slice_io.cu:233-265, and io::LoadSlice/LoadFrame,
+ * src/io/slice_io.cc).  Job j inflates src[src_off[j], +src_len[j]) into
+ * dst[dst_off[j], +dst_cap[j]) with ZSTD_decompress's contract: every zstd
+ * frame of the input is decoded and appended, skippable frames are skipped,
+ * and the job fails (status PVVC_ERR_ZSTD, out_len 0) on a malformed frame, a
+ * frame whose decoded size differs from its declared content size, a content
+ * checksum mismatch, output beyond dst_cap, a dictionary id, a legacy
+ * (pre-1.0) frame, or trailing bytes.  On well-formed frames the output is
+ * byte-identical to libzstd's.  On corrupt ones the decoder never accepts what
+ * libzstd rejects; it is stricter in one place (a Huffman literal stream must
+ * end exactly on its first bit, which libzstd's fast 4-stream path does not
+ * check).  Arrays are device memory; out_len may be NULL.  One warp per job;
+ * stream-ordered.  The reference sizes dst by the first frame's declared
+ * content size: pvvc_zstd_content_size reads it on the host. */
+int pvvc_zstd_inflate_batch(int32_t njobs, const uint8_t* src, const uint64_t* src_off, const uint32_t* src_len,
+                            uint8_t* dst, const uint64_t* dst_off, const uint32_t* dst_cap, uint32_t* out_len,
+                            int32_t* status, void* stream);
+/* ZSTD_getFrameContentSize of the first frame of a host buffer: *size gets the
+ * declared size, 0 for a skippable frame, UINT64_MAX when the frame does not
+ * declare it; PVVC_ERR_ZSTD when the header is malformed or truncated. */
+int pvvc_zstd_content_size(const uint8_t* src, uint64_t n, uint64_t* size);
+/* The same decoder as pvvc_zstd_inflate_batch, run on host buffers by one
+ * thread.  No reference counterpart; it lets a host without a GPU check the
+ * decoder against libzstd. */
+int pvvc_zstd_inflate_host(const uint8_t* src, uint64_t n, uint8_t* dst, uint64_t cap, uint64_t* out_len);
+
 /* ---- reference-signature shim --------------------------------------------
  * Same arguments as launch_cudaProcess (include/cuda/render.cuh:42-57) with
  * the decoder array replaced by a pvvc_state (slot = index[i]).  All arrays

@@ -20,6 +20,13 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-fmad=false", "-I", INCLUDE] + ARCH
 # -ffp-contract=off: host float code must not fuse a*b+c on any host (aarch64 would)
+# zstd_kernels.cu: built with ptxas -O1.  With the default -O3 schedule the
+# zstd kernel returned wrong results for some payloads, nondeterministically
+# and depending on the kernel instance, even with a single thread per CTA and
+# its tables in global memory; -O1 and -O0 builds of the same source were
+# exact on every run, and the same source compiled for the host is clean
+# under address and undefined-behaviour sanitisers.
+PER_FILE_FLAGS = {"zstd_kernels.cu": ["-Xptxas", "-O1"]}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
              "-pthread", "-I", INCLUDE]
 
@@ -44,7 +51,7 @@ def _compile(src: str, verbose: bool) -> str:
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(p) for p in deps):
         return obj
     if src.endswith(".cu"):
-        cmd = [_nvcc(), "-c", src, "-o", obj] + NVCC_FLAGS
+        cmd = [_nvcc(), "-c", src, "-o", obj] + NVCC_FLAGS + PER_FILE_FLAGS.get(os.path.basename(src), [])
     else:
         cmd = [os.environ.get("CXX", "g++"), "-c", src, "-o", obj] + CXX_FLAGS
     if verbose:

@@ -14,6 +14,7 @@
 
 #include "../host/bitstream.h"
 #include "decode_internal.h"
+#include "zstd_core.h"
 
 namespace pvvc {
 
@@ -771,6 +772,38 @@ extern "C" int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const
 
 namespace {
 thread_local double g_stage_ms[4] = {0, 0, 0, 0};  // see pvvc_host_stage_times
+
+// A zstd payload of a parsed frame, left compressed for the GPU.
+struct ZJob {
+    int32_t slice;       // within its frame
+    int32_t which;       // 0 geometry, 1 colour
+    const uint8_t* src;  // the compressed bytes (in the caller's frame)
+    uint32_t len;
+    uint64_t zoff;       // staging offset in the packed payload
+};
+
+// Replaces each zstd payload of `f` by a job: its size becomes the first
+// frame's declared content size, which the reference's ZstdDecoder sizes its
+// output by and requires to be known and non-zero (entropy_codec.cc:343-347),
+// its bytes are dropped from the view, and the type's zstd bits cleared.
+int frame_view_zstd_jobs(FrameView* f, std::vector<ZJob>* jobs) {
+    for (size_t i = 0; i < f->count(); ++i) {
+        for (int which = 0; which < 2; ++which) {
+            const uint8_t bit = which ? (uint8_t)PVVC_TYPE_COLOR_ZSTD : (uint8_t)PVVC_TYPE_GEO_ZSTD;
+            const uint8_t*& at = which ? f->col[i] : f->geo[i];
+            uint32_t& sz = which ? f->csz[i] : f->gsz[i];
+            if (!(f->type[i] & bit) || !sz) continue;
+            uint64_t raw = 0;
+            if (!pvvc_zstd::content_size(at, sz, &raw) || raw == 0 || raw == pvvc_zstd::kUnknown || raw > 0xFFFFFFFFull)
+                return PVVC_ERR_ZSTD;
+            jobs->push_back(ZJob{(int32_t)i, which, at, sz, 0});
+            at = nullptr;
+            sz = (uint32_t)raw;
+        }
+        f->type[i] &= (uint8_t)~(PVVC_TYPE_GEO_ZSTD | PVVC_TYPE_COLOR_ZSTD);
+    }
+    return PVVC_OK;
+}
 struct StageClock {
     std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
     double lap() {  // ms since the previous lap
@@ -796,13 +829,16 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     const int threads = host_threads();
     StageClock clk;
     for (double& v : g_stage_ms) v = 0;
-    // parse (io::LoadFrame) and inflate zstd on the host, frames in parallel
-    // the payloads stay in the caller's bytes until they are packed
+    // parse (io::LoadFrame), frames in parallel; the payloads stay in the
+    // caller's bytes until they are packed, and zstd payloads stay compressed:
+    // the GPU inflates them in place of the loader's host zstd stage
+    // (slice_io.cu:233-265)
     std::vector<FrameView> frames(nframes);
+    std::vector<std::vector<ZJob>> fz(nframes);
     std::vector<int> prc(nframes, PVVC_OK);
     parallel_for(nframes, threads, [&](int f) {
         prc[f] = parse_frame_view(frame_bytes[f], frame_len[f], &frames[f]);
-        if (!prc[f]) prc[f] = frame_view_inflate(&frames[f]);
+        if (!prc[f]) prc[f] = frame_view_zstd_jobs(&frames[f], &fz[f]);
     });
     for (int r : prc)
         if (r) return r;
@@ -842,9 +878,41 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     }
     if (npoints_out) *npoints_out = pts;
     if (pts > cap_points || (status_host && status_cap < nsl)) return PVVC_ERR_CAPACITY;
-    if (st->h_payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
+    // zstd staging after the raw region: the compressed payloads, then the
+    // job arrays (source offset, raw offset, source length, raw size, slice)
+    // and a status per job, all carried by the one host-to-device copy
+    int32_t nz = 0;
+    uint64_t zend = align_up(bytes + 16, 16);
+    for (int f = 0; f < nframes; ++f)
+        for (ZJob& j : fz[f]) {
+            j.zoff = zend;
+            zend += j.len;
+            ++nz;
+        }
+    const uint64_t a_src_off = align_up(zend, 16), a_dst_off = a_src_off + 8ull * nz, a_src_len = a_dst_off + 8ull * nz,
+                   a_cap = a_src_len + 4ull * nz, a_slice = a_cap + 4ull * nz, a_status = a_slice + 4ull * nz;
+    const uint64_t total = nz ? a_status + 4ull * nz : bytes;
+    if (st->h_payload.ensure(total + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     uint8_t* hp = static_cast<uint8_t*>(st->h_payload.p);
     std::memset(hp + bytes, 0, 16);  // the decoder reads whole 16-byte blocks
+    if (nz) {
+        uint64_t* zs = reinterpret_cast<uint64_t*>(hp + a_src_off);
+        uint64_t* zd = reinterpret_cast<uint64_t*>(hp + a_dst_off);
+        uint32_t* zl = reinterpret_cast<uint32_t*>(hp + a_src_len);
+        uint32_t* zc = reinterpret_cast<uint32_t*>(hp + a_cap);
+        int32_t* zk = reinterpret_cast<int32_t*>(hp + a_slice);
+        int32_t q = 0;
+        for (int f = 0; f < nframes; ++f)
+            for (const ZJob& j : fz[f]) {
+                const int32_t k = ffirst[f] + j.slice;
+                zs[q] = j.zoff;
+                zl[q] = j.len;
+                zd[q] = j.which ? coff[k] : goff[k];
+                zc[q] = j.which ? csz[k] : gsz[k];
+                zk[q] = k;
+                ++q;
+            }
+    }
     // The payload bytes go into pinned memory on helper threads while this
     // thread splits the call into runs and builds the first plan; the copy
     // to the device waits for them.
@@ -853,10 +921,10 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
             FrameView& fr = frames[f];
             for (size_t i = 0; i < fr.count(); ++i) {
                 const int32_t k = ffirst[f] + (int32_t)i;
-                if (gsz[k]) std::memcpy(hp + goff[k], fr.geo[i], gsz[k]);
-                if (csz[k]) std::memcpy(hp + coff[k], fr.col[i], csz[k]);
+                if (gsz[k] && fr.geo[i]) std::memcpy(hp + goff[k], fr.geo[i], gsz[k]);
+                if (csz[k] && fr.col[i]) std::memcpy(hp + coff[k], fr.col[i], csz[k]);
             }
-            std::vector<std::vector<uint8_t>>().swap(fr.owned);  // inflated payloads, now packed
+            for (const ZJob& j : fz[f]) std::memcpy(hp + j.zoff, j.src, j.len);
         });
     });
     struct JoinOnExit {
@@ -870,7 +938,13 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         if (sent) return true;
         sent = true;
         packer.join();
-        return !bytes || cudaMemcpyAsync(st->payload.p, hp, bytes + 16, cudaMemcpyHostToDevice, s) == cudaSuccess;
+        if (bytes && cudaMemcpyAsync(st->payload.p, hp, total + 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return false;
+        if (!nz) return true;
+        uint8_t* dp = static_cast<uint8_t*>(st->payload.p);
+        return pvvc_zstd_launch(nz, dp, reinterpret_cast<const uint64_t*>(dp + a_src_off),
+                                reinterpret_cast<const uint32_t*>(dp + a_src_len), dp,
+                                reinterpret_cast<const uint64_t*>(dp + a_dst_off), reinterpret_cast<const uint32_t*>(dp + a_cap),
+                                nullptr, reinterpret_cast<int32_t*>(dp + a_status), s) == PVVC_OK;
     };
     // Intra slices of different frames of one call may hit the same patch
     // index (a new GoP).  Split the call into runs of frames without a
@@ -926,7 +1000,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (!merge)
         for (int32_t k = 0; k < nsl; ++k) slot[k] = index[k];
     g_stage_ms[1] = clk.lap();
-    if (st->payload.ensure(bytes + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (st->payload.ensure(total + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
@@ -952,14 +1026,25 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         g_stage_ms[3] += clk.lap();
     }
     if (rc) return rc;
+    // a payload that did not inflate marks its slice (the call fails below)
+    if (nz && pvvc_zstd_merge_status(nz, reinterpret_cast<const int32_t*>(static_cast<uint8_t*>(st->payload.p) + a_status),
+                                     reinterpret_cast<const int32_t*>(static_cast<uint8_t*>(st->payload.p) + a_slice),
+                                     static_cast<int32_t*>(st->status.p), s) != PVVC_OK)
+        return PVVC_ERR_CUDA;
     if (xyz_host && pts && cudaMemcpyAsync(xyz_host, st->xyz.p, 12 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return PVVC_ERR_CUDA;
     if (rgb_host && pts && cudaMemcpyAsync(rgb_host, st->rgb.p, 3 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return PVVC_ERR_CUDA;
     if (status_host && nsl && cudaMemcpyAsync(status_host, st->status.p, 4ull * nsl, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return PVVC_ERR_CUDA;
+    std::vector<int32_t> zst(nz);
+    if (nz && cudaMemcpyAsync(zst.data(), static_cast<uint8_t*>(st->payload.p) + a_status, 4ull * nz, cudaMemcpyDeviceToHost,
+                              s) != cudaSuccess)
+        return PVVC_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return PVVC_ERR_CUDA;
     g_stage_ms[3] += clk.lap();
+    for (int32_t z : zst)  // the reference throws on a payload libzstd cannot inflate
+        if (z != PVVC_OK) return PVVC_ERR_ZSTD;
     return PVVC_OK;
 }
 

@@ -11,6 +11,12 @@
 #include "decode_types.h"
 #include "pvvc_gb300.h"
 
+// zstd_kernels.cu: pvvc_zstd_inflate_batch without the argument checks
+int pvvc_zstd_launch(int32_t njobs, const uint8_t* src, const uint64_t* src_off, const uint32_t* src_len, uint8_t* dst,
+                     const uint64_t* dst_off, const uint32_t* dst_cap, uint32_t* out_len, int32_t* status, cudaStream_t s);
+// status[zslice[j]] = PVVC_ERR_ZSTD for every job j whose zstatus is not PVVC_OK
+int pvvc_zstd_merge_status(int32_t njobs, const int32_t* zstatus, const int32_t* zslice, int32_t* status, cudaStream_t s);
+
 namespace pvvc {
 cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payload, const StateView& st, int32_t* tstatus,
                         cudaStream_t s);

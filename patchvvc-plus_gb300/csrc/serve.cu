@@ -29,12 +29,13 @@
 
 #include "../host/bitstream.h"
 #include "decode_internal.h"
+#include "zstd_core.h"
 
 namespace pvvc {
 namespace {
 
 // One queued frame: header arrays copied out of the .frame bytes, payloads
-// referenced in place (or owned, when they had to be inflated).
+// referenced in place (zstd payloads compressed, for the GPU to inflate).
 struct Request {
     uint64_t tag = 0;
     int32_t stream = -1;
@@ -45,8 +46,10 @@ struct Request {
     std::vector<uint32_t> size, gsz, csz;
     std::vector<float> mv;
     std::vector<const uint8_t*> gp, cp;
-    std::vector<std::vector<uint8_t>> owned;
+    std::vector<uint32_t> gzl, czl;  // compressed length of a zstd payload (0: raw); gsz/csz are then its raw size
     uint64_t points = 0, bytes = 0;  // bytes: 4-aligned packed payload size
+    uint64_t zbytes = 0;             // compressed bytes of the zstd payloads
+    int32_t nz = 0;
     bool has_intra = false;
     // batch bookkeeping
     uint64_t handle = 0, ring_off = 0;
@@ -101,18 +104,25 @@ int parse_request(const uint8_t* b, uint64_t len, Request* r) {
         r->cp[i] = b + o;
         o += r->csz[i];
     }
-    // host zstd stage of the reference loader (slice_io.cu:233-265)
+    // zstd payloads stay compressed: the batch inflates them on the GPU in
+    // place of the reference loader's host zstd stage (slice_io.cu:233-265).
+    // The raw size is the first frame's declared content size, which the
+    // reference's ZstdDecoder requires (entropy_codec.cc:343-347).
+    r->gzl.assign(n, 0);
+    r->czl.assign(n, 0);
     for (uint32_t i = 0; i < n; ++i) {
         for (int which = 0; which < 2; ++which) {
             const uint8_t bit = which ? PVVC_TYPE_COLOR_ZSTD : PVVC_TYPE_GEO_ZSTD;
             uint32_t& sz = which ? r->csz[i] : r->gsz[i];
-            const uint8_t*& ptr = which ? r->cp[i] : r->gp[i];
+            const uint8_t* ptr = which ? r->cp[i] : r->gp[i];
             if (!(r->type[i] & bit) || sz == 0) continue;
-            r->owned.emplace_back();
-            const int z = zstd_decompress(ptr, sz, &r->owned.back());
-            if (z) return z;
-            ptr = r->owned.back().data();
-            sz = (uint32_t)r->owned.back().size();
+            uint64_t raw = 0;
+            if (!pvvc_zstd::content_size(ptr, sz, &raw) || raw == 0 || raw == pvvc_zstd::kUnknown || raw > 0xFFFFFFFFull)
+                return PVVC_ERR_ZSTD;
+            (which ? r->czl : r->gzl)[i] = sz;
+            r->zbytes += sz;
+            r->nz++;
+            sz = (uint32_t)raw;
         }
         r->type[i] &= (uint8_t)~(PVVC_TYPE_GEO_ZSTD | PVVC_TYPE_COLOR_ZSTD);
     }
@@ -311,15 +321,23 @@ void pvvc_server::worker_loop() {
 
 // Pack, plan, upload and enqueue one batch (no lock held).
 int pvvc_server::launch(Batch& b) {
-    uint64_t bytes = 0;
-    int32_t nsl = 0;
+    uint64_t bytes = 0, zbytes = 0;
+    int32_t nsl = 0, nz = 0;
     for (Request* r : b.reqs) {
         r->first_slice = nsl;
         nsl += (int32_t)r->n;
         bytes += r->bytes;
+        zbytes += r->zbytes;
+        nz += r->nz;
     }
     b.nslices = nsl;
-    if (b.h_payload.ensure(bytes + 16) != cudaSuccess || b.d_payload.ensure(bytes + 16) != cudaSuccess ||
+    // payload buffer: the raw payloads the plan indexes; then the zstd
+    // payloads, compressed, and their job arrays (source offset, raw offset,
+    // source length, raw size, slice, status), one host-to-device copy for all
+    const uint64_t zstart = align_up(bytes + 16, 16), a_src = align_up(zstart + zbytes, 16), a_dst = a_src + 8ull * nz,
+                   a_len = a_dst + 8ull * nz, a_cap = a_len + 4ull * nz, a_slice = a_cap + 4ull * nz,
+                   a_stat = a_slice + 4ull * nz, total = nz ? a_stat + 4ull * nz : bytes;
+    if (b.h_payload.ensure(total + 16) != cudaSuccess || b.d_payload.ensure(total + 16) != cudaSuccess ||
         b.h_status.ensure(4ull * std::max(nsl, 1)) != cudaSuccess || b.d_status.ensure(4ull * std::max(nsl, 1)) != cudaSuccess)
         return PVVC_ERR_NOMEM;
     b.slot.resize(nsl);
@@ -333,8 +351,28 @@ int pvvc_server::launch(Batch& b) {
     b.coff.resize(nsl);
     b.oo.resize(nsl);
     uint8_t* hp = static_cast<uint8_t*>(b.h_payload.p);
-    uint64_t off = 0;
-    int32_t k = 0;
+    uint64_t* zsrc = reinterpret_cast<uint64_t*>(hp + a_src);
+    uint64_t* zdst = reinterpret_cast<uint64_t*>(hp + a_dst);
+    uint32_t* zlen = reinterpret_cast<uint32_t*>(hp + a_len);
+    uint32_t* zcap = reinterpret_cast<uint32_t*>(hp + a_cap);
+    int32_t* zsl = reinterpret_cast<int32_t*>(hp + a_slice);
+    uint64_t off = 0, zo = zstart;
+    int32_t k = 0, q = 0;
+    auto put = [&](const uint8_t* p, uint32_t raw, uint32_t zl) {  // one payload at `off`
+        if (!raw) return;
+        if (!zl) {
+            std::memcpy(hp + off, p, raw);
+            return;
+        }
+        std::memcpy(hp + zo, p, zl);
+        zsrc[q] = zo;
+        zdst[q] = off;
+        zlen[q] = zl;
+        zcap[q] = raw;
+        zsl[q] = k;
+        zo += zl;
+        ++q;
+    };
     for (Request* r : b.reqs) {
         uint64_t po = r->ring_off;
         for (uint32_t i = 0; i < r->n; ++i, ++k) {
@@ -345,11 +383,11 @@ int pvvc_server::launch(Batch& b) {
             std::memcpy(&b.mv[16ull * k], &r->mv[16ull * i], 64);
             b.goff[k] = off;
             b.gsz[k] = r->gsz[i];
-            if (r->gsz[i]) std::memcpy(hp + off, r->gp[i], r->gsz[i]);
+            put(r->gp[i], r->gsz[i], r->gzl[i]);
             off = align_up(off + r->gsz[i], 4);
             b.coff[k] = off;
             b.csz[k] = r->csz[i];
-            if (r->csz[i]) std::memcpy(hp + off, r->cp[i], r->csz[i]);
+            put(r->cp[i], r->csz[i], r->czl[i]);
             off = align_up(off + r->csz[i], 4);
             b.oo[k] = po;
             po += r->size[i];
@@ -361,13 +399,21 @@ int pvvc_server::launch(Batch& b) {
     int rc = build_plan(&d, &b.plan, &cfg.tune, copy);
     if (rc) return rc;
     if (b.ws.ensure(b.plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
-    if (cudaMemcpyAsync(b.d_payload.p, hp, off + 16, cudaMemcpyHostToDevice, copy) != cudaSuccess ||
+    if (cudaMemcpyAsync(b.d_payload.p, hp, (nz ? total : off) + 16, cudaMemcpyHostToDevice, copy) != cudaSuccess ||
         cudaEventRecord(b.e_h2d, copy) != cudaSuccess || cudaStreamWaitEvent(compute, b.e_h2d, 0) != cudaSuccess ||
         cudaEventRecord(b.e_start, compute) != cudaSuccess)
         return PVVC_ERR_CUDA;
+    uint8_t* dp = static_cast<uint8_t*>(b.d_payload.p);
+    rc = pvvc_zstd_launch(nz, dp, reinterpret_cast<const uint64_t*>(dp + a_src), reinterpret_cast<const uint32_t*>(dp + a_len),
+                          dp, reinterpret_cast<const uint64_t*>(dp + a_dst), reinterpret_cast<const uint32_t*>(dp + a_cap),
+                          nullptr, reinterpret_cast<int32_t*>(dp + a_stat), compute);
+    if (rc) return rc;
     rc = run_decode(&b.plan, state, static_cast<const uint8_t*>(b.d_payload.p), static_cast<float*>(ring_xyz.p),
                     static_cast<uint8_t*>(ring_rgb.p), nullptr, static_cast<int32_t*>(b.d_status.p), b.ws.p, b.ws.cap, compute,
                     nullptr);
+    if (rc) return rc;
+    rc = pvvc_zstd_merge_status(nz, reinterpret_cast<const int32_t*>(dp + a_stat), reinterpret_cast<const int32_t*>(dp + a_slice),
+                                static_cast<int32_t*>(b.d_status.p), compute);
     if (rc) return rc;
     if (cudaMemcpyAsync(b.h_status.p, b.d_status.p, 4ull * nsl, cudaMemcpyDeviceToHost, compute) != cudaSuccess ||
         cudaEventRecord(b.e_done, compute) != cudaSuccess)

@@ -6,3 +6,4 @@ from .codec import (Decoder, Encoder, Graph, Plan, autotune, encode_patch_gop, p
 from .frame import Batch, Frame, concat_batches, pack_frames, parse_frame, parse_slice, write_frame  # noqa: F401
 from .synth import Synth, config  # noqa: F401
 from .serve import Server, playback  # noqa: F401
+from . import zstd  # noqa: F401

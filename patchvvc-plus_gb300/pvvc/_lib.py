@@ -91,6 +91,9 @@ SIGNATURES = [
     ("pvvc_decode_frames_host", C.c_int, [vp, C.c_int32, C.POINTER(u8p), u64p, f32p, u8p, C.c_uint64, u64p, i32p,
                                           C.c_int32, vp]),
     ("pvvc_host_stage_times", C.c_int, [C.POINTER(C.c_double), C.c_int32]),
+    ("pvvc_zstd_inflate_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    ("pvvc_zstd_content_size", C.c_int, [u8p, C.c_uint64, u64p]),
+    ("pvvc_zstd_inflate_host", C.c_int, [u8p, C.c_uint64, u8p, C.c_uint64, u64p]),
     ("pvvc_launch_cudaProcess", C.c_int, [C.c_int, C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                           C.c_int, vp]),
     ("pvvc_encode_patch_gop", C.c_int, [f32p, C.c_uint32, f32p, C.c_int32, u8p, u8p, C.c_uint64, u64p, u8p,

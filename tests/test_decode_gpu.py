@@ -79,11 +79,7 @@ def test_golden_gop_host_api(pvvc_lib, oracle, torch):
 
 
 def test_golden_gop_zstd_payloads(pvvc_lib, oracle, torch):
-    if ctypes.util.find_library("zstd") is None:
-        try:
-            ctypes.CDLL("libzstd.so.1")
-        except OSError:
-            pytest.skip("libzstd is not installed on this host (zstd payloads are inflated on the host)")
+    """The reference encoder's zstd payloads, inflated on the GPU by the host call."""
     exp = golden_expected()
     ref = oracle_decode(oracle, pvvc_lib, golden_frames("raw"), 8)
     dec = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
@@ -278,3 +274,33 @@ def test_host_call_decodes_gops_in_one_plan_identically(pvvc_lib, torch, nframes
     b = serial.decode_frames(frames[9:11])
     for x, y in zip(a, b):
         assert np.array_equal(x, y)
+
+
+def test_host_call_zstd_sequence_matches_raw(pvvc_lib, torch):
+    """A synthetic GoP whose payloads are zstd-compressed by the reference
+    encoder's rule (GoP_encoding.cc:158-200: level 22, kept only when smaller)
+    decodes exactly as its raw form; a corrupt zstd payload fails the call
+    with PVVC_ERR_ZSTD, as the reference's ZstdDecoder throws."""
+    import libzstd_ref as zr
+    s = pvvc_lib.Synth(pvvc_lib.config("gof8", nframes=8, seed=3))
+    raw = s.frames()
+    z = [zr.zstd_frame(b, pvvc_lib, 22) for b in raw]
+    nz = sum(int(((pvvc_lib.parse_frame(b).type & 0x18) != 0).sum()) for b in z)
+    assert nz > 0
+    d1 = pvvc_lib.Decoder(nslots=256, max_leaves=4096)
+    d2 = pvvc_lib.Decoder(nslots=256, max_leaves=4096)
+    x1, r1, s1 = d1.decode_frames(raw)
+    x2, r2, s2 = d2.decode_frames(z)
+    assert (s1 == 0).all() and (s2 == 0).all()
+    assert np.array_equal(x1.view(np.uint32), x2.view(np.uint32)) and np.array_equal(r1, r2)
+    t = next(t for t in range(len(z)) if (pvvc_lib.parse_frame(z[t]).type & 0x10).any())
+    f = pvvc_lib.parse_frame(z[t])
+    i = int(np.flatnonzero(f.type & 0x10)[0])
+    c = bytearray(f.color[i])
+    c[len(c) // 2] ^= 0xFF
+    c[len(c) // 2 + 1] ^= 0x5A
+    f.color[i] = bytes(c)
+    if zr.decompress(f.color[i], zr.content_size(f.color[i])) is None:
+        with pytest.raises(pvvc_lib.PvvcError) as e:
+            pvvc_lib.Decoder(nslots=256, max_leaves=4096).decode_frames(z[:t] + [pvvc_lib.write_frame(f)] + z[t + 1:])
+        assert e.value.status == 9

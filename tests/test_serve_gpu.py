@@ -161,3 +161,41 @@ def test_small_output_ring_applies_back_pressure(pvvc_lib, torch, sequences):
             assert s == 0 and np.array_equal(x, xyz[o:o + x.shape[0]]) and np.array_equal(r, rgb[o:o + x.shape[0]])
             o += x.shape[0]
     srv.close()
+
+
+def test_zstd_frames_served_like_raw(pvvc_lib, torch, sequences):
+    """zstd payloads (the reference encoder's rule: level 22, kept when
+    smaller) are inflated on the GPU inside the batch: every frame equals the
+    raw frame's result; a payload that does not inflate fails its frame
+    with PVVC_ERR_ZSTD."""
+    import libzstd_ref as zr
+    from pvvc.serve import slots_needed
+    frames = sequences[1]
+    zf = [zr.zstd_frame(b, pvvc_lib, 22) for b in frames]
+    assert any((pvvc_lib.parse_frame(b).type & 0x18).any() for b in zf)
+    out = {}
+    for name, fs in (("raw", frames), ("zstd", zf)):
+        srv = _server(pvvc_lib)
+        sid = srv.open_stream(slots_needed(fs))
+        for k, b in enumerate(fs):
+            srv.submit(sid, b, tag=(name, k))
+        out.update(_drain(srv, len(fs)))
+        srv.close()
+    for k in range(len(frames)):
+        s0, x0, r0 = out[("raw", k)]
+        s1, x1, r1 = out[("zstd", k)]
+        assert s0 == 0 and s1 == 0
+        assert np.array_equal(x0.view(np.uint32), x1.view(np.uint32)) and np.array_equal(r0, r1)
+    # a truncated zstd frame inside a payload: the declared size stays, the inflation fails
+    f = pvvc_lib.parse_frame(zf[0])
+    i = next(i for i in range(f.n) if f.type[i] & 0x18)
+    if f.type[i] & 0x08:
+        f.geometry[i] = bytes(f.geometry[i])[:-3]
+    else:
+        f.color[i] = bytes(f.color[i])[:-3]
+    srv = _server(pvvc_lib)
+    sid = srv.open_stream(slots_needed(zf))
+    srv.submit(sid, pvvc_lib.write_frame(f), tag="bad")
+    res = _drain(srv, 1, read=False)
+    srv.close()
+    assert res["bad"][0] == 9
