@@ -65,6 +65,8 @@ def parse_args():
     ap.add_argument("--learned-train-pairs", type=int, default=32768, help="pairs to train on when no weights are committed")
     ap.add_argument("--learned-train-epochs", type=int, default=8)
     ap.add_argument("--no-knn", dest="knn", action="store_false", help="skip the GPU colour-interpolation measurement")
+    ap.add_argument("--zstd-level", type=int, default=22, help="zstd level of the zstd-payload measurement (0: skip); the "
+                                                               "reference's configs all use 22")
     ap.add_argument("--serve-streams", type=int, default=64, help="playback streams of the serving run (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="real-time length of the serving run")
     return ap.parse_args()
@@ -340,6 +342,7 @@ def run_ours(args):
         learned = measure_learned(args, torch, pvvc) if args.icp_pairs > 0 and args.learned else None
         encode = measure_encode(args, torch, pvvc, s, len(frames)) if args.encode else None
         knn = measure_knn_colors(args, torch, pvvc, s) if args.knn else None
+        zstd = measure_zstd(args, torch, pvvc, P, stream) if args.zstd_level else None
         serving = measure_serving(args, pvvc) if args.serve_streams > 0 and args.serve_seconds > 0 else None
         out = {"metric": "decoded Mpts/s (seq300, GoP 30, ~800k pts/frame)", "value": value, "unit": "Mpts/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -347,12 +350,88 @@ def run_ours(args):
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
                "clocks": clk.summary(), "gpu_launches": info["kernels"] * args.steps, "points_per_step": P * world,
                "plan": info, "autotune_ms": tune_ms, "icp": icp, "learned_icp": learned, "encode": encode,
-               "knn_colors": knn, "serving": serving}
+               "knn_colors": knn, "zstd": zstd, "serving": serving}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     return out
+
+
+def measure_zstd(args, torch, pvvc, P, stream):
+    """The same sequence with its payloads zstd-compressed as the reference
+    encoder does at its configs' zstd_level (kept where smaller,
+    GoP_encoding.cc:158-200).  Times (a) pvvc_zstd_inflate_batch over every
+    zstd payload of the sequence (CUDA events, payloads resident on the
+    device), (b) libzstd's ZSTD_decompress of the same payloads on all host
+    cores (the reference loader's zstd stage, slice_io.cu:233-265), and (c) the
+    end-to-end host call on the zstd frames, whose payloads the GPU inflates."""
+    import ctypes
+    from oracle import Oracle
+    t0 = time.time()
+    cfg = pvvc.config("seq300", nframes=args.frames, qp_i=args.qp, qp_p=args.qp, seed=0, zstd_level=args.zstd_level)
+    zs = pvvc.Synth(cfg)
+    zframes = zs.frames()
+    gen_s = time.time() - t0
+    payloads = []
+    for b in zframes:
+        f = pvvc.parse_frame(b)
+        for i in np.flatnonzero(f.type & 0x18):
+            if f.type[i] & 0x08:
+                payloads.append(bytes(f.geometry[i]))
+            if f.type[i] & 0x10:
+                payloads.append(bytes(f.color[i]))
+    caps = [pvvc.zstd.content_size(p) for p in payloads]
+    n = len(payloads)
+    src_len = np.array([len(p) for p in payloads], np.uint32)
+    cap = np.array(caps, np.uint32)
+    so = np.zeros(n, np.uint64)
+    so[1:] = np.cumsum(src_len[:-1].astype(np.uint64))
+    do = np.zeros(n, np.uint64)
+    do[1:] = np.cumsum(cap[:-1].astype(np.uint64))
+    dev = torch.device("cuda")
+    src = torch.from_numpy(np.frombuffer(b"".join(payloads), np.uint8).copy()).to(dev)
+    dst = torch.zeros(int(cap.astype(np.uint64).sum()) + 16, dtype=torch.uint8, device=dev)
+    arrs = [torch.from_numpy(a).to(dev) for a in (so.view(np.int64), src_len.view(np.int32), do.view(np.int64), cap.view(np.int32))]
+    st = torch.zeros(n, dtype=torch.int32, device=dev)
+    lib = pvvc.lib()
+    vp = ctypes.c_void_p
+
+    def launch():
+        rc = lib.pvvc_zstd_inflate_batch(n, vp(src.data_ptr()), vp(arrs[0].data_ptr()), vp(arrs[1].data_ptr()),
+                                         vp(dst.data_ptr()), vp(arrs[2].data_ptr()), vp(arrs[3].data_ptr()), None,
+                                         vp(st.data_ptr()), vp(stream.cuda_stream))
+        if rc:
+            raise pvvc.PvvcError(rc, "pvvc_zstd_inflate_batch")
+
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            launch()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 10
+        e0.record(stream)
+        for _ in range(reps):
+            launch()
+        e1.record(stream)
+        stream.synchronize()
+    kms = e0.elapsed_time(e1) / reps
+    threads = os.cpu_count() or 1
+    want, wst, cpu_s = Oracle().libzstd_inflate_batch(payloads, caps, threads)
+    d = dst.cpu().numpy()
+    same = all(d[int(do[j]):int(do[j]) + caps[j]].tobytes() == want[j] for j in range(n))
+    pz = sum(int(lib.pvvc_synth_frame_points(zs.h, t)) for t in range(len(zframes)))
+    e2e = measure_e2e(args, pvvc, zframes, pz, torch, stream)
+    raw_b, comp_b = int(cap.astype(np.uint64).sum()), int(src_len.astype(np.uint64).sum())
+    return {"payloads": n, "compressed_bytes": comp_b, "inflated_bytes": raw_b, "zstd_level": args.zstd_level,
+            "kernel_ms": kms, "kernel_out_gbs": raw_b / kms / 1e6, "statuses_ok": int((st == 0).sum()),
+            "identical_to_libzstd": bool(same and all(x == 0 for x in wst)),
+            "cpu_libzstd_ms": cpu_s * 1e3, "cpu_threads": threads, "cpu_out_gbs": raw_b / cpu_s / 1e9,
+            "e2e_zstd": {k: e2e[k] for k in ("value", "unit", "median_call_ms", "call_ms", "stage_ms_last_call")},
+            "generate_s": gen_s,
+            "note": "kernel_ms: one launch over every zstd payload of the sequence; cpu_libzstd_ms: the same payloads "
+                    "through libzstd's ZSTD_decompress on all host threads (the oracle's batch helper); e2e_zstd: "
+                    "pvvc_decode_frames_host on the zstd frames (inflation on the GPU inside the call)"}
 
 
 def measure_icp(args, torch, peak_gbs):

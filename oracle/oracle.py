@@ -120,6 +120,34 @@ class Oracle:
             lib.pvo_knn_colors_batch.argtypes = [C.c_int, _f32p, C.POINTER(C.c_uint64), _u32p, _f32p, _u8p, _u32p,
                                                  C.c_int, _f32p, C.POINTER(C.c_uint64), C.c_int]
 
+    # ---- zstd (libzstd, the reference's dependency) ----
+    def libzstd_inflate_batch(self, payloads: list, caps: list, nthreads: int):
+        """ZSTD_decompress of every payload on nthreads host threads
+        (ZstdDecoder::Decode, src/common/entropy_codec.cc:341-360).
+        Returns (outputs, statuses, seconds of the batch call)."""
+        import time
+        lib = self.lib
+        lib.pvo_libzstd_inflate_batch.restype = C.c_int
+        n = len(payloads)
+        src = np.frombuffer(b"".join(payloads) + b"\0", np.uint8).copy()
+        sl = np.array([len(p) for p in payloads], np.uint32)
+        so = np.zeros(n, np.uint64)
+        so[1:] = np.cumsum(sl[:-1].astype(np.uint64))
+        cp = np.array(caps, np.uint32)
+        do = np.zeros(n, np.uint64)
+        do[1:] = np.cumsum(cp[:-1].astype(np.uint64))
+        dst = np.zeros(int(cp.astype(np.uint64).sum()) + 1, np.uint8)
+        st = np.zeros(max(n, 1), np.int32)
+        t = time.perf_counter()
+        rc = lib.pvo_libzstd_inflate_batch(n, _ptr(src, _u8p), so.ctypes.data_as(C.c_void_p), sl.ctypes.data_as(C.c_void_p),
+                                           _ptr(dst, _u8p), do.ctypes.data_as(C.c_void_p), cp.ctypes.data_as(C.c_void_p),
+                                           _ptr(st, _i32p), nthreads)
+        dt = time.perf_counter() - t
+        if rc:
+            raise RuntimeError("libzstd is not available")
+        outs = [dst[int(do[j]):int(do[j]) + int(cp[j])].tobytes() for j in range(n)]
+        return outs, st[:n].tolist(), dt
+
     # ---- RLGR ----
     def rlgr_encode(self, sym: np.ndarray) -> bytes:
         sym = np.ascontiguousarray(sym, dtype=np.int64)

@@ -143,6 +143,12 @@ int pvo_knn_colors_batch(int npairs, const float* q, const uint64_t* qoff, const
                          const uint8_t* rgb, const uint32_t* soff, int k, float* yuv, const uint64_t* out_off,
                          int nthreads);
 
+/* libzstd's ZSTD_decompress over a batch of payloads on nthreads host
+ * threads (the reference's zstd stage); status 0 or 9 per payload.  Returns
+ * -1 when libzstd cannot be loaded. */
+int pvo_libzstd_inflate_batch(int n, const uint8_t* src, const uint64_t* src_off, const uint32_t* src_len, uint8_t* dst,
+                              const uint64_t* dst_off, const uint32_t* dst_cap, int32_t* status, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,13 +65,10 @@ struct Shared {
     Cell wt[64];                    // Huffman weight table (accuracy log <= 6)
     int16_t norm[256];              // normalised counts of the table being built
     uint8_t w[256];                 // Huffman weights
-    uint16_t run_start[256];        // Huffman fill: first entry of each symbol, in fill order
-    uint16_t run_val[256];          //   and the entry written there
+    uint16_t cnt[256];              // scratch of the FSE table builder
     uint32_t seq_ll[kSeqBatch], seq_ml[kSeqBatch], seq_off[kSeqBatch];
     int32_t wcount[16];             // Huffman fill: symbols per weight, then the next rank per weight
-    int32_t wfirst[16];             //   first run index of each weight
     int32_t wpos[16];               //   first table entry of each weight
-    int32_t nruns;                  // symbols with a code in the table being filled
     int32_t hlog;                   // Huffman table log (0: none yet in this frame)
     int32_t llog, mlog, olog;       // accuracy logs of the sequence tables (-1: undefined)
     int32_t val[8];                 // lane-0 results for the warp
@@ -86,49 +83,66 @@ ZFN uint64_t le64(const uint8_t* p) { return (uint64_t)le32(p) | ((uint64_t)le32
 // ---- backward bit stream (FSE and Huffman streams) -------------------------
 // Bit i of the stream is bit (i & 7) of byte i >> 3.  The last byte's highest
 // set bit marks the end; reading starts just below it and goes down.  A read
-// of n bits returns bits [pos - n, pos) with bit pos - 1 as the MSB.  Bits
-// below the first byte read as zero; `pos` going negative is libzstd's
-// overflow state.  A 64-bit cache holds bytes [cb, cb + 8) (bytes outside
-// the stream as zero) and is refilled when a read would leave it.
+// of n bits returns the next n bits, the highest stream bit as the MSB.  Bits
+// below the first byte read as zero; `pos` (the stream bits not yet consumed)
+// going negative is libzstd's overflow state.  The next bits sit
+// left-aligned in a 64-bit container: a read is one shift out of its top,
+// and 32 more bits are taken from the stream whenever fewer than a read
+// needs remain.
 struct BackBits {
     const uint8_t* p;
-    int64_t n;
-    int64_t pos;
-    int64_t cb;
+    int32_t n;
+    int32_t pos;    // stream bits [0, pos) not yet consumed
+    int32_t valid;  // container bits (from the top) that hold stream bits pos-1, pos-2, ...
     uint64_t c;
 
-    ZFN void refill() {
-        const int64_t t = pos - 64;
-        cb = t >= 0 ? (t + 7) >> 3 : -((-t) >> 3);  // ceil(t / 8): the cache then holds > 56 bits below pos
+    // stream bits [b0, b0 + 32), bit b0 + 31 as the MSB; bits outside the stream are zero
+    ZFN uint32_t bits32(int32_t b0) const {
+        const int32_t k0 = b0 >> 3;  // floor
         uint64_t v = 0;
-        if (cb >= 0 && cb + 8 <= n) {
-            v = le64(p + cb);
+        if (k0 >= 0 && k0 + 5 <= n) {
+            v = (uint64_t)le32(p + k0) | ((uint64_t)p[k0 + 4] << 32);
         } else {
-            for (int i = 7; i >= 0; --i) {
-                const int64_t b = cb + i;
-                v = (v << 8) | ((b >= 0 && b < n) ? p[b] : 0u);
+            for (int i = 4; i >= 0; --i) {
+                const int32_t k = k0 + i;
+                v = (v << 8) | ((k >= 0 && k < n) ? p[k] : 0u);
             }
         }
-        c = v;
+        return (uint32_t)(v >> (b0 & 7));
+    }
+    ZFN void fill() {  // valid < 32 on entry
+        const int32_t lo = pos - valid;  // the highest stream bit not in the container is lo - 1
+        if (lo <= 0) {                   // only zeros below: the container's low bits are zero already
+            valid = 64;
+            return;
+        }
+        c |= (uint64_t)bits32(lo - 32) << (32 - valid);
+        valid += 32;
     }
     // false: empty stream or a zero last byte (BIT_initDStream's errors)
     ZFN bool init(const uint8_t* s, int64_t len) {
         p = s;
-        n = len;
+        n = (int32_t)len;
         if (len <= 0 || s[len - 1] == 0) return false;
-        pos = 8 * (len - 1) + highbit(s[len - 1]);
-        refill();
+        pos = 8 * (int32_t)(len - 1) + highbit(s[len - 1]);
+        c = 0;
+        valid = 0;
+        fill();
+        fill();
         return true;
     }
     ZFN uint32_t peek(int nb) {  // nb <= 32
-        if (nb == 0) return 0;
-        if (pos - nb < 8 * cb) refill();
-        const uint32_t sh = (uint32_t)(pos - nb - 8 * cb);
-        return (uint32_t)((c >> sh) & (0xffffffffull >> (32 - nb)));
+        if (valid < nb) fill();
+        return nb ? (uint32_t)(c >> (64 - nb)) : 0u;
+    }
+    ZFN void skip(int nb) {  // after a peek of at least nb bits
+        c <<= nb;
+        pos -= nb;
+        valid -= nb;
     }
     ZFN uint32_t read(int nb) {
         const uint32_t v = peek(nb);
-        pos -= nb;
+        skip(nb);
         return v;
     }
 };
@@ -295,7 +309,7 @@ ZFN int read_huf_weights(Shared& sh, const uint8_t* p, int64_t n, int* nsym, int
         int ns, al;
         const int h = read_ncount(q, hb, sh.norm, &ns, &al, 6, 255);
         if (h < 0) return -1;
-        if (!build_fse(sh.wt, sh.norm, ns, al, sh.run_start)) return -1;
+        if (!build_fse(sh.wt, sh.norm, ns, al, sh.cnt)) return -1;
         BackBits br;
         if (!br.init(q + h, hb - h)) return -1;
         uint32_t s1 = br.read(al), s2 = br.read(al);
@@ -344,9 +358,9 @@ ZFN int read_huf_weights(Shared& sh, const uint8_t* p, int64_t n, int* nsym, int
 // Decoding table of 1 << log entries from sh.w (libzstd HUF_readDTableX1):
 // symbols ordered by weight, then by value, each taking 2^(w-1) consecutive
 // entries from index 0; an entry holds the symbol and its code length
-// log + 1 - w.  The lanes count the symbols of each weight, rank each symbol
-// among the lower symbols of its weight (rounds of nl symbols, lanes of equal
-// weight matched in a round), list the runs in fill order, then fill.
+// log + 1 - w.  The lanes count the symbols of each weight, then rank each
+// symbol among the lower symbols of its weight (rounds of nl symbols, lanes
+// of equal weight matched in a round) and write its own entries.
 ZFN void fill_huf(Shared& sh, int nsym, int log, int lane, int nl) {
     if (lane < 16) sh.wcount[lane] = 0;
     if (nl == 1)
@@ -360,38 +374,29 @@ ZFN void fill_huf(Shared& sh, int nsym, int log, int lane, int nl) {
             sh.wcount[w] += popc(peers);
         wsync();
     }
-    if (lane == 0) {  // runs and table entries of each weight, in weight order
-        int k = 0, pos = 0;
+    if (lane == 0) {  // first table entry of each weight; the counts become the next rank
+        int pos = 0;
         for (int w = 1; w <= log; ++w) {
-            sh.wfirst[w] = k;
             sh.wpos[w] = pos;
-            k += sh.wcount[w];
             pos += sh.wcount[w] << (w - 1);
-            sh.wcount[w] = 0;  // now the next rank of weight w
+            sh.wcount[w] = 0;
         }
-        sh.nruns = k;
     }
     wsync();
-    for (int base = 0; base < nsym; base += nl) {  // each symbol's run
+    for (int base = 0; base < nsym; base += nl) {
         const int s = base + lane;
         const uint32_t w = s < nsym ? sh.w[s] : 0u;
         const uint32_t peers = same_value_lanes(w);
         if (s < nsym && w) {
             const int r = sh.wcount[w] + popc(peers & ((1u << lane) - 1u));
-            sh.run_start[sh.wfirst[w] + r] = (uint16_t)(sh.wpos[w] + (r << (w - 1)));
-            sh.run_val[sh.wfirst[w] + r] = (uint16_t)((s << 4) | (log + 1 - (int)w));
+            const int at = sh.wpos[w] + (r << (w - 1)), len = 1 << (w - 1);
+            const uint16_t v = (uint16_t)((s << 4) | (log + 1 - (int)w));
+            for (int i = 0; i < len; ++i) sh.huf[at + i] = v;
         }
         wsync();
         if (s < nsym && w && (peers & ((1u << lane) - 1u)) == 0) sh.wcount[w] += popc(peers);
         wsync();
     }
-    const int nruns = sh.nruns, size = 1 << log;
-    for (int k = 0; k < nruns; ++k) {
-        const int a = sh.run_start[k], b = k + 1 < nruns ? sh.run_start[k + 1] : size;
-        const uint16_t v = sh.run_val[k];
-        for (int i = a + lane; i < b; i += nl) sh.huf[i] = v;
-    }
-    wsync();
 }
 
 // One Huffman stream of `count` symbols into out[0..count) (libzstd
@@ -403,7 +408,7 @@ ZFN bool huf_stream(const Shared& sh, int log, const uint8_t* s, int64_t len, ui
     if (!br.init(s, len)) return false;
     for (uint32_t i = 0; i < count; ++i) {
         const uint16_t e = sh.huf[br.peek(log)];
-        br.pos -= e & 15;
+        br.skip(e & 15);
         out[i] = (uint8_t)(e >> 4);
     }
     return br.pos == 0;
@@ -495,7 +500,7 @@ ZFN int seq_table(Shared& sh, int kind, int mode, const uint8_t* q, int64_t qn, 
     if (mode == 0) {
         const int ns = predefined(kind, sh.norm);
         const int al = kind == 1 ? 5 : 6;
-        if (!build_fse(t, sh.norm, ns, al, sh.run_start)) return -1;
+        if (!build_fse(t, sh.norm, ns, al, sh.cnt)) return -1;
         *lg = al;
         return 0;
     }
@@ -510,7 +515,7 @@ ZFN int seq_table(Shared& sh, int kind, int mode, const uint8_t* q, int64_t qn, 
     if (mode == 2) {
         int ns, al;
         const int used = read_ncount(q, qn, sh.norm, &ns, &al, maxlog, maxsym);
-        if (used < 0 || !build_fse(t, sh.norm, ns, al, sh.run_start)) return -1;
+        if (used < 0 || !build_fse(t, sh.norm, ns, al, sh.cnt)) return -1;
         *lg = al;
         return used;
     }

@@ -410,6 +410,17 @@ extern "C" int pvvc_synth_encode(pvvc_synth* s) {
                 return;
             }
             auto geo = tree.geometry();
+            // the reference encoder's optional zstd stage: keep the compressed
+            // payload only when it is smaller (GoP_encoding.cc:158-200)
+            auto maybe_zstd = [&](std::vector<uint8_t>* payload, uint8_t bit, uint8_t* type) {
+                if (!c.zstd_level || payload->empty()) return;
+                std::vector<uint8_t> z;
+                if (pvvc::zstd_compress(payload->data(), payload->size(), c.zstd_level, &z) == PVVC_OK &&
+                    z.size() < payload->size()) {
+                    payload->swap(z);
+                    *type |= bit;
+                }
+            };
             std::vector<float> coef;
             auto& out = per_patch[p];
             for (int f = 0; f < g.nframes; ++f) {
@@ -424,8 +435,12 @@ extern "C" int pvvc_synth_encode(pvvc_synth* s) {
                 // Slice.mv is column-major (Eigen); mv[] here is row-major
                 for (int r = 0; r < 4; ++r)
                     for (int cc = 0; cc < 4; ++cc) sl.mv[cc * 4 + r] = mv[16 * f + r * 4 + cc];
-                if (intra) sl.geometry = geo;
+                if (intra) {
+                    sl.geometry = geo;
+                    maybe_zstd(&sl.geometry, pvvc::kTypeGeoZstd, &sl.type);
+                }
                 sl.color = pvvc::encode_colors(coef.data(), tree.leaf_count(), sl.qp);
+                maybe_zstd(&sl.color, pvvc::kTypeColorZstd, &sl.type);
                 out.push_back(std::move(sl));
             }
         });

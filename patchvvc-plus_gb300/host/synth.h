@@ -29,6 +29,9 @@ typedef struct {
     float color_noise;       /* per-frame colour noise sigma                    */
     uint64_t seed;
     int32_t nthreads;
+    int32_t zstd_level;      /* 0: raw payloads; else each payload is zstd-compressed
+                                at this level and kept when smaller, with the slice
+                                type's zstd bit set (GoP_encoding.cc:158-200)     */
 } pvvc_synth_config;
 
 typedef struct pvvc_synth pvvc_synth;

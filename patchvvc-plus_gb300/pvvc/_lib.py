@@ -68,7 +68,8 @@ class SynthConfig(C.Structure):
                 ("target_points", C.c_int32), ("nframes", C.c_int32), ("gof", C.c_int32), ("size_mode", C.c_int32),
                 ("size_a", C.c_float), ("size_b", C.c_float), ("size_min", C.c_float), ("size_max", C.c_float),
                 ("qp_i", C.c_uint8), ("qp_p", C.c_uint8), ("rot_deg", C.c_float), ("trans_vox", C.c_float),
-                ("jitter", C.c_float), ("color_noise", C.c_float), ("seed", C.c_uint64), ("nthreads", C.c_int32)]
+                ("jitter", C.c_float), ("color_noise", C.c_float), ("seed", C.c_uint64), ("nthreads", C.c_int32),
+                ("zstd_level", C.c_int32)]
 
 
 # (name, restype, argtypes) of every exported entry point

@@ -17,7 +17,10 @@ def config(name: str, **over) -> L.SynthConfig:
     'seq300'  300 frames, ~800k points on a 1024^3 grid, 20 primitives
               (axes 40-240), GoP 30, ~500 patches lognormal(median 1500)
               clipped to [200, 8000], q=8 (qp overridable).
-    'tiny'    a few small patches for quick checks."""
+    'tiny'    a few small patches for quick checks.
+    zstd_level=L (any workload): payloads zstd-compressed at level L where
+    that makes them smaller, as the reference encoder does with its
+    configs' zstd_level (22 in every config the reference ships)."""
     nthreads = over.pop("nthreads", os.cpu_count() or 4)
     if name == "gof8":
         c = dict(grid_bits=9, nprims=12, axis_min=20, axis_max=120, target_points=115_000, nframes=8, gof=8,
@@ -30,7 +33,7 @@ def config(name: str, **over) -> L.SynthConfig:
                  size_mode=0, size_a=100, size_b=400, size_min=100, size_max=400, qp_i=8, qp_p=8)
     else:
         raise ValueError(name)
-    c.update(dict(rot_deg=3.0, trans_vox=2.0, jitter=0.3, color_noise=4.0, seed=0, nthreads=nthreads))
+    c.update(dict(rot_deg=3.0, trans_vox=2.0, jitter=0.3, color_noise=4.0, seed=0, nthreads=nthreads, zstd_level=0))
     c.update(over)
     return L.SynthConfig(**c)
 
