@@ -176,16 +176,18 @@ int pvvc_graph_destroy(pvvc_graph* graph);
  * consecutive frames of one sequence, in decode order) into HOST arrays.
  * Mirrors io::LoadFrame + the H2D staging + launch_cudaProcess + the D2H
  * read-back (src/cuda/common/slice_io.cu:143-275, manager.cc:41-72,230-270):
- * zstd payloads are inflated on the host, payloads are copied to the device,
- * decoded, and xyz/rgb are copied back.  Slot = patch index.  Synchronises
- * `stream` before returning.  status_host receives one entry per slice, in
- * file order. */
+ * payloads are copied to the device (zstd payloads compressed, then
+ * inflated there by the kernel of pvvc_zstd_inflate_batch instead of the
+ * loader's host zstd stage), decoded, and xyz/rgb are copied back.  Slot =
+ * patch index.  Synchronises `stream` before returning.  status_host
+ * receives one entry per slice, in file order; a zstd payload that does not
+ * inflate marks its slice PVVC_ERR_ZSTD and the call returns PVVC_ERR_ZSTD. */
 int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* const* frame_bytes, const uint64_t* frame_len,
                             float* xyz_host, uint8_t* rgb_host, uint64_t cap_points, uint64_t* npoints_out,
                             int32_t* status_host, int32_t status_cap, void* stream);
 /* Wall-clock milliseconds of the stages of the calling thread's last
  * pvvc_decode_frames_host (no counterpart in the reference):
- * out[0] parse + inflate, out[1] the batch description and the split into
+ * out[0] parse (with the zstd frame headers), out[1] the batch description and the split into
  * runs, out[2] planning (host) and plan upload, with the payload packed into
  * pinned memory beside it, out[3] H2D + decode + D2H up to the final stream
  * synchronisation.  Fills min(n, 4) values; zeros before any call. */

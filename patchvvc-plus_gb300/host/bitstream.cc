@@ -1,4 +1,4 @@
-// bitstream.cc -- .slice / .frame byte layouts and host-side zstd.
+// bitstream.cc -- .slice / .frame byte layouts and host-side zstd compression.
 #include "bitstream.h"
 
 #include <dlfcn.h>
@@ -173,8 +173,6 @@ struct Zstd {
     void* h = nullptr;
     size_t (*compressBound)(size_t) = nullptr;
     size_t (*compress)(void*, size_t, const void*, size_t, int) = nullptr;
-    size_t (*decompress)(void*, size_t, const void*, size_t) = nullptr;
-    unsigned long long (*contentSize)(const void*, size_t) = nullptr;
     unsigned (*isError)(size_t) = nullptr;
     int (*maxLevel)(void) = nullptr;
     int (*minLevel)(void) = nullptr;
@@ -191,12 +189,10 @@ Zstd* zstd() {
         if (!z.h) return;
         z.compressBound = reinterpret_cast<size_t (*)(size_t)>(dlsym(z.h, "ZSTD_compressBound"));
         z.compress = reinterpret_cast<size_t (*)(void*, size_t, const void*, size_t, int)>(dlsym(z.h, "ZSTD_compress"));
-        z.decompress = reinterpret_cast<size_t (*)(void*, size_t, const void*, size_t)>(dlsym(z.h, "ZSTD_decompress"));
-        z.contentSize = reinterpret_cast<unsigned long long (*)(const void*, size_t)>(dlsym(z.h, "ZSTD_getFrameContentSize"));
         z.isError = reinterpret_cast<unsigned (*)(size_t)>(dlsym(z.h, "ZSTD_isError"));
         z.maxLevel = reinterpret_cast<int (*)(void)>(dlsym(z.h, "ZSTD_maxCLevel"));
         z.minLevel = reinterpret_cast<int (*)(void)>(dlsym(z.h, "ZSTD_minCLevel"));
-        if (!z.compressBound || !z.compress || !z.decompress || !z.contentSize || !z.isError || !z.maxLevel || !z.minLevel) {
+        if (!z.compressBound || !z.compress || !z.isError || !z.maxLevel || !z.minLevel) {
             dlclose(z.h);
             z.h = nullptr;
         }
@@ -206,20 +202,6 @@ Zstd* zstd() {
 }  // namespace
 
 bool zstd_available() { return zstd() != nullptr; }
-
-// ZstdDecoder::Decode (src/common/entropy_codec.cc:341-360)
-int zstd_decompress(const uint8_t* src, size_t n, std::vector<uint8_t>* out) {
-    Zstd* z = zstd();
-    if (!z) return PVVC_ERR_ZSTD;
-    unsigned long long sz = z->contentSize(src, n);
-    if (sz == 0 || sz == ~0ull || sz == ~0ull - 1) return PVVC_ERR_ZSTD;  // 0 / UNKNOWN / ERROR
-    if (sz > (1ull << 32)) return PVVC_ERR_ZSTD;
-    out->resize(sz);
-    size_t r = z->decompress(out->data(), sz, src, n);
-    if (z->isError(r)) return PVVC_ERR_ZSTD;
-    out->resize(r);
-    return PVVC_OK;
-}
 
 // ZstdEncoder::Encode (src/common/entropy_codec.cc:304-324)
 int zstd_compress(const uint8_t* src, size_t n, int level, std::vector<uint8_t>* out) {
@@ -249,7 +231,6 @@ int parse_frame_view(const uint8_t* p, size_t len, FrameView* f) {
     f->col.assign(n, nullptr);
     f->gsz.assign(n, 0);
     f->csz.assign(n, 0);
-    f->owned.clear();
     for (uint32_t i = 0; i < n; ++i) f->index[i] = r.get<int32_t>();
     for (uint32_t i = 0; i < n; ++i) f->type[i] = r.get<uint8_t>();
     for (uint32_t i = 0; i < n; ++i) f->size[i] = r.get<uint32_t>();
@@ -272,48 +253,5 @@ int parse_frame_view(const uint8_t* p, size_t len, FrameView* f) {
     return PVVC_OK;
 }
 
-int frame_view_inflate(FrameView* f) {
-    auto inflate = [&](const uint8_t** at, uint32_t* sz) {
-        std::vector<uint8_t> t;
-        const int s = zstd_decompress(*at, *sz, &t);
-        if (s) return s;
-        if (t.size() > 0xFFFFFFFFull) return (int)PVVC_ERR_ZSTD;
-        f->owned.emplace_back(std::move(t));  // moving keeps the buffer where it is
-        *at = f->owned.back().data();
-        *sz = (uint32_t)f->owned.back().size();
-        return (int)PVVC_OK;
-    };
-    for (size_t i = 0; i < f->count(); ++i) {
-        if ((f->type[i] & kTypeGeoZstd) && f->gsz[i]) {
-            const int s = inflate(&f->geo[i], &f->gsz[i]);
-            if (s) return s;
-        }
-        if ((f->type[i] & kTypeColorZstd) && f->csz[i]) {
-            const int s = inflate(&f->col[i], &f->csz[i]);
-            if (s) return s;
-        }
-        f->type[i] &= static_cast<uint8_t>(~(kTypeGeoZstd | kTypeColorZstd));
-    }
-    return PVVC_OK;
-}
-
-int frame_inflate(Frame* f) {
-    for (size_t i = 0; i < f->count(); ++i) {
-        if ((f->type[i] & kTypeGeoZstd) && !f->geometry[i].empty()) {
-            std::vector<uint8_t> t;
-            int s = zstd_decompress(f->geometry[i].data(), f->geometry[i].size(), &t);
-            if (s) return s;
-            f->geometry[i].swap(t);
-        }
-        if ((f->type[i] & kTypeColorZstd) && !f->color[i].empty()) {
-            std::vector<uint8_t> t;
-            int s = zstd_decompress(f->color[i].data(), f->color[i].size(), &t);
-            if (s) return s;
-            f->color[i].swap(t);
-        }
-        f->type[i] &= static_cast<uint8_t>(~(kTypeGeoZstd | kTypeColorZstd));
-    }
-    return PVVC_OK;
-}
 
 }  // namespace pvvc

@@ -53,8 +53,7 @@ struct Frame {
 };
 
 // A parsed .frame whose slice payloads point into the parsed bytes (no
-// copies); payloads inflated from zstd live in `owned` and point there.
-// Valid while those bytes live.
+// copies).  Valid while those bytes live.
 struct FrameView {
     int32_t timestamp = -1;
     std::vector<int32_t> index;
@@ -64,7 +63,6 @@ struct FrameView {
     std::vector<float> mv;
     std::vector<const uint8_t*> geo, col;
     std::vector<uint32_t> gsz, csz;
-    std::vector<std::vector<uint8_t>> owned;
     size_t count() const { return index.size(); }
 };
 
@@ -76,20 +74,16 @@ std::vector<uint8_t> write_frame(const Frame& f);
 int parse_frame(const uint8_t* p, size_t len, Frame* out);
 // parse_frame's checks, the payloads left in place
 int parse_frame_view(const uint8_t* p, size_t len, FrameView* out);
-// zstd payloads of a view inflated into its `owned` buffers, flags cleared
-int frame_view_inflate(FrameView* f);
 
 // Frame from slices sorted by patch index (ChangeSliceToFrame, slice_io.cc:208-322).
 Frame frame_from_slices(std::vector<Slice> slices);
 
-// zstd (host-side, as the reference's GPU loader does: slice_io.cu:246-280).
-// libzstd is loaded at run time; returns false if it is not present.
+// zstd compression on the host (ZstdEncoder::Encode), for the synthetic
+// generator's zstd stage.  libzstd is loaded at run time; zstd_available()
+// is false when it is not present.  Payloads are inflated on the GPU
+// (zstd_core.h), never here.
 bool zstd_available();
-int zstd_decompress(const uint8_t* src, size_t n, std::vector<uint8_t>* out);
 int zstd_compress(const uint8_t* src, size_t n, int level, std::vector<uint8_t>* out);
 
-// Replace zstd payloads of a frame by their decompressed bytes and clear the
-// zstd type bits.  Returns 0 or a status.
-int frame_inflate(Frame* f);
 
 }  // namespace pvvc

@@ -125,7 +125,7 @@ class Batch:
 
 
 def pack_frames(frames: list[Frame], slot_base: int = 0) -> Batch:
-    """Pack frames (raw payloads, zstd already inflated) into one batch.  The
+    """Pack frames (raw payloads: pvvc.zstd.inflate_device inflates zstd ones) into one batch.  The
     slot of a slice is slot_base + its patch index."""
     nsl = sum(f.n for f in frames)
     tot = sum(_align(len(g)) + _align(len(c)) for f in frames for g, c in zip(f.geometry, f.color))
@@ -139,7 +139,7 @@ def pack_frames(frames: list[Frame], slot_base: int = 0) -> Batch:
     for f in frames:
         for i in range(f.n):
             if f.type[i] & (TYPE_GEO_ZSTD | TYPE_COLOR_ZSTD):
-                raise ValueError("pack_frames wants raw payloads (inflate zstd first)")
+                raise ValueError("pack_frames wants raw payloads (inflate zstd payloads first)")
             slot[k] = slot_base + int(f.index[i]); typ[k] = f.type[i]; size[k] = f.size[i]; qp[k] = f.qp[i]
             mv[k] = f.mv[i]
             g = f.geometry[i]; c = f.color[i]
