@@ -913,9 +913,16 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
                 ++q;
             }
     }
+    if (st->payload.ensure(total + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     // The payload bytes go into pinned memory on helper threads while this
-    // thread splits the call into runs and builds the first plan; the copy
-    // to the device waits for them.
+    // thread splits the call into runs and plans.  As soon as they are
+    // packed, the packer thread queues their copy to the device and the zstd
+    // inflation on `s`, so both run on the GPU during planning; the decode
+    // is queued after the packer has finished.
+    bool sent_ok = true;
     std::thread packer([&] {
         parallel_for(nframes, std::max(1, threads / 2), [&](int f) {
             FrameView& fr = frames[f];
@@ -926,6 +933,17 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
             }
             for (const ZJob& j : fz[f]) std::memcpy(hp + j.zoff, j.src, j.len);
         });
+        if (bytes && cudaMemcpyAsync(st->payload.p, hp, total + 16, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            sent_ok = false;
+            return;
+        }
+        if (!nz) return;
+        uint8_t* dp = static_cast<uint8_t*>(st->payload.p);
+        sent_ok = pvvc_zstd_launch(nz, dp, reinterpret_cast<const uint64_t*>(dp + a_src_off),
+                                   reinterpret_cast<const uint32_t*>(dp + a_src_len), dp,
+                                   reinterpret_cast<const uint64_t*>(dp + a_dst_off),
+                                   reinterpret_cast<const uint32_t*>(dp + a_cap), nullptr,
+                                   reinterpret_cast<int32_t*>(dp + a_status), s) == PVVC_OK;
     });
     struct JoinOnExit {
         std::thread& t;
@@ -933,18 +951,9 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
             if (t.joinable()) t.join();
         }
     } join_packer{packer};
-    bool sent = false;
-    auto send_payload = [&]() -> bool {  // once: the packed payload to the device
-        if (sent) return true;
-        sent = true;
-        packer.join();
-        if (bytes && cudaMemcpyAsync(st->payload.p, hp, total + 16, cudaMemcpyHostToDevice, s) != cudaSuccess) return false;
-        if (!nz) return true;
-        uint8_t* dp = static_cast<uint8_t*>(st->payload.p);
-        return pvvc_zstd_launch(nz, dp, reinterpret_cast<const uint64_t*>(dp + a_src_off),
-                                reinterpret_cast<const uint32_t*>(dp + a_src_len), dp,
-                                reinterpret_cast<const uint64_t*>(dp + a_dst_off), reinterpret_cast<const uint32_t*>(dp + a_cap),
-                                nullptr, reinterpret_cast<int32_t*>(dp + a_status), s) == PVVC_OK;
+    auto payload_queued = [&]() -> bool {  // the copy (and inflation) queued before the first decode
+        if (packer.joinable()) packer.join();
+        return sent_ok;
     };
     // Intra slices of different frames of one call may hit the same patch
     // index (a new GoP).  Split the call into runs of frames without a
@@ -1000,10 +1009,6 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (!merge)
         for (int32_t k = 0; k < nsl; ++k) slot[k] = index[k];
     g_stage_ms[1] = clk.lap();
-    if (st->payload.ensure(total + 16) != cudaSuccess) return PVVC_ERR_NOMEM;
-    if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
-    if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
-    if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     int rc = PVVC_OK;
     const std::vector<int32_t> one_run{0, nsl};
     const std::vector<int32_t>& runs = merge ? one_run : bounds;
@@ -1013,10 +1018,12 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         pvvc_batch_desc d{cnt,          slot.data() + first, type.data() + first, size.data() + first, qp.data() + first,
                           mv.data() + 16ull * first, goff.data() + first, gsz.data() + first, coff.data() + first,
                           csz.data() + first, oo.data() + first};
-        rc = build_plan(&d, &st->plan, nullptr, nullptr);
+        // the plan's arrays go up on `s` from pinned mirrors that stay as
+        // they are until the next plan, which follows a synchronisation
+        rc = build_plan(&d, &st->plan, nullptr, s);
         if (rc) break;
         if (st->ws.ensure(st->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
-        if (!send_payload()) return PVVC_ERR_CUDA;
+        if (!payload_queued()) return PVVC_ERR_CUDA;
         g_stage_ms[2] += clk.lap();
         rc = run_decode(&st->plan, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
                         static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
