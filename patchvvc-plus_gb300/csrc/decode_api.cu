@@ -551,6 +551,9 @@ extern "C" int pvvc_state_destroy(pvvc_state* st) {
     void* ptrs[] = {v.info, v.occ, v.mask, v.cbase, v.coff, v.ab, v.wsum, v.ctr, v.xyz, v.ref};
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    for (cudaEvent_t e : st->part_done)
+        if (e) cudaEventDestroy(e);
+    if (st->copy) cudaStreamDestroy(st->copy);
     delete st;
     return PVVC_OK;
 }
@@ -1010,8 +1013,64 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         for (int32_t k = 0; k < nsl; ++k) slot[k] = index[k];
     g_stage_ms[1] = clk.lap();
     int rc = PVVC_OK;
+    // A merged call of several GoPs is decoded in parts, split at run (GoP)
+    // boundaries near equal slice counts: each part has its own plan, and a
+    // part's xyz/rgb go back to the host on a second stream while the host
+    // plans and the GPU decodes the next part.  The device-to-host copy runs
+    // at the host link's rate and is the longest stage, so starting it early
+    // shortens the call.
+    std::vector<int32_t> cuts{0};
+    if (merge && nruns >= 2 && (xyz_host || rgb_host)) {
+        const int parts = std::min(nruns, (int)pvvc_state::kParts);
+        for (int q = 1; q < parts; ++q) {  // the run boundary nearest q/parts of the slices
+            int32_t best = -1;
+            for (int r = 1; r < nruns; ++r)
+                if (bounds[r] > cuts.back() &&
+                    (best < 0 || std::abs((int64_t)parts * bounds[r] - (int64_t)q * nsl) <
+                                     std::abs((int64_t)parts * best - (int64_t)q * nsl)))
+                    best = bounds[r];
+            if (best > cuts.back() && best < nsl) cuts.push_back(best);
+        }
+        cuts.push_back(nsl);
+        if (!st->copy && cudaStreamCreateWithFlags(&st->copy, cudaStreamNonBlocking) != cudaSuccess) return PVVC_ERR_CUDA;
+        for (cudaEvent_t& e : st->part_done)
+            if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return PVVC_ERR_CUDA;
+    }
+    const int nparts = (int)cuts.size() - 1;  // 0: not split
+    for (int h = 0; h < nparts && rc == PVVC_OK; ++h) {
+        const int32_t first = cuts[h], cnt = cuts[h + 1] - first;
+        pvvc_plan* pl = h ? &st->part_plan[h - 1] : &st->plan;
+        pvvc_batch_desc d{cnt,          slot.data() + first, type.data() + first, size.data() + first, qp.data() + first,
+                          mv.data() + 16ull * first, goff.data() + first, gsz.data() + first, coff.data() + first,
+                          csz.data() + first, oo.data() + first};
+        rc = build_plan(&d, pl, nullptr, s);
+        if (rc) break;
+        if (st->ws.ensure(pl->ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
+        if (!payload_queued()) return PVVC_ERR_CUDA;
+        g_stage_ms[2] += clk.lap();
+        rc = run_decode(pl, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
+                        static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
+                        st->ws.cap, s, nullptr);
+        if (rc) break;
+        // this part's points: [oo[first], end of its last slice), contiguous in frame order
+        const uint64_t p0 = oo[first], p1 = oo[first + cnt - 1] + size[first + cnt - 1];
+        if (cudaEventRecord(st->part_done[h], s) != cudaSuccess || cudaStreamWaitEvent(st->copy, st->part_done[h], 0) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        if (xyz_host && p1 > p0 &&
+            cudaMemcpyAsync(xyz_host + 3 * p0, static_cast<float*>(st->xyz.p) + 3 * p0, 12 * (p1 - p0), cudaMemcpyDeviceToHost,
+                            st->copy) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        if (rgb_host && p1 > p0 &&
+            cudaMemcpyAsync(rgb_host + 3 * p0, static_cast<uint8_t*>(st->rgb.p) + 3 * p0, 3 * (p1 - p0), cudaMemcpyDeviceToHost,
+                            st->copy) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        g_stage_ms[3] += clk.lap();
+    }
+    if (rc) return rc;
+    const int32_t split = nparts > 0 ? 1 : 0;
     const std::vector<int32_t> one_run{0, nsl};
-    const std::vector<int32_t>& runs = merge ? one_run : bounds;
+    const std::vector<int32_t> no_runs{0};
+    const std::vector<int32_t>& runs = split > 0 ? no_runs : merge ? one_run : bounds;
     for (size_t b = 0; b + 1 < runs.size() && rc == PVVC_OK; ++b) {
         const int32_t first = runs[b], cnt = runs[b + 1] - first;
         if (cnt <= 0) continue;
@@ -1038,10 +1097,12 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
                                      reinterpret_cast<const int32_t*>(static_cast<uint8_t*>(st->payload.p) + a_slice),
                                      static_cast<int32_t*>(st->status.p), s) != PVVC_OK)
         return PVVC_ERR_CUDA;
-    if (xyz_host && pts && cudaMemcpyAsync(xyz_host, st->xyz.p, 12 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-        return PVVC_ERR_CUDA;
-    if (rgb_host && pts && cudaMemcpyAsync(rgb_host, st->rgb.p, 3 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
-        return PVVC_ERR_CUDA;
+    if (split <= 0) {
+        if (xyz_host && pts && cudaMemcpyAsync(xyz_host, st->xyz.p, 12 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        if (rgb_host && pts && cudaMemcpyAsync(rgb_host, st->rgb.p, 3 * pts, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+    }
     if (status_host && nsl && cudaMemcpyAsync(status_host, st->status.p, 4ull * nsl, cudaMemcpyDeviceToHost, s) != cudaSuccess)
         return PVVC_ERR_CUDA;
     std::vector<int32_t> zst(nz);
@@ -1049,6 +1110,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
                               s) != cudaSuccess)
         return PVVC_ERR_CUDA;
     if (cudaStreamSynchronize(s) != cudaSuccess) return PVVC_ERR_CUDA;
+    if (split > 0 && cudaStreamSynchronize(st->copy) != cudaSuccess) return PVVC_ERR_CUDA;
     g_stage_ms[3] += clk.lap();
     for (int32_t z : zst)  // the reference throws on a payload libzstd cannot inflate
         if (z != PVVC_OK) return PVVC_ERR_ZSTD;

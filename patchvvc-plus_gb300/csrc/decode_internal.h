@@ -154,6 +154,10 @@ struct pvvc_state {
     pvvc::DevBuf payload, xyz, rgb, ws, status;
     pvvc::HostBuf h_payload;
     pvvc_plan plan;
+    static constexpr int kParts = 3;        // a multi-GoP call is decoded in up to this many parts
+    pvvc_plan part_plan[kParts - 1];        // the plans of parts 1.. (part 0 uses `plan`)
+    cudaStream_t copy = nullptr;            // device-to-host copies that overlap the next part's decode
+    cudaEvent_t part_done[kParts] = {};
 };
 
 namespace pvvc {

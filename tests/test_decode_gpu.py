@@ -255,9 +255,10 @@ def test_rlgr_golden_vectors_through_gpu_decode(pvvc_lib, oracle, torch):
 @pytest.mark.parametrize("nframes", [12, 28])
 def test_host_call_decodes_gops_in_one_plan_identically(pvvc_lib, torch, nframes):
     """pvvc_decode_frames_host with slots for one region per GoP decodes all
-    GoPs of a call in one plan (3 and 7 GoPs); the bytes equal run-by-run
-    decoding (a state with one slot per patch), and so does the next call,
-    which continues the last GoP from the patch slots."""
+    GoPs of a call together (3 and 7 GoPs, in parts split at GoP boundaries
+    whose device-to-host copies overlap the next part's decode); the bytes
+    equal run-by-run decoding (a state with one slot per patch), and so does
+    the next call, which continues the last GoP from the patch slots."""
     s = pvvc_lib.Synth(pvvc_lib.config("tiny", nframes=nframes, gof=4, seed=21))
     frames = s.frames()
     nidx = max(int(pvvc_lib.parse_frame(b).index.max()) + 1 for b in frames)
