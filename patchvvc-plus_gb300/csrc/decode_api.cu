@@ -553,7 +553,10 @@ extern "C" int pvvc_state_destroy(pvvc_state* st) {
         if (p) cudaFree(p);
     for (cudaEvent_t e : st->part_done)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : st->zdone)
+        if (e) cudaEventDestroy(e);
     if (st->copy) cudaStreamDestroy(st->copy);
+    if (st->zside) cudaStreamDestroy(st->zside);
     delete st;
     return PVVC_OK;
 }
@@ -920,44 +923,6 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     if (st->xyz.ensure(std::max<uint64_t>(12 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->rgb.ensure(std::max<uint64_t>(3 * pts, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
     if (st->status.ensure(std::max<uint64_t>(4ull * nsl, 4)) != cudaSuccess) return PVVC_ERR_NOMEM;
-    // The payload bytes go into pinned memory on helper threads while this
-    // thread splits the call into runs and plans.  As soon as they are
-    // packed, the packer thread queues their copy to the device and the zstd
-    // inflation on `s`, so both run on the GPU during planning; the decode
-    // is queued after the packer has finished.
-    bool sent_ok = true;
-    std::thread packer([&] {
-        parallel_for(nframes, std::max(1, threads / 2), [&](int f) {
-            FrameView& fr = frames[f];
-            for (size_t i = 0; i < fr.count(); ++i) {
-                const int32_t k = ffirst[f] + (int32_t)i;
-                if (gsz[k] && fr.geo[i]) std::memcpy(hp + goff[k], fr.geo[i], gsz[k]);
-                if (csz[k] && fr.col[i]) std::memcpy(hp + coff[k], fr.col[i], csz[k]);
-            }
-            for (const ZJob& j : fz[f]) std::memcpy(hp + j.zoff, j.src, j.len);
-        });
-        if (bytes && cudaMemcpyAsync(st->payload.p, hp, total + 16, cudaMemcpyHostToDevice, s) != cudaSuccess) {
-            sent_ok = false;
-            return;
-        }
-        if (!nz) return;
-        uint8_t* dp = static_cast<uint8_t*>(st->payload.p);
-        sent_ok = pvvc_zstd_launch(nz, dp, reinterpret_cast<const uint64_t*>(dp + a_src_off),
-                                   reinterpret_cast<const uint32_t*>(dp + a_src_len), dp,
-                                   reinterpret_cast<const uint64_t*>(dp + a_dst_off),
-                                   reinterpret_cast<const uint32_t*>(dp + a_cap), nullptr,
-                                   reinterpret_cast<int32_t*>(dp + a_status), s) == PVVC_OK;
-    });
-    struct JoinOnExit {
-        std::thread& t;
-        ~JoinOnExit() {
-            if (t.joinable()) t.join();
-        }
-    } join_packer{packer};
-    auto payload_queued = [&]() -> bool {  // the copy (and inflation) queued before the first decode
-        if (packer.joinable()) packer.join();
-        return sent_ok;
-    };
     // Intra slices of different frames of one call may hit the same patch
     // index (a new GoP).  Split the call into runs of frames without a
     // repeated intra index.
@@ -1011,8 +976,6 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     }
     if (!merge)
         for (int32_t k = 0; k < nsl; ++k) slot[k] = index[k];
-    g_stage_ms[1] = clk.lap();
-    int rc = PVVC_OK;
     // A merged call of several GoPs is decoded in parts, split at run (GoP)
     // boundaries near equal slice counts: each part has its own plan, and a
     // part's xyz/rgb go back to the host on a second stream while the host
@@ -1037,6 +1000,70 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
             if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return PVVC_ERR_CUDA;
     }
     const int nparts = (int)cuts.size() - 1;  // 0: not split
+    // zstd jobs of each part: jobs are in slice order, so a part's jobs are
+    // the contiguous range of those whose slice lies in it
+    std::vector<int32_t> zcut(std::max(nparts, 1) + 1, 0);
+    if (nparts > 0 && nz) {
+        const int32_t* zk = reinterpret_cast<const int32_t*>(hp + a_slice);
+        for (int h = 1; h < nparts; ++h)
+            zcut[h] = (int32_t)(std::lower_bound(zk, zk + nz, cuts[h]) - zk);
+        zcut[nparts] = nz;
+        if (!st->zside && cudaStreamCreateWithFlags(&st->zside, cudaStreamNonBlocking) != cudaSuccess) return PVVC_ERR_CUDA;
+        for (cudaEvent_t& e : st->zdone)
+            if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return PVVC_ERR_CUDA;
+    }
+    // The payload bytes go into pinned memory on helper threads while this
+    // thread splits the call into runs and plans.  As soon as they are
+    // packed, the packer thread queues their copy to the device and the zstd
+    // inflation on `s`, so both run on the GPU during planning; the decode
+    // is queued after the packer has finished.
+    bool sent_ok = true;
+    std::thread packer([&] {
+        parallel_for(nframes, std::max(1, threads / 2), [&](int f) {
+            FrameView& fr = frames[f];
+            for (size_t i = 0; i < fr.count(); ++i) {
+                const int32_t k = ffirst[f] + (int32_t)i;
+                if (gsz[k] && fr.geo[i]) std::memcpy(hp + goff[k], fr.geo[i], gsz[k]);
+                if (csz[k] && fr.col[i]) std::memcpy(hp + coff[k], fr.col[i], csz[k]);
+            }
+            for (const ZJob& j : fz[f]) std::memcpy(hp + j.zoff, j.src, j.len);
+        });
+        if (bytes && cudaMemcpyAsync(st->payload.p, hp, total + 16, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+            sent_ok = false;
+            return;
+        }
+        if (!nz) return;
+        uint8_t* dp = static_cast<uint8_t*>(st->payload.p);
+        auto inflate = [&](int32_t j0, int32_t j1, cudaStream_t on) {  // jobs [j0, j1)
+            return pvvc_zstd_launch(j1 - j0, dp, reinterpret_cast<const uint64_t*>(dp + a_src_off) + j0,
+                                    reinterpret_cast<const uint32_t*>(dp + a_src_len) + j0, dp,
+                                    reinterpret_cast<const uint64_t*>(dp + a_dst_off) + j0,
+                                    reinterpret_cast<const uint32_t*>(dp + a_cap) + j0, nullptr,
+                                    reinterpret_cast<int32_t*>(dp + a_status) + j0, on) == PVVC_OK;
+        };
+        if (nparts < 2) {
+            sent_ok = inflate(0, nz, s);
+            return;
+        }
+        // the first part's payloads on `s`, before its decode; the others on
+        // a side stream, each part's decode waiting for its own event
+        sent_ok = inflate(zcut[0], zcut[1], s) && cudaEventRecord(st->zdone[0], s) == cudaSuccess &&
+                  cudaStreamWaitEvent(st->zside, st->zdone[0], 0) == cudaSuccess;
+        for (int h = 1; h < nparts && sent_ok; ++h)
+            sent_ok = inflate(zcut[h], zcut[h + 1], st->zside) && cudaEventRecord(st->zdone[h], st->zside) == cudaSuccess;
+    });
+    struct JoinOnExit {
+        std::thread& t;
+        ~JoinOnExit() {
+            if (t.joinable()) t.join();
+        }
+    } join_packer{packer};
+    auto payload_queued = [&]() -> bool {  // the copy (and inflation) queued before the first decode
+        if (packer.joinable()) packer.join();
+        return sent_ok;
+    };
+    g_stage_ms[1] = clk.lap();
+    int rc = PVVC_OK;
     for (int h = 0; h < nparts && rc == PVVC_OK; ++h) {
         const int32_t first = cuts[h], cnt = cuts[h + 1] - first;
         pvvc_plan* pl = h ? &st->part_plan[h - 1] : &st->plan;
@@ -1047,6 +1074,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         if (rc) break;
         if (st->ws.ensure(pl->ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
         if (!payload_queued()) return PVVC_ERR_CUDA;
+        if (h > 0 && nz && cudaStreamWaitEvent(s, st->zdone[h], 0) != cudaSuccess) return PVVC_ERR_CUDA;
         g_stage_ms[2] += clk.lap();
         rc = run_decode(pl, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
                         static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,

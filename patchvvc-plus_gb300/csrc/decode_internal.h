@@ -158,6 +158,8 @@ struct pvvc_state {
     pvvc_plan part_plan[kParts - 1];        // the plans of parts 1.. (part 0 uses `plan`)
     cudaStream_t copy = nullptr;            // device-to-host copies that overlap the next part's decode
     cudaEvent_t part_done[kParts] = {};
+    cudaStream_t zside = nullptr;           // zstd inflation of the parts after the first
+    cudaEvent_t zdone[kParts] = {};
 };
 
 namespace pvvc {
