@@ -6,6 +6,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -985,12 +986,11 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     std::vector<int32_t> cuts{0};
     if (merge && nruns >= 2 && (xyz_host || rgb_host)) {
         const int parts = std::min(nruns, (int)pvvc_state::kParts);
-        for (int q = 1; q < parts; ++q) {  // the run boundary nearest q/parts of the slices
+        for (int q = 1; q < parts; ++q) {  // the run boundary nearest the q-th cut fraction of the slices
+            const double at = parts == pvvc_state::kParts ? pvvc_state::kCutAt[q - 1] : (double)q / parts;
             int32_t best = -1;
             for (int r = 1; r < nruns; ++r)
-                if (bounds[r] > cuts.back() &&
-                    (best < 0 || std::abs((int64_t)parts * bounds[r] - (int64_t)q * nsl) <
-                                     std::abs((int64_t)parts * best - (int64_t)q * nsl)))
+                if (bounds[r] > cuts.back() && (best < 0 || std::fabs(bounds[r] - at * nsl) < std::fabs(best - at * nsl)))
                     best = bounds[r];
             if (best > cuts.back() && best < nsl) cuts.push_back(best);
         }

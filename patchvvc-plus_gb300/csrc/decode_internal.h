@@ -155,6 +155,7 @@ struct pvvc_state {
     pvvc::HostBuf h_payload;
     pvvc_plan plan;
     static constexpr int kParts = 3;        // a multi-GoP call is decoded in up to this many parts
+    static constexpr double kCutAt[kParts - 1] = {1.0 / 3, 2.0 / 3};  // part boundaries, as fractions of the slices
     pvvc_plan part_plan[kParts - 1];        // the plans of parts 1.. (part 0 uses `plan`)
     cudaStream_t copy = nullptr;            // device-to-host copies that overlap the next part's decode
     cudaEvent_t part_done[kParts] = {};
