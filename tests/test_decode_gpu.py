@@ -305,3 +305,35 @@ def test_host_call_zstd_sequence_matches_raw(pvvc_lib, torch):
         with pytest.raises(pvvc_lib.PvvcError) as e:
             pvvc_lib.Decoder(nslots=256, max_leaves=4096).decode_frames(z[:t] + [pvvc_lib.write_frame(f)] + z[t + 1:])
         assert e.value.status == 9
+
+
+def test_host_call_zstd_multi_gop_parts(pvvc_lib, torch):
+    """Several GoPs with zstd payloads in one call: the call is decoded in
+    parts, each part's payloads inflated ahead of its decode (the first on
+    the call's stream, the others on a side stream).  The bytes equal the
+    raw frames' and run-by-run decoding; a corrupt zstd payload in the last
+    GoP fails the call with PVVC_ERR_ZSTD."""
+    import libzstd_ref as zr
+    nframes, gof = 24, 4
+    raw = pvvc_lib.Synth(pvvc_lib.config("tiny", nframes=nframes, gof=gof, seed=31)).frames()
+    z = pvvc_lib.Synth(pvvc_lib.config("tiny", nframes=nframes, gof=gof, seed=31, zstd_level=19)).frames()
+    assert sum(int(((pvvc_lib.parse_frame(b).type & 0x18) != 0).sum()) for b in z) > 0
+    nidx = max(int(pvvc_lib.parse_frame(b).index.max()) + 1 for b in raw)
+    x1, r1, s1 = pvvc_lib.Decoder(nslots=(nframes // gof) * nidx, max_leaves=4096).decode_frames(z)
+    x2, r2, s2 = pvvc_lib.Decoder(nslots=nidx, max_leaves=4096).decode_frames(raw)
+    assert (s1 == 0).all() and (s2 == 0).all()
+    assert np.array_equal(x1.view(np.uint32), x2.view(np.uint32)) and np.array_equal(r1, r2)
+    # truncate one zstd payload of the last frame that has one (the declared size stays)
+    t = max(t for t in range(nframes) if (pvvc_lib.parse_frame(z[t]).type & 0x18).any())
+    assert t >= nframes - gof  # in the last GoP, so in the call's last part
+    f = pvvc_lib.parse_frame(z[t])
+    i = int(np.flatnonzero(f.type & 0x18)[0])
+    if f.type[i] & 0x08:
+        f.geometry[i] = bytes(f.geometry[i])[:-2]
+    else:
+        f.color[i] = bytes(f.color[i])[:-2]
+    bad = z[:t] + [pvvc_lib.write_frame(f)] + z[t + 1:]
+    dec = pvvc_lib.Decoder(nslots=(nframes // gof) * nidx, max_leaves=4096)
+    with pytest.raises(pvvc_lib.PvvcError) as e:
+        dec.decode_frames(bad)
+    assert e.value.status == 9
