@@ -344,13 +344,15 @@ def run_ours(args):
         knn = measure_knn_colors(args, torch, pvvc, s) if args.knn else None
         zstd = measure_zstd(args, torch, pvvc, P, stream) if args.zstd_level else None
         serving = measure_serving(args, pvvc) if args.serve_streams > 0 and args.serve_seconds > 0 else None
+        serving_zstd = (measure_serving(args, pvvc, args.zstd_level)
+                        if args.serve_streams > 0 and args.serve_seconds > 0 and args.zstd_level else None)
         out = {"metric": "decoded Mpts/s (seq300, GoP 30, ~800k pts/frame)", "value": value, "unit": "Mpts/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
                "clocks": clk.summary(), "gpu_launches": info["kernels"] * args.steps, "points_per_step": P * world,
                "plan": info, "autotune_ms": tune_ms, "icp": icp, "learned_icp": learned, "encode": encode,
-               "knn_colors": knn, "zstd": zstd, "serving": serving}
+               "knn_colors": knn, "zstd": zstd, "serving": serving, "serving_zstd": serving_zstd}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
@@ -706,21 +708,24 @@ def measure_encode(args, torch, pvvc, synth, nframes):
                                        f"{cdt:.1f}s"}}
 
 
-def measure_serving(args, pvvc):
+def measure_serving(args, pvvc, zstd_level=0):
     """Playback serving: --serve-streams streams, each one GoP (30 frames, an
     intra frame + 29 predicted) of a seq300-style sequence whose point count
     is drawn U(100k, 1M) per stream, looped; frame requests arrive as a
     Poisson process at 30 fps x U(0.8, 1.2) per stream, in real time, for
     --serve-seconds; the server admits streams against a 150 GB HBM budget
     and decodes with continuous batching.  Latency = request accepted ->
-    its batch finished on the GPU."""
+    its batch finished on the GPU.  With zstd_level, every stream's payloads
+    are zstd-compressed as the reference encoder does at that level, and the
+    server inflates them on the GPU inside each batch."""
     from pvvc.serve import Server, playback
     rng = np.random.default_rng(1234)
     t0 = time.time()
     streams, pts = [], []
     for i in range(args.serve_streams):
         tp = int(rng.uniform(100_000, 1_000_000))
-        syn = pvvc.Synth(pvvc.config("seq300", nframes=30, target_points=tp, qp_i=args.qp, qp_p=args.qp, seed=1000 + i))
+        syn = pvvc.Synth(pvvc.config("seq300", nframes=30, target_points=tp, qp_i=args.qp, qp_p=args.qp, seed=1000 + i,
+                                     zstd_level=zstd_level))
         fr = syn.frames()
         syn.close()
         streams.append(fr)
@@ -734,8 +739,9 @@ def measure_serving(args, pvvc):
     res.update({"budget_gb": 150, "fps": 30, "rate_jitter": 0.2, "seconds": args.serve_seconds, "generate_s": gen_s,
                 "frame_points": {"min": int(min(pts)), "mean": float(np.mean(pts)), "max": int(max(pts))},
                 "demand_mpts_per_s": float(np.sum(pts) * 30 / 1e6),
-                "latency": "request accepted -> batch done on the GPU (CUDA event), after a 1 s warm-up"})
-    log(f"serving: p50 {res['p50_ms']:.2f} p99 {res['p99_ms']:.2f} ms, {res['mpts_per_s']:.0f} Mpts/s, "
+                "latency": "request accepted -> batch done on the GPU (CUDA event), after a 1 s warm-up",
+                "zstd_level": zstd_level})
+    log(f"serving (zstd {zstd_level}): p50 {res['p50_ms']:.2f} p99 {res['p99_ms']:.2f} ms, {res['mpts_per_s']:.0f} Mpts/s, "
         f"{res['batches']} batches")
     return res
 
