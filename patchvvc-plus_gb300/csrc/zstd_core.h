@@ -51,7 +51,6 @@ constexpr int kLLLog = 9, kMLLog = 9, kOFLog = 8;
 constexpr int kMaxLL = 35, kMaxML = 52, kMaxOF = 31;
 constexpr uint32_t kBlockMax = 128u * 1024u;
 constexpr int kSeqBatch = 32;  // sequences decoded by lane 0 ahead of the warp's copies
-constexpr int kSeqCells = (1 << kLLLog) + (1 << kMLLog) + (1 << kOFLog);
 
 struct Cell {  // one FSE decoding-table entry
     uint16_t base;  // next-state baseline
@@ -62,8 +61,7 @@ struct Cell {  // one FSE decoding-table entry
 // Everything a decoder keeps between lanes and between blocks of a frame.
 struct Shared {
     uint16_t huf[1 << kHufLogMax];  // Huffman table: (symbol << 4) | code length
-    Cell* seq;                      // the sequence tables, kSeqCells cells outside shared memory:
-                                    // literal lengths at 0, match lengths at 512, offsets at 1024
+    Cell ll[1 << kLLLog], ml[1 << kMLLog], of[1 << kOFLog];
     Cell wt[64];                    // Huffman weight table (accuracy log <= 6)
     int16_t norm[256];              // normalised counts of the table being built
     uint8_t w[256];                 // Huffman weights
@@ -496,7 +494,7 @@ ZFN void put_match(uint8_t* dst, uint64_t o, uint32_t off, uint32_t n, int lane,
 // the current log, must be defined).  Lane 0 only.  Returns the bytes used or
 // -1; *lg receives the table's accuracy log.
 ZFN int seq_table(Shared& sh, int kind, int mode, const uint8_t* q, int64_t qn, int* lg) {
-    Cell* t = sh.seq + (kind == 0 ? 0 : kind == 1 ? (1 << kLLLog) + (1 << kMLLog) : (1 << kLLLog));
+    Cell* t = kind == 0 ? sh.ll : kind == 1 ? sh.of : sh.ml;
     const int maxsym = kind == 0 ? kMaxLL : kind == 1 ? kMaxOF : kMaxML;
     const int maxlog = kind == 0 ? kLLLog : kind == 1 ? kOFLog : kMLLog;
     if (mode == 0) {
@@ -683,8 +681,7 @@ ZFN bool compressed_block(Shared& sh, FrameState& fs, const uint8_t* b, uint32_t
         const uint32_t cnt = nseq - s0 < (uint32_t)kSeqBatch ? nseq - s0 : (uint32_t)kSeqBatch;
         if (lane == 0) {
             for (uint32_t j = 0; j < cnt && !bad; ++j) {
-                const Cell cl = sh.seq[sll], co = sh.seq[(1 << kLLLog) + (1 << kMLLog) + sof],
-                           cm = sh.seq[(1 << kLLLog) + sml];
+                const Cell cl = sh.ll[sll], co = sh.of[sof], cm = sh.ml[sml];
                 const uint32_t ob = br.read(co.sym);  // offset bits, then match length, then literal length
                 const uint32_t ml = ml_base(cm.sym) + br.read(ml_bits(cm.sym));
                 const uint32_t ll = ll_base(cl.sym) + br.read(ll_bits(cl.sym));

@@ -7,10 +7,8 @@
 // The decoder itself is zstd_core.h.
 #include <cuda_runtime.h>
 
-#include <algorithm>
 #include <memory>
 #include <mutex>
-#include <vector>
 
 #include "pvvc_gb300.h"
 #include "zstd_core.h"
@@ -20,26 +18,21 @@ namespace {
 constexpr int kZWarps = 1;  // payloads per CTA (one warp each; faster than four per CTA)
 constexpr size_t kZSmem = kZWarps * sizeof(pvvc_zstd::Shared);
 
-// Persistent: CTA b inflates jobs b, b + gridDim.x, ...: src[src_off, +src_len)
-// into dst[dst_off, +dst_cap).  Its sequence tables live in its slot of
-// `seq` (global memory; only lane 0 touches them), the rest in shared memory.
+// Warp w of CTA b inflates job b * kZWarps + w: src[src_off, +src_len) into
+// dst[dst_off, +dst_cap).
 __global__ void __launch_bounds__(32 * kZWarps)
     k_zstd(int32_t njobs, const uint8_t* src, const uint64_t* __restrict__ src_off, const uint32_t* __restrict__ src_len,
            uint8_t* dst, const uint64_t* __restrict__ dst_off, const uint32_t* __restrict__ dst_cap,
-           uint32_t* __restrict__ out_len, int32_t* __restrict__ status, pvvc_zstd::Cell* seq) {
+           uint32_t* __restrict__ out_len, int32_t* __restrict__ status) {
     extern __shared__ __align__(16) unsigned char zsmem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int job = blockIdx.x * kZWarps + warp;
+    if (job >= njobs) return;  // the whole warp
     pvvc_zstd::Shared& sh = reinterpret_cast<pvvc_zstd::Shared*>(zsmem)[warp];
-    const int slot = blockIdx.x * kZWarps + warp, nslots = gridDim.x * kZWarps;
-    if (lane == 0) sh.seq = seq + (size_t)slot * pvvc_zstd::kSeqCells;
-    __syncwarp();
-    for (int job = slot; job < njobs; job += nslots) {
-        const int64_t r = pvvc_zstd::decompress(sh, src + src_off[job], src_len[job], dst + dst_off[job], dst_cap[job], lane, 32);
-        if (lane == 0) {
-            if (out_len) out_len[job] = r < 0 ? 0u : (uint32_t)r;
-            status[job] = r < 0 ? PVVC_ERR_ZSTD : PVVC_OK;
-        }
-        __syncwarp();
+    const int64_t r = pvvc_zstd::decompress(sh, src + src_off[job], src_len[job], dst + dst_off[job], dst_cap[job], lane, 32);
+    if (lane == 0) {
+        if (out_len) out_len[job] = r < 0 ? 0u : (uint32_t)r;
+        status[job] = r < 0 ? PVVC_ERR_ZSTD : PVVC_OK;
     }
 }
 
@@ -50,36 +43,19 @@ __global__ void k_zstd_merge(int32_t njobs, const int32_t* __restrict__ zstatus,
     if (j < njobs && zstatus[j] != PVVC_OK) status[zslice[j]] = PVVC_ERR_ZSTD;
 }
 
-// Per device: the shared-memory opt-in, the persistent grid and the
-// sequence-table scratch of its CTAs (allocated at the first launch on the
-// device, kept until exit).
-struct ZDevice {
-    bool ready = false;
-    int grid = 0;
-    pvvc_zstd::Cell* seq = nullptr;
-};
-std::mutex g_zdev_mu;
-ZDevice g_zdev[128];
+std::mutex g_zattr_mu;
+bool g_zattr[128] = {};
 
-const ZDevice* zstd_device() {
+bool zstd_attr_ready() {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return nullptr;
-    std::lock_guard<std::mutex> lk(g_zdev_mu);
-    ZDevice& z = g_zdev[dev];
-    if (!z.ready) {
-        int sms = 0, per_sm = 0;
-        if (cudaFuncSetAttribute(k_zstd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZSmem) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zstd, 32 * kZWarps, kZSmem) != cudaSuccess ||
-            per_sm < 1)
-            return nullptr;
-        const int grid = sms * per_sm;
-        if (cudaMalloc(&z.seq, (size_t)grid * kZWarps * pvvc_zstd::kSeqCells * sizeof(pvvc_zstd::Cell)) != cudaSuccess)
-            return nullptr;
-        z.grid = grid;
-        z.ready = true;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return false;
+    std::lock_guard<std::mutex> lk(g_zattr_mu);
+    if (!g_zattr[dev]) {
+        if (cudaFuncSetAttribute(k_zstd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kZSmem) != cudaSuccess)
+            return false;
+        g_zattr[dev] = true;
     }
-    return &z;
+    return true;
 }
 
 }  // namespace
@@ -88,10 +64,9 @@ int pvvc_zstd_launch(int32_t njobs, const uint8_t* src, const uint64_t* src_off,
                      const uint64_t* dst_off, const uint32_t* dst_cap, uint32_t* out_len, int32_t* status,
                      cudaStream_t s) {
     if (njobs == 0) return PVVC_OK;
-    const ZDevice* z = zstd_device();
-    if (!z) return PVVC_ERR_CUDA;
-    const int grid = std::min(z->grid, (njobs + kZWarps - 1) / kZWarps);
-    k_zstd<<<grid, 32 * kZWarps, kZSmem, s>>>(njobs, src, src_off, src_len, dst, dst_off, dst_cap, out_len, status, z->seq);
+    if (!zstd_attr_ready()) return PVVC_ERR_CUDA;
+    const int grid = (njobs + kZWarps - 1) / kZWarps;
+    k_zstd<<<grid, 32 * kZWarps, kZSmem, s>>>(njobs, src, src_off, src_len, dst, dst_off, dst_cap, out_len, status);
     return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
 }
 
@@ -117,9 +92,7 @@ extern "C" int pvvc_zstd_content_size(const uint8_t* src, uint64_t n, uint64_t* 
 extern "C" int pvvc_zstd_inflate_host(const uint8_t* src, uint64_t n, uint8_t* dst, uint64_t cap, uint64_t* out_len) {
     if ((!src && n) || (!dst && cap)) return PVVC_ERR_ARG;
     std::unique_ptr<pvvc_zstd::Shared> sh(new (std::nothrow) pvvc_zstd::Shared);
-    std::unique_ptr<pvvc_zstd::Cell[]> seq(new (std::nothrow) pvvc_zstd::Cell[pvvc_zstd::kSeqCells]);
-    if (!sh || !seq) return PVVC_ERR_NOMEM;
-    sh->seq = seq.get();
+    if (!sh) return PVVC_ERR_NOMEM;
     const int64_t r = pvvc_zstd::decompress(*sh, src, n, dst, cap, 0, 1);
     if (out_len) *out_len = r < 0 ? 0 : (uint64_t)r;
     return r < 0 ? PVVC_ERR_ZSTD : PVVC_OK;
