@@ -774,7 +774,7 @@ def measure_e2e(args, pvvc, frames, P, torch, stream):
         if rc:
             raise pvvc.PvvcError(rc, "pvvc_decode_frames_host")
 
-    for _ in range(2):
+    for _ in range(4):  # untimed: the first calls after pinning 3.6 GB of host outputs can stall on the host
         call()
     assert (st == 0).all()
     n = max(2, min(args.steps, 8))
