@@ -69,6 +69,8 @@ def parse_args():
                                                                "reference's configs all use 22")
     ap.add_argument("--serve-streams", type=int, default=64, help="playback streams of the serving run (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=10.0, help="real-time length of the serving run")
+    ap.add_argument("--qp-sweep", default="4,8,16,32", help="quantisation steps of the decode sweep ('' : none); each "
+                                                         "other than --qp gets its own timed pass, roofline and parity")
     return ap.parse_args()
 
 
@@ -160,9 +162,13 @@ class Clocks:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def cpu_baseline(frames, seconds):
+def cpu_baseline(frames, seconds, gpu=None):
     """The oracle port of the reference CPU decoder on a bounded sample: the
-    first frames of the sequence, in order, with all host cores."""
+    first frames of the sequence, in order, with all host cores (the decode
+    calls alone are timed).  gpu: optional (xyz, rgb, frame_first_point) of a
+    GPU pass over the same frames; every frame the oracle decodes is then
+    compared with it bit for bit, outside the timed region, and the result
+    is returned as the second value."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pvvc
     from oracle import Oracle
@@ -171,18 +177,29 @@ def cpu_baseline(frames, seconds):
     decs = [o.decoder() for _ in range(4096)]
     pts = 0
     nfr = 0
-    t0 = time.perf_counter()
-    for b in frames:
+    dt = 0.0
+    par = {"frames": 0, "points": 0, "mismatched_points": 0, "slice_errors": 0} if gpu is not None else None
+    for f, b in enumerate(frames):
         fr = pvvc.parse_frame(b)
-        _, _, st = o.decode_frame(decs, fr, nthreads=cores)
+        t0 = time.perf_counter()
+        x, r, st = o.decode_frame(decs, fr, nthreads=cores)
+        dt += time.perf_counter() - t0
         assert (st == 0).all()
         pts += fr.points
         nfr += 1
-        if time.perf_counter() - t0 > seconds:
+        if gpu is not None:
+            gx, gr, ffp = gpu
+            a, e = int(ffp[f]), int(ffp[f + 1])
+            hx, hr = gx[a:e].cpu().numpy(), gr[a:e].cpu().numpy()
+            bad = (hx.view(np.uint32) != x.view(np.uint32)).any(1) | (hr != r).any(1)
+            par["frames"] += 1
+            par["points"] += e - a
+            par["mismatched_points"] += int(bad.sum())
+        if dt > seconds:
             break
-    dt = time.perf_counter() - t0
-    return {"value": pts / dt / 1e6, "unit": "Mpts/s", "cores": cores, "kind": "port",
-            "sample": f"first {nfr} frames of the sequence ({pts} points), {dt:.1f}s"}
+    cb = {"value": pts / dt / 1e6, "unit": "Mpts/s", "cores": cores, "kind": "port",
+          "sample": f"first {nfr} frames of the sequence ({pts} points), {dt:.1f}s"}
+    return (cb, par) if gpu is not None else cb
 
 
 def run_reference(args):
@@ -215,6 +232,124 @@ def _config(args, nframes):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+class DecodePass:
+    """One device-resident decode pass of the seq300 workload at one
+    quantisation step: the sequence generated and encoded, all GoPs packed
+    into one batch (a slot region per GoP), launch shapes from the autotuner
+    (or --tune), and the whole decode captured in one CUDA graph."""
+
+    def __init__(self, args, qp, rank, local, torch, pvvc):
+        import ctypes
+        self.torch, self.pvvc = torch, pvvc
+        t0 = time.time()
+        cfg = pvvc.config("seq300", nframes=args.frames, qp_i=qp, qp_p=qp, seed=rank)
+        self.synth = pvvc.Synth(cfg)
+        self.synth.encode()
+        self.frames = self.synth.frames()
+        log(f"[rank {rank}] q={qp}: generated + encoded {len(self.frames)} frames in {time.time() - t0:.1f}s")
+        self.parsed = [pvvc.parse_frame(b) for b in self.frames]
+        gof = 30
+        ngof = (len(self.parsed) + gof - 1) // gof
+        stride = max(int(f.index.max()) + 1 for f in self.parsed)
+        batches = [pvvc.pack_frames(self.parsed[g * gof:(g + 1) * gof]) for g in range(ngof)]
+        self.batch = pvvc.concat_batches(batches, slot_stride=stride)
+        self.dec = pvvc.Decoder(nslots=stride * ngof, max_leaves=8192, max_nodes=16384)
+        dev = torch.device("cuda", local)
+        self.pay = torch.from_numpy(self.batch.payload).to(dev)
+        self.stream = torch.cuda.current_stream(dev)
+        self.sp = self.stream.cuda_stream
+        t_tune = time.time()
+        if args.tune:
+            g, m, b, l, mid, ln = (int(x) for x in args.tune.split(","))
+            self.tune, self.tune_ms = {"group_ctas_per_sm": g, "min_group": m, "rlgr_block": b, "rlgr_long_ctas": l,
+                                       "rlgr_mid_pct": mid, "rlgr_long_lanes": ln}, None
+        else:
+            self.tune, self.tune_ms = pvvc.autotune(self.batch, self.dec, self.pay.data_ptr(), reps=2, stream=self.sp)
+        log(f"[rank {rank}] q={qp}: launch shapes {self.tune} ({self.tune_ms} ms) in {time.time() - t_tune:.1f}s")
+        self.plan = pvvc.Plan(self.batch, tune=self.tune)
+        self.info = self.plan.info()
+        P = self.P = self.plan.total_points
+        self.xyz = torch.empty((P, 3), dtype=torch.float32, device=dev)
+        self.rgb = torch.empty((P, 3), dtype=torch.uint8, device=dev)
+        self.st = torch.empty(self.batch.nslices, dtype=torch.int32, device=dev)
+        self.ws = torch.empty(self.plan.workspace_bytes, dtype=torch.uint8, device=dev)
+        self.graph = self.plan.graph(self.dec, self.pay.data_ptr(), self.xyz.data_ptr(), self.rgb.data_ptr(), 0,
+                                     self.st.data_ptr(), self.ws.data_ptr(), self.ws.numel())
+        self.ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        for e in self.ev:
+            e.record(self.stream)  # torch creates the CUDA event on first record
+        torch.cuda.synchronize()
+        self.evp = (ctypes.c_void_p * 5)(*[e.cuda_event for e in self.ev])
+        self.qp = qp
+
+    def step(self, profiled=False):
+        if not profiled:
+            self.graph.launch(self.sp)
+            return
+        rc = self.pvvc.lib().pvvc_decode_profiled(self.plan.h, self.dec.h, self.pay.data_ptr(), self.xyz.data_ptr(),
+                                                  self.rgb.data_ptr(), None, self.st.data_ptr(), self.ws.data_ptr(),
+                                                  self.ws.numel(), self.sp, self.evp)
+        if rc:
+            raise self.pvvc.PvvcError(rc, "pvvc_decode")
+
+    def warm(self, n):
+        for _ in range(max(n, 3)):
+            self.step()
+        self.torch.cuda.synchronize()
+        assert (self.st.cpu().numpy() == 0).all(), "decode reported slice errors"
+
+    def stage_ms(self):
+        """Per-stage device time: the same kernels launched in stream order
+        with CUDA events between the stages, mean of three decodes."""
+        kt = np.zeros(4)
+        for _ in range(3):
+            self.step(profiled=True)
+            self.torch.cuda.synchronize()
+            kt += np.array([self.ev[i].elapsed_time(self.ev[i + 1]) for i in range(4)])
+        return kt / 3
+
+    def roofline(self, ms, peak, peaks_found):
+        alg = algorithmic_bytes(self.parsed)
+        achieved = alg / (ms / 1e3) / 1e9
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "algorithmic_bytes_per_step": alg, "peak_source": "MEASURED_PEAKS.json" if peaks_found else "fallback"}
+
+    def parity(self, seconds):
+        """The GPU pass's output against the oracle, frame by frame, on the
+        frames the CPU baseline decodes within `seconds`."""
+        return cpu_baseline(self.frames, seconds, gpu=(self.xyz, self.rgb, self.batch.frame_first_point))
+
+    def close(self):
+        for k in ("graph", "plan", "dec"):
+            o = getattr(self, k, None)
+            if o is not None:
+                o.close()
+        for k in ("xyz", "rgb", "st", "ws", "pay", "graph", "plan", "dec", "synth"):
+            setattr(self, k, None)
+        self.torch.cuda.empty_cache()
+
+
+def raht_fp64_error(frames):
+    """The decoded colours' inverse-RAHT error against the oracle's FP64
+    restatement on the first GoP of the sequence (the GPU's colours equal the
+    FP32 oracle's bit for bit, which `parity` checks)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pvvc
+    from oracle import Oracle
+    t0 = time.time()
+    r = Oracle().raht_fp64_error(frames, pvvc.parse_frame)
+    r.update({"frames": len(frames), "seconds": time.time() - t0,
+              "what": "|YUV of the FP32 inverse RAHT - YUV of its FP64 restatement|, and RGB bytes that differ"})
+    return r
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), True
+    except Exception:
+        return {}, False
+
+
 def run_ours(args):
     import torch
 
@@ -234,55 +369,10 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    s, frames = make_workload(args, rank)
-    parsed = [pvvc.parse_frame(b) for b in frames]
-    gof = 30
-    ngof = (len(parsed) + gof - 1) // gof
-    stride = max(int(f.index.max()) + 1 for f in parsed)
-    batches = [pvvc.pack_frames(parsed[g * gof:(g + 1) * gof]) for g in range(ngof)]
-    batch = pvvc.concat_batches(batches, slot_stride=stride)
-    dec = pvvc.Decoder(nslots=stride * ngof, max_leaves=8192, max_nodes=16384)
-    dev = torch.device("cuda", local)
-    pay = torch.from_numpy(batch.payload).to(dev)
-    stream = torch.cuda.current_stream(dev)
-    t_tune = time.time()
-    if args.tune:
-        g, m, b, l, mid, ln = (int(x) for x in args.tune.split(","))
-        tune, tune_ms = {"group_ctas_per_sm": g, "min_group": m, "rlgr_block": b, "rlgr_long_ctas": l,
-                         "rlgr_mid_pct": mid, "rlgr_long_lanes": ln}, None
-    else:
-        tune, tune_ms = pvvc.autotune(batch, dec, pay.data_ptr(), reps=2, stream=stream.cuda_stream)
-    log(f"[rank {rank}] launch shapes {tune} ({tune_ms} ms) in {time.time() - t_tune:.1f}s")
-    plan = pvvc.Plan(batch, tune=tune)
-    info = plan.info()
-    P = plan.total_points
-    xyz = torch.empty((P, 3), dtype=torch.float32, device=dev)
-    rgb = torch.empty((P, 3), dtype=torch.uint8, device=dev)
-    st = torch.empty(batch.nslices, dtype=torch.int32, device=dev)
-    ws = torch.empty(plan.workspace_bytes, dtype=torch.uint8, device=dev)
-    sp = stream.cuda_stream
-    graph = plan.graph(dec, pay.data_ptr(), xyz.data_ptr(), rgb.data_ptr(), 0, st.data_ptr(), ws.data_ptr(), ws.numel())
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
-    for e in ev:
-        e.record(stream)  # torch creates the CUDA event on first record
-    torch.cuda.synchronize()
-    import ctypes
-    evp = (ctypes.c_void_p * 5)(*[e.cuda_event for e in ev])
-    lib = pvvc.lib()
-
-    def step(profiled=False):
-        if not profiled:
-            graph.launch(sp)
-            return
-        rc = lib.pvvc_decode_profiled(plan.h, dec.h, pay.data_ptr(), xyz.data_ptr(), rgb.data_ptr(), None, st.data_ptr(),
-                                      ws.data_ptr(), ws.numel(), sp, evp)
-        if rc:
-            raise pvvc.PvvcError(rc, "pvvc_decode")
-
-    for _ in range(max(args.warmup, 3)):
-        step()
-    torch.cuda.synchronize()
-    assert (st.cpu().numpy() == 0).all(), "decode reported slice errors"
+    dp = DecodePass(args, args.qp, rank, local, torch, pvvc)
+    s, frames, parsed, info, P = dp.synth, dp.frames, dp.parsed, dp.info, dp.P
+    stream = dp.stream
+    dp.warm(args.warmup)
 
     # timed region
     t0 = torch.cuda.Event(enable_timing=True)
@@ -291,53 +381,46 @@ def run_ours(args):
     with Clocks(local) as clk:
         t0.record(stream)
         for _ in range(args.steps):
-            step()
+            dp.step()
         t1.record(stream)
         barrier()
     ms = t0.elapsed_time(t1) / args.steps
     if dist is not None:
-        tt = torch.tensor([ms], device=dev)
+        tt = torch.tensor([ms], device=torch.device("cuda", local))
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         ms = float(tt.item())
     value = P * world / (ms / 1e3) / 1e6
 
-    # per-kernel device time (CUDA events on the launching stream)
-    kt = np.zeros(4)
-    for _ in range(3):
-        step(profiled=True)
-        torch.cuda.synchronize()
-        kt += np.array([ev[i].elapsed_time(ev[i + 1]) for i in range(4)])
-    kt /= 3
+    kt = dp.stage_ms()
     names = ["k_tree", "memset+k_rlgr", "k_raht phase A", "k_raht phase B"]
+    # the outputs of a graph replay (the stage-timed decodes write the same bytes)
+    dp.step()
+    torch.cuda.synchronize()
 
     out = None
     if rank == 0:
-        alg = algorithmic_bytes(parsed)
-        peaks = {}
-        try:
-            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        except Exception:
-            pass
+        peaks, found = load_peaks()
         peak = float(peaks.get("hbm_gbs", 6800.0))
         # the decode pass is one CUDA-graph launch: its duration is the timed region's
-        achieved = alg / (ms / 1e3) / 1e9
+        roof = dp.roofline(ms, peak, found)
         dom = int(np.argmax(kt))
         # traffic: the kernels' DRAM bytes (ncu) plus the coefficient clear of
         # the memset nodes, which ncu does not capture (a memset writes its size)
         kdram = kernel_traffic_per_step()
-        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": (kdram + info["clear_bytes"]) if kdram is not None else None,
-                "traffic_parts": {"kernels_ncu": kdram, "memset_clear": info["clear_bytes"]},
-                "kernel": f"decode pass (one CUDA-graph launch of {info['kernels']} kernels)",
-                "dominant_kernel": names[dom],
-                "kernel_ms_stream_order": {n: float(t) for n, t in zip(names, kt)},
-                "note": "kernel_ms_stream_order: the same kernels launched in stream order with CUDA events between "
-                        "them (the graph runs the two RLGR launches side by side, so their sum exceeds the pass)",
-                "algorithmic_bytes_per_step": alg, "peak_source": "MEASURED_PEAKS.json" if peaks else "fallback"}
+        roof.update({"traffic": (kdram + info["clear_bytes"]) if kdram is not None else None,
+                     "traffic_parts": {"kernels_ncu": kdram, "memset_clear": info["clear_bytes"]},
+                     "kernel": f"decode pass (one CUDA-graph launch of {info['kernels']} kernels)",
+                     "dominant_kernel": names[dom],
+                     "kernel_ms_stream_order": {n: float(t) for n, t in zip(names, kt)},
+                     "note": "kernel_ms_stream_order: the same kernels launched in stream order with CUDA events between "
+                             "them (the graph runs the RLGR tiers side by side, so their sum exceeds the pass)"})
+        # CPU baseline, and parity of the timed pass's output on the frames it decodes
+        cb, par = dp.parity(args.cpu_seconds)
+        raht64 = raht_fp64_error(frames[:30])
         e2e = None
         if not args.no_e2e:
             e2e = measure_e2e(args, pvvc, frames, P, torch, stream)
-        cb = cpu_baseline(frames, args.cpu_seconds)
+        sweep = measure_qp_sweep(args, rank, local, torch, pvvc, dp, peak, found) if args.qp_sweep else None
         icp = measure_icp(args, torch, peak) if args.icp_pairs > 0 else None
         learned = measure_learned(args, torch, pvvc) if args.icp_pairs > 0 and args.learned else None
         encode = measure_encode(args, torch, pvvc, s, len(frames)) if args.encode else None
@@ -350,14 +433,48 @@ def run_ours(args):
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
-               "clocks": clk.summary(), "gpu_launches": info["kernels"] * args.steps, "points_per_step": P * world,
-               "plan": info, "autotune_ms": tune_ms, "icp": icp, "learned_icp": learned, "encode": encode,
-               "knn_colors": knn, "zstd": zstd, "serving": serving, "serving_zstd": serving_zstd}
+               "parity": par, "raht_fp64_error": raht64, "clocks": clk.summary(), "gpu_launches": info["kernels"] * args.steps,
+               "points_per_step": P * world, "plan": info, "autotune_ms": dp.tune_ms, "qp_sweep": sweep, "icp": icp,
+               "learned_icp": learned, "encode": encode, "knn_colors": knn, "zstd": zstd, "serving": serving,
+               "serving_zstd": serving_zstd}
         print(json.dumps(out), flush=True)
     if dist is not None:
         dist.barrier()
         dist.destroy_process_group()
     return out
+
+
+def measure_qp_sweep(args, rank, local, torch, pvvc, main, peak, found):
+    """The same decode pass at the other quantisation steps of the sweep:
+    each sequence generated at that step, autotuned, captured in a graph,
+    timed over min(steps, 20) replays after the warm-up (CUDA events), with
+    its roofline and its parity against the oracle on every frame the CPU
+    baseline decodes within --cpu-seconds / 2."""
+    res = [{"qp": args.qp, "value": None, "note": "the main line"}]
+    for q in [int(x) for x in args.qp_sweep.split(",") if x.strip()]:
+        if q == args.qp:
+            continue
+        if main is not None:
+            main.close()
+            main = None
+        dp = DecodePass(args, q, rank, local, torch, pvvc)
+        dp.warm(args.warmup)
+        n = max(1, min(args.steps, 20))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(dp.stream)
+        for _ in range(n):
+            dp.step()
+        e1.record(dp.stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / n
+        cb, par = dp.parity(args.cpu_seconds / 2)
+        res.append({"qp": q, "value": dp.P / (ms / 1e3) / 1e6, "unit": "Mpts/s", "ms_per_step": ms, "steps": n,
+                    "points_per_step": dp.P, "roofline": dp.roofline(ms, peak, found), "parity": par,
+                    "cpu_baseline": cb, "tune": dp.tune, "clear_bytes": dp.info["clear_bytes"]})
+        log(f"q={q}: {ms:.3f} ms, {dp.P / (ms / 1e3) / 1e6:.0f} Mpts/s, parity {par}")
+        dp.close()
+        del dp
+    return res
 
 
 def measure_zstd(args, torch, pvvc, P, stream):

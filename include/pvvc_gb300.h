@@ -321,10 +321,16 @@ int pvvc_icp_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off
  * grid scratch lives in one fixed device array of about 25 MB that every GPU
  * loading the library holds until exit.  Limits: npairs <= 512 and
  * total_tgt_points (which must equal tgt_off[npairs]) <= 1,048,576;
- * larger batches return PVVC_ERR_CAPACITY.  The first call on a device looks
+ * larger batches return PVVC_ERR_CAPACITY.  The kernels also check every
+ * pair's tgt_off against that capacity on the device: a pair that runs past
+ * it (a caller that understated total_tgt_points) gets NaN results, nothing
+ * is written outside the array, and pvvc_device_error_take reports
+ * PVVC_ERR_CAPACITY.  The first call in each CUDA context of a device looks
  * up the array's address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture.  All calls share the
- * array: calls that overlap on the GPU (different streams, or different host
+ * that first call returns PVVC_ERR_ARG on a stream under capture, so make
+ * it before any stream capture.  The address is cached per context: after a
+ * device reset the next call looks it up again.  All calls share the array:
+ * calls that overlap on the GPU (different streams, or different host
  * threads on the same device) race and must be serialised by the caller.
  * Results are those of pvvc_icp_batch. */
 int pvvc_icp_batch_noalloc(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
@@ -376,7 +382,9 @@ int pvvc_knn_colors_batch(int32_t npairs, const float* query_xyz, const uint64_t
  *                             added atomically; the only epilogue with splits > 1)
  *   PVVC_GEMM_MASK_BF16       C bf16 = acc where aux[M,N] (bf16) > 0, else 0
  * Stream-ordered.  A kernel whose bounded internal wait gave up sets a device
- * error code that pvvc_device_error_take returns (and clears); 0 = none. */
+ * error code that pvvc_device_error_take returns (and clears); 0 = none.
+ * The same call also returns (and clears) PVVC_ERR_CAPACITY when an ICP
+ * kernel found a pair beyond its fixed scratch (pvvc_icp_batch_noalloc). */
 #define PVVC_GEMM_BIAS_RELU_BF16 0
 #define PVVC_GEMM_F32 1
 #define PVVC_GEMM_F32_ACCUM 2

@@ -15,7 +15,8 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _ORACLE_SO = os.path.join(_HERE, "_build", "libpvvc_oracle.so")
 _REF_SO = os.path.join(_HERE, "_ref", "libpvvc_ref.so")
-REFERENCE_ROOT = "/root/reference"
+# the reference project's checkout (read-only); PVVC_REFERENCE_ROOT overrides
+REFERENCE_ROOT = os.environ.get("PVVC_REFERENCE_ROOT", "/root/reference")
 
 _u8p = C.POINTER(C.c_uint8)
 _f32p = C.POINTER(C.c_float)
@@ -103,6 +104,9 @@ class Oracle:
         lib.pvo_decoder_size.argtypes = [C.c_void_p]
         lib.pvo_decoder_get_patch.restype = C.c_int
         lib.pvo_decoder_get_patch.argtypes = [C.c_void_p, _f32p, _f32p, _u8p]
+        lib.pvo_decoder_enable_fp64.argtypes = [C.c_void_p, C.c_int]
+        lib.pvo_decoder_get_yuv_fp64.restype = C.c_int
+        lib.pvo_decoder_get_yuv_fp64.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
         lib.pvo_transform.argtypes = [_f32p, _f32p, C.c_size_t, _f32p]
         lib.pvo_decode_frame.restype = C.c_int
         lib.pvo_decode_frame.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.POINTER(_PvoFrame), _f32p, _u8p, _i32p, C.c_int]
@@ -195,6 +199,43 @@ class Oracle:
             return geo[:gsz].tobytes(), nl, cols, coefs
         finally:
             self.lib.pvo_encoder_free(h)
+
+    def raht_fp64_error(self, frames: list, parse) -> dict:
+        """The FP32 inverse RAHT (the reference's arithmetic, which the GPU
+        decoder reproduces bit for bit) against its FP64 restatement on the
+        same bitstreams: frames in order, one decoder per patch index.
+        Returns the max and mean absolute YUV error, and how many RGB bytes
+        (rounded as the CPU decoder rounds them, clamped) the FP32 result
+        changes against RGB from the FP64 colours."""
+        decs = {}
+        mx = 0.0
+        tot = 0.0
+        cnt = 0
+        rgb_diff = 0
+        rgb_max = 0
+        for b in frames:
+            fr = parse(b)
+            for i in range(fr.n):
+                idx = int(fr.index[i])
+                if idx not in decs:
+                    decs[idx] = self.decoder()
+                    decs[idx].enable_fp64()
+                d = decs[idx]
+                st = d.set_slice(int(fr.type[i]), int(fr.size[i]), int(fr.qp[i]), fr.geometry[i], fr.color[i])
+                if st:
+                    raise ValueError(f"slice status {st}")
+                _, y32, rgb32 = d.get_patch()
+                y64 = d.get_yuv_fp64()
+                e = np.abs(y32.astype(np.float64) - y64)
+                mx = max(mx, float(e.max()) if e.size else 0.0)
+                tot += float(e.sum())
+                cnt += e.size
+                r64 = _rgb_from_yuv64(y64)
+                dd = np.abs(r64.astype(np.int32) - rgb32.astype(np.int32))
+                rgb_diff += int((dd != 0).sum())
+                rgb_max = max(rgb_max, int(dd.max()) if dd.size else 0)
+        return {"yuv_max_abs": mx, "yuv_mean_abs": tot / max(cnt, 1), "values": cnt,
+                "rgb_bytes_differing": rgb_diff, "rgb_frac_differing": rgb_diff / max(cnt, 1), "rgb_max_abs": rgb_max}
 
     # ---- decoder ----
     def decoder(self):
@@ -310,6 +351,15 @@ class Oracle:
         return [out[int(a):int(a) + int(m)] for a, m in zip(qoff, qn)]
 
 
+def _rgb_from_yuv64(yuv: np.ndarray) -> np.ndarray:
+    """BT.601 YUV->RGB of common.h:154-158 evaluated in double, rounded half
+    away from zero and clamped to [0, 255]."""
+    y, u, v = yuv[:, 0], yuv[:, 1], yuv[:, 2]
+    rgb = np.stack([y + 1.402 * (v - 128), y - 0.3441 * (u - 128) - 0.7141 * (v - 128), y + 1.772 * (u - 128)], 1)
+    r = np.sign(rgb) * np.floor(np.abs(rgb) + 0.5)
+    return np.clip(r, 0, 255).astype(np.uint8)
+
+
 class OracleDecoder:
     """One persistent per-patch-index decoder (InvertRAHTOctree)."""
 
@@ -338,6 +388,19 @@ class OracleDecoder:
         if s:
             raise ValueError(f"get_patch status {s}")
         return xyz[:n], yuv[:n], rgb[:n]
+
+    def enable_fp64(self, on: bool = True):
+        """Also run the FP64 restatement of the inverse RAHT on every slice
+        (enable before the slot's intra slice)."""
+        self.o.lib.pvo_decoder_enable_fp64(self.h, 1 if on else 0)
+
+    def get_yuv_fp64(self) -> np.ndarray:
+        n = self.o.lib.pvo_decoder_size(self.h)
+        yuv = np.zeros((max(n, 1), 3), np.float64)
+        s = self.o.lib.pvo_decoder_get_yuv_fp64(self.h, yuv.ctypes.data_as(C.POINTER(C.c_double)))
+        if s:
+            raise ValueError(f"get_yuv_fp64 status {s}")
+        return yuv[:n]
 
 
 class Reference:

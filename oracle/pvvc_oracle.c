@@ -548,6 +548,9 @@ struct pvo_decoder {
     float* xyz;         /* leaf centres, leaf order */
     yuv_t* ref;         /* reference colours (intra result) */
     yuv_t* out;         /* current colours */
+    int fp64;           /* also run the FP64 restatement of the inverse RAHT */
+    double* ref64;      /* its reference colours, 3 per leaf */
+    double* out64;      /* its current colours, 3 per leaf */
 };
 
 pvo_decoder* pvo_decoder_new(void) { return (pvo_decoder*)calloc(1, sizeof(pvo_decoder)); }
@@ -558,7 +561,9 @@ static void dec_clear(pvo_decoder* d) {
     free(d->xyz);
     free(d->ref);
     free(d->out);
-    d->levels = NULL; d->xyz = NULL; d->ref = NULL; d->out = NULL;
+    free(d->ref64);
+    free(d->out64);
+    d->levels = NULL; d->xyz = NULL; d->ref = NULL; d->out = NULL; d->ref64 = NULL; d->out64 = NULL;
     d->height = 0; d->n = 0; d->valid = 0;
 }
 
@@ -711,6 +716,79 @@ static int dec_inverse_raht(pvo_decoder* d, const yuv_t* coef, int predict) {
     return PVO_OK;
 }
 
+/* The inverse RAHT of dec_inverse_raht in FP64: the same tree, weights,
+ * coefficient order and butterfly order (InvertHaarTransform,
+ * octree_base.cc:186-206, with sqrt and the divisions in double), the
+ * dequantised coefficients exact as doubles, the reference colours of a
+ * predictive slice the FP64 intra result.  It measures the error of the FP32
+ * arithmetic the reference decoder (and the product, bit for bit) uses. */
+static int dec_inverse_raht_fp64(pvo_decoder* d, const int64_t* sym, uint8_t qp, int predict) {
+    const size_t n = d->n;
+    if (!d->out64) d->out64 = (double*)calloc(3 * (n ? n : 1), sizeof(double));
+    if (!d->ref64) d->ref64 = (double*)calloc(3 * (n ? n : 1), sizeof(double));
+    if (!d->out64 || !d->ref64) return PVO_ERR_NOMEM;
+    /* coefficient k of the stream order, reversed per plane (invert_raht_octree.cc:63-69) */
+#define C64(k, p) ((double)(sym[(size_t)(p) * n + (n - 1 - (k))] * (int64_t)qp))
+    size_t widest = 1;
+    for (int i = 0; i < d->height; ++i) widest = d->levels[i].n > widest ? d->levels[i].n : widest;
+    double* cur = (double*)malloc(3 * widest * sizeof(double));
+    double* nxt = (double*)malloc(3 * widest * sizeof(double));
+    if (!cur || !nxt) { free(cur); free(nxt); return PVO_ERR_NOMEM; }
+    size_t it = 0;
+    for (int p = 0; p < 3; ++p) cur[p] = C64(0, p);
+    ++it;
+    for (int i = 0; i < d->height - 1; ++i) {
+        const level_t* L = &d->levels[i];
+        for (size_t j = 0; j < L->n; ++j) {
+            const node_t* nd = &L->v[j];
+            double g[16][3], h[8][3];
+            for (int p = 0; p < 3; ++p) g[1][p] = cur[3 * j + p];
+            for (int idx = 1; idx < 8; ++idx) {
+                const int coded = nd->weight[kNodeWeight[idx][0]] != 0 && nd->weight[kNodeWeight[idx][1]] != 0;
+                if (coded && it >= n) { free(cur); free(nxt); return PVO_ERR_SIZE; }
+                for (int p = 0; p < 3; ++p) h[idx][p] = coded ? C64(it, p) : 0.0;
+                if (coded) ++it;
+            }
+            for (int idx = 1; idx < 8; ++idx) {
+                const int w0 = nd->weight[kNodeWeight[idx][0]], w1 = nd->weight[kNodeWeight[idx][1]];
+                double a = 0, b = 0;
+                if (w0 || w1) {
+                    const double base = sqrt((double)(w0 + w1));
+                    a = sqrt((double)w0) / base;
+                    b = sqrt((double)w1) / base;
+                }
+                for (int p = 0; p < 3; ++p) {
+                    const double x = g[idx][p], y = h[idx][p];
+                    g[kNodeWeight[idx][0]][p] = a * x - b * y;
+                    g[kNodeWeight[idx][1]][p] = b * x + a * y;
+                }
+            }
+            for (int c = 0; c < 8; ++c)
+                if (nd->index[c] != -1)
+                    for (int p = 0; p < 3; ++p) nxt[3 * (size_t)nd->index[c] + p] = g[c + 8][p];
+        }
+        double* t = cur; cur = nxt; nxt = t;
+    }
+#undef C64
+    for (size_t j = 0; j < n; ++j)
+        for (int p = 0; p < 3; ++p) {
+            const double v = cur[3 * j + p];
+            if (predict) d->out64[3 * j + p] = v + d->ref64[3 * j + p];
+            else d->out64[3 * j + p] = d->ref64[3 * j + p] = v;
+        }
+    free(cur);
+    free(nxt);
+    return PVO_OK;
+}
+
+void pvo_decoder_enable_fp64(pvo_decoder* d, int on) { d->fp64 = on; }
+
+int pvo_decoder_get_yuv_fp64(const pvo_decoder* d, double* yuv) {
+    if (!d->valid || !d->fp64 || !d->out64) return PVO_ERR_NO_REFERENCE;
+    memcpy(yuv, d->out64, 3 * d->n * sizeof(double));
+    return PVO_OK;
+}
+
 /* SetSlice (invert_raht_octree.cc:22-85) */
 int pvo_decoder_set_slice(pvo_decoder* d, uint8_t type, uint32_t size, uint8_t qp,
                           const uint8_t* geo, size_t gsz, const uint8_t* col, size_t csz) {
@@ -730,14 +808,17 @@ int pvo_decoder_set_slice(pvo_decoder* d, uint8_t type, uint32_t size, uint8_t q
         coef[i].u = (float)(sym[i + size] * (int64_t)qp);
         coef[i].v = (float)(sym[i + 2 * (size_t)size] * (int64_t)qp);
     }
-    free(sym);
     if (!predict) {
+        const int fp64 = d->fp64;
         dec_clear(d);
+        d->fp64 = fp64;
         s = dec_make_tree(d, geo, gsz, size);
-        if (s) { dec_clear(d); free(coef); return s; }
+        if (s) { dec_clear(d); free(coef); free(sym); return s; }
     }
     s = dec_inverse_raht(d, coef, predict);
     free(coef);
+    if (!s && d->fp64) s = dec_inverse_raht_fp64(d, sym, qp, predict);
+    free(sym);
     if (s) return s;
     d->valid = 1;
     d->type = type;

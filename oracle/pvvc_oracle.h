@@ -78,6 +78,10 @@ size_t pvo_decoder_size(const pvo_decoder* d);
  * rounds it (common.h:154-158), clamped to [0,255] where the reference's cast
  * is undefined.  Any output pointer may be NULL. */
 int pvo_decoder_get_patch(const pvo_decoder* d, float* xyz, float* yuv, uint8_t* rgb);
+/* FP64 restatement of the inverse RAHT, run beside the FP32 one on every
+ * slice once enabled (before the slot's intra slice); the leaf YUV in double. */
+void pvo_decoder_enable_fp64(pvo_decoder* d, int on);
+int pvo_decoder_get_yuv_fp64(const pvo_decoder* d, double* yuv);
 
 /* per-point rigid transform, mv row-major (pvvc_decompression.cc:141-150) */
 void pvo_transform(const float* mv_rowmajor, const float* xyz_in, size_t n, float* xyz_out);

@@ -272,22 +272,20 @@ __global__ void __launch_bounds__(T) k_tree(const SliceWork* __restrict__ work, 
 // ---------------------------------------------------------------------------
 // k_rlgr
 //
-// Bit window: the stream continues at bit `o` (0..31, counted from the MSB)
-// of `hi`, then `mid`, then `lo` -- 96 - o >= 65 bits in registers, so any
-// 32 bits starting up to 32 bits ahead can be peeked without a refill, and
-// one advance (at most 64 bits) per loop iteration consumes a whole zero run
-// plus a Golomb-Rice code.  Words come from 16-byte blocks: `cur` holds the
-// block words are taken from, `nxt` the following block, loaded when `cur`
-// became current, four words ahead of its first use.  Blocks past the
-// payload read as zero.
+// Bit window: 64 bits `hi:lo` of the stream with the next bit at bit `o`
+// (0..31, counted from the MSB) of `hi`: peek() returns the next 32 bits with
+// one funnel shift, advance(n <= 32) consumes n of them and takes the next
+// word into the window when `o` passes 32.  Words come from 16-byte blocks:
+// `cur` holds the words not yet taken (the next one in cur.x), `nxt` the
+// following block, loaded when `cur` was refilled -- 128 bits, some 25 loop
+// iterations, ahead of its first use.  Blocks past the payload read as zero.
 struct BitReader {
     const uint4* p;      // next block to load
     const uint4* end;    // one past the last block holding payload bytes
     uint4 cur, nxt;
-    uint32_t k;          // index in cur of the next word to enter the window
-    uint32_t hi, mid, lo;
+    uint32_t ci;         // words left in cur
+    uint32_t hi, lo;
     uint32_t o;
-    uint32_t taken;      // words that have entered the window
 
     __device__ __forceinline__ uint4 load() {
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
@@ -295,58 +293,50 @@ struct BitReader {
         ++p;
         return v;
     }
-    __device__ __forceinline__ uint32_t take() {  // next big-endian word of the stream
-        const uint32_t v = k == 0 ? cur.x : k == 1 ? cur.y : k == 2 ? cur.z : cur.w;
-        ++taken;
-        if (++k == 4) {
-            k = 0;
-            cur = nxt;
-            nxt = load();
-        }
-        return __byte_perm(v, 0, 0x0123);
-    }
+    __device__ __forceinline__ static uint32_t be(uint32_t w) { return __byte_perm(w, 0, 0x0123); }
     __device__ __forceinline__ void init(const uint8_t* payload, uint64_t off, uint32_t nbytes) {
         p = reinterpret_cast<const uint4*>(payload + (off & ~15ull));
         end = reinterpret_cast<const uint4*>(payload + ((off + nbytes + 15) & ~15ull));
-        cur = load();
+        const uint4 b0 = load();
         nxt = load();
-        k = 0;
-        taken = 0;
-        hi = take();
-        mid = take();
-        lo = take();
-        o = (uint32_t)(off & 15) * 8;
-        while (o >= 32) {
-            o -= 32;
-            shift();
+        hi = be(b0.x);
+        lo = be(b0.y);
+        cur = make_uint4(b0.z, b0.w, 0u, 0u);
+        ci = 2;
+        o = 0;
+        uint32_t skip = (uint32_t)(off & 15) * 8;  // payload bytes before the slice's first byte
+        while (skip >= 32) {
+            advance(32);
+            skip -= 32;
+        }
+        advance(skip);
+    }
+    // the next 32 bits of the stream
+    __device__ __forceinline__ uint32_t peek() const { return __funnelshift_l(lo, hi, o); }
+    // consume n <= 32 bits; branch-free apart from the block refill (a lane
+    // needs one about every 25 iterations)
+    __device__ __forceinline__ void advance(uint32_t n) {
+        o += n;
+        const bool take = o >= 32;
+        o &= 31u;
+        hi = take ? lo : hi;
+        lo = take ? be(cur.x) : lo;
+        cur.x = take ? cur.y : cur.x;
+        cur.y = take ? cur.z : cur.y;
+        cur.z = take ? cur.w : cur.z;
+        ci -= take ? 1u : 0u;
+        if (ci == 0) {
+            cur = nxt;
+            ci = 4;
+            nxt = load();
         }
     }
-    __device__ __forceinline__ void shift() {
-        hi = mid;
-        mid = lo;
-        lo = take();
-    }
-    // 32 bits starting `at` bits ahead (at <= 32)
-    __device__ __forceinline__ uint32_t peek(uint32_t at = 0) const {
-        const uint32_t s = o + at;
-        const bool second = s >= 32;
-        return __funnelshift_l(second ? lo : mid, second ? mid : hi, s);  // shift taken mod 32
-    }
-    __device__ __forceinline__ void advance(uint32_t n) {  // n <= 64
-        uint32_t s = o + n;
-        if (s >= 32) {
-            s -= 32;
-            shift();
-            if (s >= 32) {
-                s -= 32;
-                shift();
-            }
-        }
-        o = s;
-    }
-    // payload bits consumed (words before hi, plus o, minus the leading skip)
-    __device__ __forceinline__ int64_t consumed(uint64_t off) const {
-        return ((int64_t)taken - 3) * 32 + (int64_t)o - (int64_t)(off & 15) * 8;
+    // payload bits consumed: the words that entered the window before hi,
+    // plus o, minus the bytes before the slice in its first block
+    __device__ __forceinline__ int64_t consumed(const uint8_t* payload, uint64_t off) const {
+        const int64_t blocks = p - reinterpret_cast<const uint4*>(payload + (off & ~15ull));  // loaded, nxt included
+        const int64_t words = (blocks - 1) * 4 - (int64_t)ci;                                  // entered the window
+        return (words - 2) * 32 + (int64_t)o - (int64_t)(off & 15) * 8;
     }
 };
 
@@ -368,6 +358,11 @@ __device__ __forceinline__ uint32_t run_ones_length(uint32_t kP, uint32_t c) {
     return S << (kP >> 2);
 }
 
+// bits [at, at + k) of w (k <= 32; k = 0 gives 0, and so does at >= 32)
+__device__ __forceinline__ uint32_t field(uint32_t w, uint32_t at, uint32_t k) {
+    return __funnelshift_rc(__funnelshift_lc(0u, w, at), 0u, 32u - k);
+}
+
 // k_rlgr: one thread per slice.  The coefficient planes are zeroed before the
 // launch, so a run of zeros only moves the output position; symbol j of a
 // plane goes to coefficient N-1-j (the stream is reversed).  The loop keeps
@@ -375,15 +370,17 @@ __device__ __forceinline__ uint32_t run_ones_length(uint32_t kP, uint32_t c) {
 // plane's symbols still to come, `left` all symbols still to come.
 //
 // One iteration = an optional zero run (run mode, kP >= 4) followed by one
-// Golomb-Rice symbol, or a run that ends the slice.  The common case is one
-// straight line that every lane of a warp executes in step, whatever mode
-// its slice is in (a lane outside run mode computes an empty run): the run's
-// leading ones are counted with one clz and summed in closed form
-// (run_ones_length), the run code and the symbol's code are both read from
-// the 96-bit window and consumed by one advance.  Rare cases leave the line:
-// a run code longer than 32 bits, a Golomb-Rice code longer than 32 bits
-// (wide remainders, the 32-ones escape), symbols of 2^23 or more, and runs
-// that reach the end of a plane.
+// Golomb-Rice symbol.  The common case -- run code and symbol code together
+// within the next 32 bits, a symbol below 2^23, the run inside the current
+// plane -- is one branch-free line that every lane of a warp executes in
+// step, whatever mode its slice is in (a lane outside run mode computes an
+// empty run): the run's leading ones are counted with one clz and summed in
+// closed form (run_ones_length), the symbol's ones with a second clz on the
+// same 32 bits, and one advance consumes both.  Its dependent chain is about
+// fifteen integer operations.  All other iterations (longer codes, the
+// 32-ones escape, wide symbols, runs across a plane or to the end of the
+// slice) take the general path, which reads the codes piece by piece as the
+// reference does; at q = 8 about one lane-iteration in 4,000 goes there.
 //
 // LANES < 32: only the first LANES lanes of each warp decode (the rest exit at
 // once), so a warp executes the union of fewer lanes' paths per iteration --
@@ -408,39 +405,63 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
     const uint32_t csz = wk.csz;
     BitReader br;
     br.init(payload, off, csz);
-    const int64_t cs = wk.coef_stride;
-    const int64_t wrap = (int64_t)(2 * N - 1) * cs;  // last coefficient of a plane -> top of the next
-    float* dst = coef + wk.coef_off + (uint64_t)(N - 1) * cs + wk.coef_lane;  // coefficient of the next symbol
+    const uint32_t csh = wk.coef_stride == 32 ? 5u : 0u;   // coefficient stride 32 (group region) or 1
+    const int64_t cs = (int64_t)1 << csh;
+    const int64_t wrap = (int64_t)(2 * N - 1) << csh;       // last coefficient of a plane -> top of the next
+    float* dst = coef + wk.coef_off + ((uint64_t)(N - 1) << csh) + wk.coef_lane;  // coefficient of the next symbol
     uint32_t rem = N;                         // symbols left in the current plane
     uint32_t left = 3u * N;                   // symbols left in the slice
     uint32_t kP = 0, kRP = 8;
     int err = PVVC_OK;
     for (;;) {
-        // ---- zero run (entropy_codec.cc:226-241) ----
-        const bool run = kP >= 4;
+        // ---- common case: the whole iteration within the next 32 bits ----
         const uint32_t v = br.peek();
-        uint32_t c = run ? __clz(~v) : 0u;       // leading ones
-        uint32_t kP2 = kP + 2 * c;               // kP after the ones
-        const uint32_t k = run ? (kP2 >> 2) : 0u;
-        uint32_t r = run ? c + 1 + k : 0u;       // bits of the run code
-        uint32_t m;                              // zeros in the run
-        if (r <= 32) {
-            const uint32_t tail = (v << c) << 1;  // the k remainder bits, left-aligned
-            m = run ? run_ones_length(kP, c) + (k ? tail >> (32 - k) : 0u) : 0u;
-        } else {  // 31+ ones, or the remainder runs past 32 bits
+        const bool run = kP >= 4;
+        const uint32_t c = run ? __clz(~v) : 0u;   // leading ones of the run code
+        const uint32_t kP2 = kP + 2 * c;           // kP after the ones
+        const uint32_t k = run ? (kP2 >> 2) : 0u;  // remainder bits of the run code
+        const uint32_t r = run ? c + 1 + k : 0u;   // bits of the run code
+        const uint32_t v2 = __funnelshift_lc(0u, v, r);  // the symbol's code, left-aligned
+        const uint32_t q = __clz(~v2);             // its leading ones
+        const uint32_t kR = kRP >> 2;
+        const uint32_t nb = r + q + 1 + kR;        // bits of the whole iteration
+        const uint32_t u = (q << kR) | field(v2, q + 1, kR);
+        const uint32_t m = run ? run_ones_length(kP, c) + field(v, c + 1, k) : 0u;  // zeros of the run
+        if (nb <= 32 && u < (1u << 23) && m < rem) {
+            br.advance(nb);
+            dst -= (int64_t)m << csh;
+            const uint32_t zz = u + (uint32_t)run;  // Unsign2Sign(u + after_run) * qp, stored unless zero
+            const int32_t sym = (int32_t)(zz >> 1) ^ -(int32_t)(zz & 1);
+            if (sym) *dst = __int2float_rn(sym * qp);
+            // adaptation (entropy_codec.cc:245-281); here p = u >> kR = q
+            kRP = q ? min(kRP + q - 1, kRlMaxRP) : (kRP < 2 ? 0u : kRP - 2);
+            kP = (run || u) ? (kP2 ? kP2 - kRlD1 : 0u) : kP2 + kRlU0;  // D0 = D1 = 1
+            left -= m + 1;
+            rem -= m + 1;
+            const bool end_of_plane = rem == 0;
+            dst += end_of_plane ? wrap : -cs;
+            rem = end_of_plane ? N : rem;
+            if (left == 0) break;
+            continue;
+        }
+        // ---- general path: the codes read piece by piece ----
+        uint32_t mm = 0;   // zeros in the run
+        uint32_t kPr = kP;  // kP after the run's ones
+        if (run) {
+            // zero run (entropy_codec.cc:226-233): ones, a zero, k remainder bits
             uint64_t m64 = 0;
             uint32_t kk = kP >> 2;
-            kP2 = kP;
+            uint32_t cc;
             int guard = 0;
             do {
-                c = __clz(~br.peek());
-                for (uint32_t i = 0; i < c; ++i) {
+                cc = __clz(~br.peek());
+                for (uint32_t i = 0; i < cc; ++i) {
                     m64 += 1ull << (kk & 31);
-                    kP2 += kRlU1;
-                    kk = kP2 >> 2;
+                    kPr += kRlU1;
+                    kk = kPr >> 2;
                 }
-                br.advance(c);
-            } while (c == 32 && ++guard < 64);
+                br.advance(cc);
+            } while (cc == 32 && ++guard < 64);
             br.advance(1);
             if (kk > 31) {
                 err = PVVC_ERR_OVERRUN;
@@ -448,76 +469,52 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
             }
             m64 += br.peek() >> (32 - kk);
             br.advance(kk);
-            m = m64 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)m64;
-            r = 0;  // consumed
+            mm = m64 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)m64;
         }
-        // skip m zeros (they may cross plane boundaries)
+        // skip mm zeros (they may cross plane boundaries)
         {
-            uint32_t z = m < left ? m : left;
+            uint32_t z = mm < left ? mm : left;
             left -= z;
-            if (z < rem) {
-                dst -= (int64_t)z * cs;
-                rem -= z;
-            } else {
-                while (z >= rem && rem) {
-                    z -= rem;
-                    dst += (int64_t)(2 * N - rem) * cs;  // to the top of the next plane
-                    rem = N;
-                }
-                dst -= (int64_t)z * cs;
-                rem -= z;
+            while (z >= rem && rem) {
+                z -= rem;
+                dst += (int64_t)(2 * N - rem) << csh;  // to the top of the next plane
+                rem = N;
             }
+            dst -= (int64_t)z << csh;
+            rem -= z;
         }
-        if (left == 0) {
-            br.advance(r);
-            break;
-        }
-        // ---- Golomb-Rice symbol (GRRead, entropy_codec.cc:196-205) ----
-        const uint32_t kR = kRP >> 2;
-        const uint32_t v2 = br.peek(r);
-        const uint32_t q = __clz(~v2);
-        const uint32_t len = q + 1 + kR;
-        uint32_t u, pq;
+        if (left == 0) break;
+        // Golomb-Rice symbol (GRRead, entropy_codec.cc:196-205)
+        const uint32_t w = br.peek();
+        const uint32_t qq = __clz(~w);
         uint64_t uw;
-        bool wide;  // u does not fit the fast symbol path
-        if (len <= 32) {  // the whole code is in this peek
-            u = (q << kR) | ((v2 >> (32 - len)) & ((1u << kR) - 1u));
-            br.advance(r + len);
-            pq = q;
-            uw = u;
-            wide = u >= (1u << 23);
-        } else if (q < 32) {
-            br.advance(r + q + 1);
-            const uint32_t rr = kR == 32 ? br.peek() : (br.peek() >> (32 - kR));
-            br.advance(kR);
-            uw = ((uint64_t)q << kR) | rr;
-            u = (uint32_t)uw | (uint32_t)(uw >> 32);  // nonzero iff uw is
-            pq = q;
-            wide = true;
+        uint32_t pq;
+        if (qq < 32) {
+            br.advance(qq + 1);
+            uint32_t rr = 0;
+            if (kR) {
+                rr = kR >= 32 ? br.peek() : (br.peek() >> (32 - kR));
+                br.advance(kR >= 32 ? 32u : kR);
+            }
+            uw = ((uint64_t)qq << kR) | rr;
+            pq = qq;
         } else {  // 32 ones: a raw 32-bit value follows
-            br.advance(r + 32);
-            u = br.peek();
             br.advance(32);
-            uw = u;
+            const uint32_t raw = br.peek();
+            br.advance(32);
+            uw = raw;
             // p may be far above the kRP cap; any p > kRlMaxRP saturates
             // kRP + p - 1 at the cap (kRP >= 0), so clamp p to kRlMaxRP + 1,
             // not kRlMaxRP (that would leave kRP one short when kRP = 0)
-            const uint32_t t2 = kR >= 32 ? 0u : (u >> kR);
+            const uint32_t t2 = kR >= 32 ? 0u : (raw >> kR);
             pq = t2 > kRlMaxRP ? kRlMaxRP + 1 : t2;
-            wide = true;
         }
-        // adaptation (entropy_codec.cc:245-281)
         kRP = pq ? min(kRP + pq - 1, kRlMaxRP) : (kRP < 2 ? 0u : kRP - 2);
-        kP = (run || u) ? (kP2 ? kP2 - kRlD1 : 0u) : kP2 + kRlU0;  // D0 = D1 = 1
-        // Unsign2Sign(u + after_run) * qp, stored unless zero
-        if (!wide) {
-            const uint32_t zz = u + (uint32_t)run;
-            const int32_t sym = (int32_t)(zz >> 1) ^ -(int32_t)(zz & 1);
-            if (sym) *dst = __int2float_rn(sym * qp);
-        } else {
+        kP = (run || uw) ? (kPr ? kPr - kRlD1 : 0u) : kPr + kRlU0;
+        {
             const uint64_t zz = uw + (uint64_t)run;
             const long long sym = (long long)(zz >> 1) ^ -(long long)(zz & 1);
-            *dst = __ll2float_rn(sym * (long long)qp);
+            if (sym) *dst = __ll2float_rn(sym * (long long)qp);
         }
         --left;
         const bool end_of_plane = --rem == 0;
@@ -527,7 +524,7 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
     }
     // bits consumed vs the payload (the reference reads past it, which is undefined)
     if (!err) {
-        if (br.consumed(off) > 8ll * csz) err = PVVC_ERR_OVERRUN;
+        if (br.consumed(payload, off) > 8ll * csz) err = PVVC_ERR_OVERRUN;
     }
     rstatus[item] = err;
 }

@@ -507,10 +507,16 @@ extern "C" int pvvc_gemm_bf16(int32_t M, int32_t N, int32_t K, const void* A, in
     return pvvc::gemm_bf16(M, N, K, A, lda, B, ldb, C, ldc, bias, aux, ldaux, epilogue, splits, (cudaStream_t)stream);
 }
 
+namespace pvvc {
+int icp_error_take(int* code);  // icp_kernels.cu
+}
+
 extern "C" int pvvc_device_error_take(int32_t* code) {
     if (!code) return PVVC_ERR_ARG;
-    int v = 0;
-    const int rc = pvvc::device_error_take(&v);
-    *code = v;
+    int v = 0, w = 0;
+    int rc = pvvc::device_error_take(&v);
+    const int rc2 = pvvc::icp_error_take(&w);
+    if (rc == PVVC_OK) rc = rc2;
+    *code = v ? v : w;
     return rc;
 }

@@ -51,6 +51,11 @@ __host__ __device__ constexpr uint64_t cell_ints(int kmul, uint64_t npoints, int
     return (uint64_t)kmul * npoints + 65ull * (uint64_t)npairs;
 }
 
+// Error word of the fixed-scratch entry point: set (to PVVC_ERR_CAPACITY) by
+// a k_grid CTA whose pair lies beyond the scratch's point capacity; read and
+// cleared by icp_error_take (pvvc_device_error_take).
+__device__ int g_icp_error = 0;
+
 struct GridHdr {  // per pair
     float lo[3];
     float h;
@@ -62,13 +67,20 @@ struct GridHdr {  // per pair
 template <int T>
 __global__ void __launch_bounds__(T) k_grid(const float* __restrict__ pts, const uint32_t* __restrict__ off,
                                             const float* __restrict__ xform, GridHdr* __restrict__ hdr,
-                                            int* __restrict__ cstart, float4* __restrict__ sorted, int kmul) {
+                                            int* __restrict__ cstart, float4* __restrict__ sorted, int kmul,
+                                            uint32_t cap = 0xFFFFFFFFu) {
     extern __shared__ int s_cnt[];  // kGridSmem bytes: budget + 1 counters
     __shared__ float s_red[T / 32][6];
     __shared__ float s_box[6];
     __shared__ int s_warp[T / 32];
     const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t a = off[pair], b = off[pair + 1], n = b - a;
+    // cap: the point capacity of a fixed scratch (pvvc_icp_batch_noalloc).
+    // A pair whose offsets run past it, or backwards, writes nothing.
+    if (b > cap || a > b) {
+        if (tid == 0) atomicExch(&g_icp_error, PVVC_ERR_CAPACITY);
+        return;
+    }
     const int C = cell_budget(kmul, n);
     float M[12];
     const bool tr = xform != nullptr;
@@ -358,7 +370,8 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp(const float* __restrict__ s
                                                      const int* __restrict__ cstart, const float4* __restrict__ tsorted,
                                                      int kmul, const float* __restrict__ init, pvvc_icp_params prm,
                                                      float* __restrict__ T_out, float* __restrict__ mse_out,
-                                                     int32_t* __restrict__ iters_out, uint8_t* __restrict__ conv_out) {
+                                                     int32_t* __restrict__ iters_out, uint8_t* __restrict__ conv_out,
+                                                     uint32_t cap = 0xFFFFFFFFu) {
     __shared__ double s_part[kIcpThreads / 32][kNSum];
     __shared__ double s_T[16];
     __shared__ float s_Tf[12];
@@ -366,8 +379,17 @@ __global__ void __launch_bounds__(kIcpThreads) k_icp(const float* __restrict__ s
     __shared__ double s_prev;
     const int pair = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const uint32_t a = soff[pair], b = soff[pair + 1];
-    const GridHdr g = hdr[pair];
     const uint32_t tb = toff[pair];
+    if (toff[pair + 1] > cap || tb > toff[pair + 1]) {  // k_grid built no grid for this pair
+        if (tid < 16) T_out[pair * 16 + tid] = __int_as_float(0x7fc00000);
+        if (tid == 0) {
+            if (mse_out) mse_out[pair] = __int_as_float(0x7fc00000);
+            if (iters_out) iters_out[pair] = 0;
+            if (conv_out) conv_out[pair] = 0;
+        }
+        return;
+    }
+    const GridHdr g = hdr[pair];
     const int* cs = cstart + cell_base(kmul, tb, pair);
     const bool empty_t = toff[pair + 1] == tb;
     if (tid == 0) {
@@ -689,22 +711,82 @@ static __device__ __align__(256) unsigned char g_icp_noalloc_scratch[pvvc::kNoAl
 namespace pvvc {
 namespace {
 std::mutex g_noalloc_mu;
-void* g_noalloc_addr[128] = {};  // device address of the array, per device ordinal
-bool g_grid_attr[128] = {};      // k_grid's shared-memory opt-in done, per device ordinal
+// Per device ordinal, the CUDA context the cached values belong to: the
+// array's device address and k_grid's shared-memory opt-in live only as long
+// as that context, so a device reset (a new primary context) makes the next
+// call look them up again.
+struct CtxCache {
+    unsigned long long ctx = 0;  // cuCtxGetId of the context; 0 = nothing cached
+    void* addr = nullptr;        // device address of the fixed array
+    bool grid_attr = false;      // k_grid's opt-in done
+};
+CtxCache g_ctx_cache[128];
+
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+// Unique id of the calling thread's current context (0 if it cannot be read).
+unsigned long long current_ctx_id() {
+    static CtxGetCurrentFn get_cur = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_cur = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(p);
+    });
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_cur || !get_id || get_cur(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// The cache entry of the current device, reset when its context changed.
+// Called with g_noalloc_mu held; the runtime has made the context current.
+CtxCache* ctx_cache(int dev) {
+    if (dev < 0 || dev >= 128) return nullptr;
+    unsigned long long id = current_ctx_id();
+    if (id == 0 && cudaFree(nullptr) == cudaSuccess) id = current_ctx_id();  // no context yet: create it
+    CtxCache& c = g_ctx_cache[dev];
+    if (id == 0 || c.ctx != id) c = CtxCache{id, nullptr, false};
+    return &c;
+}
 }  // namespace
 
 // k_grid's histogram takes kGridSmem (64 KB) of dynamic shared memory, above
-// the 48 KB default: opt in once per device (the caller's current device).
+// the 48 KB default: opt in once per device context (the caller's current
+// device).
 bool grid_attr_ready() {
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return false;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_grid_attr[dev]) {
+    CtxCache* c = ctx_cache(dev);
+    if (!c) return false;
+    if (!c->grid_attr) {
         if (cudaFuncSetAttribute(k_grid<256>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGridSmem) != cudaSuccess)
             return false;
-        g_grid_attr[dev] = true;
+        c->grid_attr = c->ctx != 0;  // without a context id, opt in on every call
     }
     return true;
+}
+
+// Reads and clears the ICP error word (PVVC_ERR_CAPACITY from a pair that lay
+// beyond the fixed scratch of pvvc_icp_batch_noalloc).
+int icp_error_take(int* code) {
+    int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_icp_error, sizeof(int)) != cudaSuccess) return PVVC_ERR_CUDA;
+    if (v) {
+        const int z = 0;
+        if (cudaMemcpyToSymbol(g_icp_error, &z, sizeof(int)) != cudaSuccess) return PVVC_ERR_CUDA;
+    }
+    *code = v;
+    return PVVC_OK;
 }
 
 __global__ void k_max2(const float* __restrict__ a, int n, float* __restrict__ o) {
@@ -854,30 +936,54 @@ extern "C" int pvvc_icp_batch_noalloc(int32_t npairs, const float* src_xyz, cons
     if (npairs > kNoAllocMaxPairs || total_tgt_points > kNoAllocMaxTgtPoints) return PVVC_ERR_CAPACITY;
     if (npairs == 0) return PVVC_OK;
     if (!src_xyz || !src_off || !tgt_xyz || !tgt_off || !T_out) return PVVC_ERR_ARG;
-    // first call on each device: look up the array's device address with that
-    // device current (the caller's current device)
+    cudaStream_t s = (cudaStream_t)stream;
+    // the array's device address, looked up with the caller's device current
+    // on the first call in each context; that lookup is not allowed while the
+    // stream is being captured
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return PVVC_ERR_CUDA;
-    if (dev < 0 || dev >= 128) return PVVC_ERR_ARG;
     void* base = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_addr[dev]) {
+        CtxCache* c = ctx_cache(dev);
+        if (!c) return PVVC_ERR_ARG;
+        if (!c->addr) {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) return PVVC_ERR_CUDA;
+            if (cs != cudaStreamCaptureStatusNone) return PVVC_ERR_ARG;
             void* p = nullptr;
             if (cudaGetSymbolAddress(&p, g_icp_noalloc_scratch) != cudaSuccess || !p) return PVVC_ERR_CUDA;
-            g_noalloc_addr[dev] = p;
+            c->addr = c->ctx ? p : nullptr;  // without a context id, look it up on every call
+            base = p;
+        } else {
+            base = c->addr;
         }
-        base = g_noalloc_addr[dev];
     }
     uint8_t* b = static_cast<uint8_t*>(base);
     GridHdr* hdr = reinterpret_cast<GridHdr*>(b + kNoAllocHdrOff);
     int* cstart = reinterpret_cast<int*>(b + kNoAllocCellOff);
     float4* sorted = reinterpret_cast<float4*>(b + kNoAllocSortedOff);
-    cudaStream_t s = (cudaStream_t)stream;
     if (!grid_attr_ready()) return PVVC_ERR_CUDA;
-    k_grid<256><<<npairs, 256, kGridSmem, s>>>(tgt_xyz, tgt_off, nullptr, hdr, cstart, sorted, kNoAllocCellMul);
-    k_icp<<<npairs, kIcpThreads, 0, s>>>(src_xyz, src_off, tgt_off, hdr, cstart, sorted, kNoAllocCellMul, init, *params, T_out,
-                                         mse_out,
-                                         iters_out, converged_out);
-    return cudaGetLastError() == cudaSuccess ? PVVC_OK : PVVC_ERR_CUDA;
+    // The kernels bound every pair by the array's point capacity themselves
+    // (a pair past it gets NaN results and PVVC_ERR_CAPACITY in
+    // pvvc_device_error_take), whatever total_tgt_points says.  Launched
+    // through cudaLaunchKernel so that the return code is these launches'
+    // own, not an error left by earlier unrelated work.
+    const float* nul = nullptr;
+    int kmul = kNoAllocCellMul;
+    uint32_t cap = (uint32_t)kNoAllocMaxTgtPoints;
+    void* ga[] = {(void*)&tgt_xyz, (void*)&tgt_off, (void*)&nul, (void*)&hdr, (void*)&cstart, (void*)&sorted, (void*)&kmul,
+                  (void*)&cap};
+    if (cudaLaunchKernel((const void*)k_grid<256>, dim3(npairs), dim3(256), ga, kGridSmem, s) != cudaSuccess)
+        return PVVC_ERR_CUDA;
+    const int* ccs = cstart;
+    const float4* csorted = sorted;
+    const GridHdr* chdr = hdr;
+    pvvc_icp_params prm = *params;
+    void* ia[] = {(void*)&src_xyz, (void*)&src_off, (void*)&tgt_off, (void*)&chdr, (void*)&ccs, (void*)&csorted,
+                  (void*)&kmul, (void*)&init, (void*)&prm, (void*)&T_out, (void*)&mse_out, (void*)&iters_out,
+                  (void*)&converged_out, (void*)&cap};
+    if (cudaLaunchKernel((const void*)k_icp, dim3(npairs), dim3(kIcpThreads), ia, 0, s) != cudaSuccess)
+        return PVVC_ERR_CUDA;
+    return PVVC_OK;
 }

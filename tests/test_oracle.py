@@ -82,3 +82,28 @@ def test_oracle_decoder_matches_reference_on_random_patches(oracle, reference):
             xr, rr = dr.get_patch(nl)
             assert np.array_equal(xo, xr)
             assert rgb_matches(ro, rr, yo).all()
+
+
+def test_fp64_inverse_raht_restatement(pvvc_lib, oracle):
+    """The FP64 restatement of the inverse RAHT (octree_base.cc:186-206 in
+    double) against the FP32 one the reference (and the GPU, bit for bit)
+    uses: on the reference-written golden GoP and on a synthetic GoP the FP32
+    colours stay within 1e-3 of the FP64 ones, and RGB bytes differ by at most
+    one.  An intra slice quantised with step 1 reproduces the encoder's leaf
+    colours within the rounding of the symbols (|error| <= 0.5 per
+    coefficient, orthonormal transform: at most 0.5 * sqrt(N) in norm)."""
+    r = oracle.raht_fp64_error(golden_frames("raw"), pvvc_lib.parse_frame)
+    assert r["values"] > 0 and r["yuv_max_abs"] < 1e-3 and r["rgb_max_abs"] <= 1
+    s = pvvc_lib.Synth(pvvc_lib.config("gof8", seed=5))
+    r = oracle.raht_fp64_error(s.frames(), pvvc_lib.parse_frame)
+    assert r["yuv_max_abs"] < 1e-3 and r["rgb_max_abs"] <= 1 and r["rgb_frac_differing"] < 1e-3
+    rng = np.random.default_rng(2)
+    xyz = rng.integers(0, 40, (600, 3)).astype(np.float32)
+    yuv = rng.uniform(16, 235, (600, 3)).astype(np.float32)
+    geo, nl, leaf = pvvc_lib.patch_leaf_yuv(xyz, yuv[None])
+    _, _, cols = pvvc_lib.encode_patch_gop(xyz, yuv[None], [1])
+    d = oracle.decoder()
+    d.enable_fp64()
+    assert d.set_slice(1, nl, 1, geo, cols[0]) == 0
+    err = d.get_yuv_fp64() - leaf[0].astype(np.float64)
+    assert np.sqrt((err ** 2).sum(0)).max() <= 0.5 * np.sqrt(nl) + 1e-6
