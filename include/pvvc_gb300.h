@@ -188,9 +188,12 @@ int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* cons
 /* Wall-clock milliseconds of the stages of the calling thread's last
  * pvvc_decode_frames_host (no counterpart in the reference):
  * out[0] parse (with the zstd frame headers), out[1] the batch description and the split into
- * runs, out[2] planning (host) and plan upload, with the payload packed into
- * pinned memory beside it, out[3] H2D + decode + D2H up to the final stream
- * synchronisation.  Fills min(n, 4) values; zeros before any call. */
+ * runs, out[2] planning (host) and plan upload, out[3] the wait for the
+ * last device-to-host copies (and, for a call decoded in one piece, its
+ * decode), out[4] the wait for the payload packed into pinned memory beside
+ * the planning, out[5] workspace growth, out[6] queuing the decode kernels,
+ * out[7] queuing the device-to-host copies of each part.  Fills min(n, 8)
+ * values; zeros before any call. */
 int pvvc_host_stage_times(double* out, int32_t n);
 
 /* ---- zstd payloads on the GPU ----------------------------------------------
@@ -342,6 +345,28 @@ int pvvc_icp_batch_noalloc(int32_t npairs, const float* src_xyz, const uint32_t*
 int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
                          const uint32_t* tgt_off, const float* T, float* mse_out, void* workspace,
                          uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream);
+
+/* ---- reconstruction quality --------------------------------------------
+ * Replaces common::MSE::SetClouds + Compute + GetGeoMSEs/GetYMSEs/GetUMSEs/
+ * GetVMSEs (src/registration/registration_base.cc:160-240), the measure the
+ * decoder turns into PSNR (src/codec/pvvc_decompression.cc:151-171:
+ * PSNR_geo = 10 log10(1024^2 / max(geo)), PSNR_Y = 10 log10(256^2 / max(Y))).
+ * Two coloured clouds A (the reference's p_, e.g. the source frame) and B
+ * (q_, e.g. the decoded frame), device memory: xyz float[3n], rgb uint8[3n].
+ * For every point of A its exact nearest neighbour in B (FP32 squared
+ * distance, x, y, z accumulated in order; the lower index of B among equal
+ * distances), and the squared differences of their BT.601 Y, U, V
+ * (ColorYUV(const PointXYZRGB&), include/common/common.h:94-98); then the
+ * same for B against A.  mse_out: device double[8] = {geo A->B, geo B->A,
+ * Y A->B, Y B->A, U A->B, U B->A, V A->B, V B->A}, each the mean over the
+ * query cloud (summed in double; the reference sums in float).  An empty
+ * cloud gives -1 on its side and 0 on the other, as the reference returns
+ * early.  Stream-ordered; workspace of pvvc_cloud_quality_workspace_size
+ * bytes, 256-byte aligned. */
+int pvvc_cloud_quality_workspace_size(uint64_t npoints_a, uint64_t npoints_b, uint64_t* bytes);
+int pvvc_cloud_quality(uint64_t npoints_a, const float* xyz_a, const uint8_t* rgb_a, uint64_t npoints_b,
+                       const float* xyz_b, const uint8_t* rgb_b, double* mse_out, void* workspace,
+                       uint64_t workspace_bytes, void* stream);
 
 /* ---- colour interpolation of the GoP encoder -------------------------------
  * Replaces GoPEncoding::Interpolation and the k-NN loop of GoPEncoding::Encode

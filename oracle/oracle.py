@@ -118,6 +118,9 @@ class Oracle:
                                           C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
             lib.pvo_cloud_mse.restype = C.c_float
             lib.pvo_cloud_mse.argtypes = [_f32p, C.c_size_t, _f32p, C.c_size_t]
+            lib.pvo_cloud_quality.restype = C.c_int
+            lib.pvo_cloud_quality.argtypes = [_f32p, _u8p, C.c_size_t, _f32p, _u8p, C.c_size_t, C.c_int,
+                                              C.POINTER(C.c_double)]
             lib.pvo_knn_colors.restype = C.c_int
             lib.pvo_knn_colors.argtypes = [_f32p, C.c_size_t, _f32p, _u8p, C.c_size_t, C.c_int, C.c_int, _f32p]
             lib.pvo_knn_colors_batch.restype = C.c_int
@@ -319,6 +322,19 @@ class Oracle:
         b = np.ascontiguousarray(b, np.float32)
         return float(self.lib.pvo_cloud_mse(_ptr(a, _f32p), a.shape[0], _ptr(b, _f32p), b.shape[0]))
 
+    def cloud_quality(self, p_xyz, p_rgb, q_xyz, q_rgb, brute: bool = False) -> np.ndarray:
+        """common::MSE::Compute of p against q: [geo p->q, geo q->p, Y, Y, U, U, V, V]."""
+        a = np.ascontiguousarray(p_xyz, np.float32).reshape(-1, 3)
+        ac = np.ascontiguousarray(p_rgb, np.uint8).reshape(-1, 3)
+        b = np.ascontiguousarray(q_xyz, np.float32).reshape(-1, 3)
+        bc = np.ascontiguousarray(q_rgb, np.uint8).reshape(-1, 3)
+        out = np.zeros(8, np.float64)
+        st = self.lib.pvo_cloud_quality(_ptr(a, _f32p), _ptr(ac, _u8p), a.shape[0], _ptr(b, _f32p), _ptr(bc, _u8p),
+                                        b.shape[0], 1 if brute else 0, out.ctypes.data_as(C.POINTER(C.c_double)))
+        if st:
+            raise RuntimeError(f"cloud_quality status {st}")
+        return out
+
     # ---- colour interpolation (GoP_encoding.cc:73-95,131-150) ----
     def knn_colors(self, q, src, rgb, k=10, brute=False) -> np.ndarray:
         """YUV [nq,3] interpolated at the query points from the k nearest
@@ -436,6 +452,8 @@ class Reference:
         lib.ref_decoder_get_patch.argtypes = [C.c_void_p, _f32p, _u8p, C.c_size_t]
         lib.ref_cloud_mse.restype = C.c_float
         lib.ref_cloud_mse.argtypes = [_f32p, C.c_size_t, _f32p, C.c_size_t]
+        lib.ref_mse_compute.restype = C.c_int
+        lib.ref_mse_compute.argtypes = [_f32p, _u8p, C.c_size_t, _f32p, _u8p, C.c_size_t, C.POINTER(C.c_double)]
         lib.ref_gop_encode.restype = C.c_int
         lib.ref_gop_encode.argtypes = [_f32p, C.c_size_t, C.c_int, C.POINTER(_f32p), C.POINTER(_u8p),
                                        C.POINTER(C.c_size_t), C.c_int, C.c_int, C.c_int, _f32p, _u8p, C.c_size_t,
@@ -451,6 +469,18 @@ class Reference:
         a = np.ascontiguousarray(a, np.float32)
         b = np.ascontiguousarray(b, np.float32)
         return float(self.lib.ref_cloud_mse(_ptr(a, _f32p), a.shape[0], _ptr(b, _f32p), b.shape[0]))
+
+    def mse_compute(self, p_xyz, p_rgb, q_xyz, q_rgb) -> np.ndarray:
+        """The reference's common::MSE::Compute: [geo p->q, geo q->p, Y, Y, U, U, V, V]."""
+        a = np.ascontiguousarray(p_xyz, np.float32).reshape(-1, 3)
+        ac = np.ascontiguousarray(p_rgb, np.uint8).reshape(-1, 3)
+        b = np.ascontiguousarray(q_xyz, np.float32).reshape(-1, 3)
+        bc = np.ascontiguousarray(q_rgb, np.uint8).reshape(-1, 3)
+        out = np.zeros(8, np.float64)
+        if self.lib.ref_mse_compute(_ptr(a, _f32p), _ptr(ac, _u8p), a.shape[0], _ptr(b, _f32p), _ptr(bc, _u8p), b.shape[0],
+                                    out.ctypes.data_as(C.POINTER(C.c_double))):
+            raise RuntimeError("reference MSE::Compute threw")
+        return out
 
     def gop_encode(self, fit_xyz, srcs, rgbs, k, qp_i, qp_p):
         """GoPEncoding::Encode on one patch's GoP (ref_gop_encode): the

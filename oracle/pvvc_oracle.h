@@ -130,6 +130,11 @@ int pvo_icp_batch(int npairs, const float* src, const uint32_t* soff, const floa
                   const pvo_icp_params* p, float* T, float* fit, int* iters, int* conv, int nthreads);
 /* Symmetric mean squared NN distance, max of both directions. */
 float pvo_cloud_mse(const float* a, size_t na, const float* b, size_t nb);
+/* common::MSE::Compute: geometric and Y/U/V errors of p against q and q
+ * against p (out[8]: geo p->q, geo q->p, Y, Y, U, U, V, V); brute: exact
+ * search over all points instead of the grid. */
+int pvo_cloud_quality(const float* p, const uint8_t* prgb, size_t np, const float* q, const uint8_t* qrgb, size_t nq,
+                      int brute, double* out);
 
 /* Colour interpolation of the GoP encoder (GoPEncoding::Interpolation and its
  * k-NN loop, src/patch/GoP_encoding.cc:73-95,131-150): for each query point,

@@ -490,6 +490,70 @@ static void fgrid_knn(const fgrid_t* g, const float* src, float qx, float qy, fl
     }
 }
 
+/* ColorYUV(const pcl::PointXYZRGB&) (include/common/common.h:94-98) */
+static void yuv_of_rgb(const uint8_t* c, float* o) {
+    const float r = c[0], g = c[1], b = c[2];
+    o[0] = r * 0.299f + g * 0.587f + b * 0.114f;
+    o[1] = r * -0.168736f - g * 0.331264f + b * 0.5f + 128;
+    o[2] = r * 0.5f - g * 0.418688f - b * 0.081312f + 128;
+}
+
+/* common::MSE::Compute (src/registration/registration_base.cc:168-223):
+ * every point of p against its nearest neighbour in q, then q against p,
+ * accumulated as the reference does -- the geometric error in float, each
+ * colour term as a double square added into a float sum -- and divided by
+ * the cloud sizes.  out = {geo p->q, geo q->p, Y.., Y.., U.., U.., V.., V..}.
+ * An empty cloud sets its side to -1 and the call returns early (:170-177).
+ * Neighbour ties go to the lower index (PCL's k-d tree leaves it open). */
+int pvo_cloud_quality(const float* p, const uint8_t* prgb, size_t np, const float* q, const uint8_t* qrgb, size_t nq,
+                      int brute, double* out) {
+    float m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (!np) m[0] = m[2] = m[4] = m[6] = -1.0f;
+    if (!nq) m[1] = m[3] = m[5] = m[7] = -1.0f;
+    if (np && nq) {
+        for (int dir = 0; dir < 2; ++dir) {
+            const float* a = dir ? q : p;
+            const uint8_t* ac = dir ? qrgb : prgb;
+            const size_t na = dir ? nq : np;
+            const float* b = dir ? p : q;
+            const uint8_t* bc = dir ? prgb : qrgb;
+            const size_t nb = dir ? np : nq;
+            fgrid_t g;
+            memset(&g, 0, sizeof(g));
+            if (!brute && fgrid_build(&g, b, nb)) return PVO_ERR_NOMEM;
+            float geo = 0, ey = 0, eu = 0, ev = 0;
+            for (size_t i = 0; i < na; ++i) {
+                knn_t s;
+                s.n = 0;
+                s.k = 1;
+                const float* x = a + 3 * i;
+                if (brute)
+                    for (size_t j = 0; j < nb; ++j) knn_offer(&s, sqdist(b + 3 * j, x[0], x[1], x[2]), (int)j);
+                else
+                    fgrid_knn(&g, b, x[0], x[1], x[2], &s);
+                geo += s.d[0];
+                float ya[3], yb[3];
+                yuv_of_rgb(ac + 3 * i, ya);
+                yuv_of_rgb(bc + 3 * (size_t)s.i[0], yb);
+                /* pp is the point of p, qq its neighbour in q (and the other way round) */
+                const float dy = dir ? yb[0] - ya[0] : ya[0] - yb[0];
+                const float du = dir ? yb[1] - ya[1] : ya[1] - yb[1];
+                const float dv = dir ? yb[2] - ya[2] : ya[2] - yb[2];
+                ey = (float)((double)ey + pow((double)dy, 2));
+                eu = (float)((double)eu + pow((double)du, 2));
+                ev = (float)((double)ev + pow((double)dv, 2));
+            }
+            if (!brute) fgrid_free(&g);
+            m[dir] = geo / (float)na;
+            m[2 + dir] = ey / (float)na;
+            m[4 + dir] = eu / (float)na;
+            m[6 + dir] = ev / (float)na;
+        }
+    }
+    for (int k = 0; k < 8; ++k) out[k] = m[k];
+    return PVO_OK;
+}
+
 int pvo_knn_colors(const float* q, size_t nq, const float* src, const uint8_t* rgb, size_t ns, int k, int brute,
                    float* yuv_out) {
     if (!src || !rgb || !ns || k < 1 || k > KNN_MAX || (nq && (!q || !yuv_out))) return PVO_ERR_ARG;

@@ -349,6 +349,36 @@ float ref_cloud_mse(const float* a, size_t na, const float* b, size_t nb) {
     }
 }
 
+/* ---- common::MSE::Compute (src/registration/registration_base.cc:160-240)
+ * of coloured clouds p and q, through the reference's own class; out =
+ * {geo p->q, geo q->p, Y.., Y.., U.., U.., V.., V..}.  Returns 0, or -1 when
+ * the reference threw. */
+int ref_mse_compute(const float* p, const uint8_t* prgb, size_t np, const float* q, const uint8_t* qrgb, size_t nq,
+                    double* out) {
+    auto coloured = [](const float* xyz, const uint8_t* rgb, size_t n) {
+        pcl::PointCloud<pcl::PointXYZRGB>::Ptr c = make_cloud(xyz, n);
+        for (size_t i = 0; i < n; ++i) {
+            (*c)[i].r = rgb[3 * i];
+            (*c)[i].g = rgb[3 * i + 1];
+            (*c)[i].b = rgb[3 * i + 2];
+        }
+        return c;
+    };
+    try {
+        common::MSE m;
+        m.SetClouds(coloured(p, prgb, np), coloured(q, qrgb, nq));
+        m.Compute();
+        const std::pair<float, float> v[4] = {m.GetGeoMSEs(), m.GetYMSEs(), m.GetUMSEs(), m.GetVMSEs()};
+        for (int k = 0; k < 4; ++k) {
+            out[2 * k] = v[k].first;
+            out[2 * k + 1] = v[k].second;
+        }
+        return 0;
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
 int ref_change_slice_to_frame(const char* dir, const char* out_name) {
     try {
         io::ChangeSliceToFrame(dir, out_name);

@@ -778,7 +778,8 @@ extern "C" int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const
 
 
 namespace {
-thread_local double g_stage_ms[4] = {0, 0, 0, 0};  // see pvvc_host_stage_times
+constexpr int kStages = 8;
+thread_local double g_stage_ms[kStages] = {};  // see pvvc_host_stage_times
 
 // A zstd payload of a parsed frame, left compressed for the GPU.
 struct ZJob {
@@ -824,7 +825,7 @@ struct StageClock {
 
 extern "C" int pvvc_host_stage_times(double* out, int32_t n) {
     if (!out || n < 0) return PVVC_ERR_ARG;
-    for (int i = 0; i < n && i < 4; ++i) out[i] = g_stage_ms[i];
+    for (int i = 0; i < n && i < kStages; ++i) out[i] = g_stage_ms[i];
     return PVVC_OK;
 }
 
@@ -1072,14 +1073,17 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
                           csz.data() + first, oo.data() + first};
         rc = build_plan(&d, pl, nullptr, s);
         if (rc) break;
+        g_stage_ms[2] += clk.lap();
         if (st->ws.ensure(pl->ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
+        g_stage_ms[5] += clk.lap();
         if (!payload_queued()) return PVVC_ERR_CUDA;
         if (h > 0 && nz && cudaStreamWaitEvent(s, st->zdone[h], 0) != cudaSuccess) return PVVC_ERR_CUDA;
-        g_stage_ms[2] += clk.lap();
+        g_stage_ms[4] += clk.lap();
         rc = run_decode(pl, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
                         static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
                         st->ws.cap, s, nullptr);
         if (rc) break;
+        g_stage_ms[6] += clk.lap();
         // this part's points: [oo[first], end of its last slice), contiguous in frame order
         const uint64_t p0 = oo[first], p1 = oo[first + cnt - 1] + size[first + cnt - 1];
         if (cudaEventRecord(st->part_done[h], s) != cudaSuccess || cudaStreamWaitEvent(st->copy, st->part_done[h], 0) != cudaSuccess)
@@ -1092,7 +1096,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
             cudaMemcpyAsync(rgb_host + 3 * p0, static_cast<uint8_t*>(st->rgb.p) + 3 * p0, 3 * (p1 - p0), cudaMemcpyDeviceToHost,
                             st->copy) != cudaSuccess)
             return PVVC_ERR_CUDA;
-        g_stage_ms[3] += clk.lap();
+        g_stage_ms[7] += clk.lap();
     }
     if (rc) return rc;
     const int32_t split = nparts > 0 ? 1 : 0;

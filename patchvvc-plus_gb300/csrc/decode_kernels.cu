@@ -275,30 +275,60 @@ __global__ void __launch_bounds__(T) k_tree(const SliceWork* __restrict__ work, 
 // Bit window: 64 bits `hi:lo` of the stream with the next bit at bit `o`
 // (0..31, counted from the MSB) of `hi`: peek() returns the next 32 bits with
 // one funnel shift, advance(n <= 32) consumes n of them and takes the next
-// word into the window when `o` passes 32.  Words come from 16-byte blocks:
-// `cur` holds the words not yet taken (the next one in cur.x), `nxt` the
-// following block, loaded when `cur` was refilled -- 128 bits, some 25 loop
-// iterations, ahead of its first use.  Blocks past the payload read as zero.
+// word into the window when `o` passes 32.  Words come from 16-byte payload
+// blocks staged in shared memory: each thread owns a ring of kRing block
+// slots (slot j of thread t at s_ring[j * blockDim + t], so a warp's 16-byte
+// reads are conflict-free), filled by cp.async kRing - 1 blocks -- about 180
+// loop iterations -- ahead of their use, so the serial chain does not wait
+// on global memory.  `cur` holds the words of the current block not yet
+// taken (the next one in cur.x).  Blocks past the payload are zero-filled.
+constexpr int kRing = 8;
+
+__device__ __forceinline__ void ring_fetch(uint4* slot, const uint4* src, bool valid) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(slot);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(valid ? 16 : 0) : "memory");
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+// every block but the kRing - 2 most recently requested has landed
+__device__ __forceinline__ void ring_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(kRing - 2) : "memory"); }
+
 struct BitReader {
-    const uint4* p;      // next block to load
+    const uint4* p;      // next block to request
     const uint4* end;    // one past the last block holding payload bytes
-    uint4 cur, nxt;
+    const uint4* first;  // the slice's first block
+    uint4* ring;         // this thread's slot 0
+    uint32_t stride;     // between slots (uint4 units)
+    uint32_t rb;         // blocks read from the ring
+    uint4 cur;
     uint32_t ci;         // words left in cur
     uint32_t hi, lo;
     uint32_t o;
 
-    __device__ __forceinline__ uint4 load() {
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (p < end) v = __ldg(p);
+    __device__ __forceinline__ static uint32_t be(uint32_t w) { return __byte_perm(w, 0, 0x0123); }
+    __device__ __forceinline__ void request() {  // block p into the slot of the block read last
+        const bool valid = p < end;
+        ring_fetch(ring + ((rb + kRing - 1) & (kRing - 1)) * stride, valid ? p : first, valid);
         ++p;
+    }
+    __device__ __forceinline__ uint4 next_block() {
+        ring_wait();
+        const uint4 v = ring[(rb & (kRing - 1)) * stride];
+        request();
+        ++rb;
         return v;
     }
-    __device__ __forceinline__ static uint32_t be(uint32_t w) { return __byte_perm(w, 0, 0x0123); }
-    __device__ __forceinline__ void init(const uint8_t* payload, uint64_t off, uint32_t nbytes) {
-        p = reinterpret_cast<const uint4*>(payload + (off & ~15ull));
+    __device__ __forceinline__ void init(const uint8_t* payload, uint64_t off, uint32_t nbytes, uint4* ring0, uint32_t str) {
+        first = p = reinterpret_cast<const uint4*>(payload + (off & ~15ull));
         end = reinterpret_cast<const uint4*>(payload + ((off + nbytes + 15) & ~15ull));
-        const uint4 b0 = load();
-        nxt = load();
+        ring = ring0;
+        stride = str;
+        rb = 0;
+        for (int j = 0; j < kRing - 1; ++j) {  // blocks 0 .. kRing-2 into slots 0 .. kRing-2
+            const bool valid = p < end;
+            ring_fetch(ring + j * stride, valid ? p : first, valid);
+            ++p;
+        }
+        const uint4 b0 = next_block();
         hi = be(b0.x);
         lo = be(b0.y);
         cur = make_uint4(b0.z, b0.w, 0u, 0u);
@@ -326,18 +356,18 @@ struct BitReader {
         cur.z = take ? cur.w : cur.z;
         ci -= take ? 1u : 0u;
         if (ci == 0) {
-            cur = nxt;
+            cur = next_block();
             ci = 4;
-            nxt = load();
         }
     }
     // payload bits consumed: the words that entered the window before hi,
     // plus o, minus the bytes before the slice in its first block
-    __device__ __forceinline__ int64_t consumed(const uint8_t* payload, uint64_t off) const {
-        const int64_t blocks = p - reinterpret_cast<const uint4*>(payload + (off & ~15ull));  // loaded, nxt included
-        const int64_t words = (blocks - 1) * 4 - (int64_t)ci;                                  // entered the window
+    __device__ __forceinline__ int64_t consumed(uint64_t off) const {
+        const int64_t words = (int64_t)rb * 4 - (int64_t)ci;  // entered the window
         return (words - 2) * 32 + (int64_t)o - (int64_t)(off & 15) * 8;
     }
+    // no copy of this thread's left in flight (before its shared memory is reused)
+    __device__ __forceinline__ void drain() const { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 };
 
 constexpr uint32_t kRlU0 = 3, kRlU1 = 2, kRlD0 = 1, kRlD1 = 1, kRlMaxRP = 32 * 4;
@@ -403,8 +433,9 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
     }
     const uint64_t off = wk.col_off;
     const uint32_t csz = wk.csz;
+    extern __shared__ uint4 s_ring[];  // kRing * blockDim payload blocks
     BitReader br;
-    br.init(payload, off, csz);
+    br.init(payload, off, csz, s_ring + threadIdx.x, blockDim.x);
     const uint32_t csh = wk.coef_stride == 32 ? 5u : 0u;   // coefficient stride 32 (group region) or 1
     const int64_t cs = (int64_t)1 << csh;
     const int64_t wrap = (int64_t)(2 * N - 1) << csh;       // last coefficient of a plane -> top of the next
@@ -524,8 +555,9 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
     }
     // bits consumed vs the payload (the reference reads past it, which is undefined)
     if (!err) {
-        if (br.consumed(payload, off) > 8ll * csz) err = PVVC_ERR_OVERRUN;
+        if (br.consumed(off) > 8ll * csz) err = PVVC_ERR_OVERRUN;
     }
+    br.drain();
     rstatus[item] = err;
 }
 
@@ -1196,6 +1228,7 @@ cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices
                         int32_t* rstatus, int block, int smem, cudaStream_t s) {
     if (nslices <= 0) return cudaSuccess;
     const int grid = (nslices + block - 1) / block;
+    smem = smem > block * kRing * 16 ? smem : block * kRing * 16;  // at least the payload rings
     switch (block) {
         case 32: k_rlgr<32><<<grid, 32, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
         case 64: k_rlgr<64><<<grid, 64, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
@@ -1212,6 +1245,7 @@ cudaError_t launch_rlgr_long(const SliceWork* work, const int32_t* order, int ns
                              int32_t* rstatus, int lanes, int smem, cudaStream_t s) {
     if (nslices <= 0) return cudaSuccess;
     static_assert(kRlgrLongBlock == 128, "a long CTA holds 128 slices");
+    static_assert(kRlgrLongSmem >= 512 * kRing * 16, "the long launch's reservation holds its payload rings");
     const int grid = (nslices + kRlgrLongBlock - 1) / kRlgrLongBlock;
     switch (lanes) {
         case 8: k_rlgr<512, 8><<<grid, 512, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;

@@ -112,6 +112,8 @@ SIGNATURES = [
     ("pvvc_icp_batch_noalloc", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, C.POINTER(IcpParams), vp, vp, vp, vp,
                                          C.c_uint64, vp]),
     ("pvvc_cloud_mse_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
+    ("pvvc_cloud_quality_workspace_size", C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]),
+    ("pvvc_cloud_quality", C.c_int, [C.c_uint64, vp, vp, C.c_uint64, vp, vp, vp, vp, C.c_uint64, vp]),
     ("pvvc_knn_colors_workspace_size", C.c_int, [C.c_int32, C.c_uint64, u64p]),
     ("pvvc_knn_colors_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, C.c_int32, vp, vp, vp, vp, vp, C.c_uint64,
                                         C.c_uint64, vp]),

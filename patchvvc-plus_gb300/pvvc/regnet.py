@@ -171,11 +171,18 @@ def register_learned(net: RegNet, b, refine_iters: int = 10, accept_rel: float =
     the identity (50 iterations, the encoder's default) registers it.
     judge="plain": plain ICP is run for every pair as well (`plain` = its
     (T, mse) if already computed) and a pair keeps the refined result only if
-    its MSE is no worse.  Returns device tensors (T [n,16], mse [n]) and
+    its MSE is no worse.  judge="tight": ICP refines the proposal to plain
+    ICP's own stopping rule (at most 50 iterations, |dMSE| < 1e-6), with no
+    fallback.  Returns device tensors (T [n,16], mse [n]) and
     {"fallback": pairs registered by plain ICP, "accepted": device bool [n]}."""
     import torch
     data = PairData(b)
     T0 = net.propose(data, seed=seed, stream=torch.cuda.current_stream().cuda_stream)
+    if judge == "tight":
+        # ICP from the proposal to plain ICP's own stopping rule (at most 50
+        # iterations, |dMSE| < 1e-6): both runs end in a converged ICP minimum
+        b.run(init=T0, max_iter=50, fitness_eps=0.0, transform_eps=0.0, mse_abs_eps=1e-6)
+        return b.T.clone(), b.mse.clone(), {"fallback": 0, "accepted": b.conv.clone().bool()}
     b.run(init=T0, max_iter=refine_iters, fitness_eps=accept_rel, transform_eps=0.0, mse_abs_eps=1e-6)
     T = b.T.clone()
     mse = b.mse.clone()

@@ -28,8 +28,12 @@ It compiles the reference's sources against the oracle's shim headers
                    114-158) of 6 cloud pairs (its k-d tree the shim's exact
                    search; the sums in float, in point order).
 
-`python tests/golden/make_golden.py gop_encode` (or `cloud_mse`) writes only
-that fixture.
+  cloud_quality.npz common::MSE::Compute (src/registration/registration_base.cc:
+                   160-223) of 6 coloured cloud pairs: geometric and Y/U/V
+                   errors both ways, summed in float as the reference does.
+
+`python tests/golden/make_golden.py gop_encode` (or `cloud_mse`,
+`cloud_quality`) writes only that fixture.
 
 Patches: 4 from the seeded synthetic surface generator plus 4 edge cases
 (a single point, two distant points, a full 8^3 cube, and points that share
@@ -207,15 +211,46 @@ def make_cloud_mse(ref: Reference, seed: int = 43):
                         b=np.concatenate(b_list), b_off=off(b_list), mse=mse)
 
 
+def make_cloud_quality(ref: Reference, seed: int = 47):
+    """Coloured clouds: voxel clouds with many equidistant neighbours, and
+    synthetic patches against a moved, jittered, recoloured copy (a decoded
+    frame against its source)."""
+    import pvvc
+    rng = np.random.default_rng(seed)
+    a_list, b_list, ac_list, bc_list = [], [], [], []
+    for _ in range(3):
+        a_list.append(rng.integers(0, 30, (int(rng.integers(50, 900)), 3)).astype(np.float32))
+        b_list.append(rng.integers(0, 30, (int(rng.integers(50, 900)), 3)).astype(np.float32))
+    s = pvvc.Synth(pvvc.config("gof8", nframes=1, gof=1, seed=seed))
+    for p in range(3):
+        x = s.patch(0, p)[0].astype(np.float32)
+        R = rot(rng.normal(size=3), 1.0)
+        y = ((x - x.mean(0)) @ R.T + x.mean(0) + rng.uniform(-1, 1, 3) + rng.normal(0, 0.3, x.shape)).astype(np.float32)
+        a_list.append(x)
+        b_list.append(np.round(y).astype(np.float32))
+    for k, (a, b) in enumerate(zip(a_list, b_list)):
+        ac_list.append(rng.integers(0, 256, a.shape).astype(np.uint8))
+        if k < 3:  # unrelated colours
+            bc_list.append(rng.integers(0, 256, b.shape).astype(np.uint8))
+        else:      # the same points' colours with N(0, 6) noise
+            bc_list.append(np.clip(np.round(ac_list[-1] + rng.normal(0, 6, b.shape)), 0, 255).astype(np.uint8))
+    mse = np.array([ref.mse_compute(a, ac, b, bc) for a, ac, b, bc in zip(a_list, ac_list, b_list, bc_list)], np.float64)
+    off = lambda xs: np.concatenate([[0], np.cumsum([len(x) for x in xs])]).astype(np.int64)
+    np.savez_compressed(os.path.join(HERE, "cloud_quality.npz"), a=np.concatenate(a_list), a_rgb=np.concatenate(ac_list),
+                        a_off=off(a_list), b=np.concatenate(b_list), b_rgb=np.concatenate(bc_list), b_off=off(b_list),
+                        mse=mse)
+
+
 def main():
     ref = Reference()
-    one = {"gop_encode": make_gop_encode, "cloud_mse": make_cloud_mse}
+    one = {"gop_encode": make_gop_encode, "cloud_mse": make_cloud_mse, "cloud_quality": make_cloud_quality}
     if len(sys.argv) == 2 and sys.argv[1] in one:
         one[sys.argv[1]](ref)
         print(sys.argv[1] + ".npz written to", HERE)
         return
     make_gop_encode(ref)
     make_cloud_mse(ref)
+    make_cloud_quality(ref)
     rng = np.random.default_rng(2024)
     make_rlgr(ref, rng)
 
