@@ -62,6 +62,7 @@ def parse_args():
     ap.add_argument("--icp-pairs", type=int, default=4096, help="batched ICP workload size (0: skip)")
     ap.add_argument("--no-learned", dest="learned", action="store_false", help="skip the learned-ICP comparison")
     ap.add_argument("--no-psnr", dest="psnr", action="store_false", help="skip the encode-flow PSNR comparison")
+    ap.add_argument("--no-fitting", dest="fitting", action="store_false", help="skip the fitting-cloud measurement")
     ap.add_argument("--no-encode", dest="encode", action="store_false", help="skip the GPU encoder measurement")
     ap.add_argument("--learned-train-pairs", type=int, default=32768, help="pairs to train on when no weights are committed")
     ap.add_argument("--learned-train-epochs", type=int, default=8)
@@ -425,6 +426,7 @@ def run_ours(args):
         icp = measure_icp(args, torch, peak) if args.icp_pairs > 0 else None
         learned = measure_learned(args, torch, pvvc) if args.icp_pairs > 0 and args.learned else None
         encode = measure_encode(args, torch, pvvc, s, len(frames)) if args.encode else None
+        fitting = measure_fitting(args, torch, pvvc) if args.fitting else None
         knn = measure_knn_colors(args, torch, pvvc, s) if args.knn else None
         zstd = measure_zstd(args, torch, pvvc, P, stream) if args.zstd_level else None
         serving = measure_serving(args, pvvc) if args.serve_streams > 0 and args.serve_seconds > 0 else None
@@ -436,7 +438,7 @@ def run_ours(args):
                "config": _config(args, len(frames)), "roofline": roof, "cpu_baseline": cb, "e2e": e2e,
                "parity": par, "raht_fp64_error": raht64, "clocks": clk.summary(), "gpu_launches": info["kernels"] * args.steps,
                "points_per_step": P * world, "plan": info, "autotune_ms": dp.tune_ms, "qp_sweep": sweep, "icp": icp,
-               "learned_icp": learned, "encode": encode, "knn_colors": knn, "zstd": zstd, "serving": serving,
+               "learned_icp": learned, "encode": encode, "fitting": fitting, "knn_colors": knn, "zstd": zstd, "serving": serving,
                "serving_zstd": serving_zstd}
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -783,6 +785,61 @@ def measure_psnr(args, torch, pvvc, net):
     return res
 
 
+def measure_fitting(args, torch, pvvc):
+    """The GoP encoder's fitting clouds (pvvc_fitting_clouds: PatchFitting::
+    Compute with direct clustering) for every patch of the config-2
+    sequence's first GoP: 30 registered patches each (the frames' patches
+    moved, jittered, voxelised and registered back by the true motion), one
+    batched call; the octree descent on the host, the k-means of every
+    clustering cell on the GPU.  CPU baseline: the oracle's restatement (one
+    thread per GoP, as the reference's thread pool runs one patch index per
+    task) on a bounded sample of patch GoPs; its clouds are also the check."""
+    from pvvc import encode_flow as ef
+    from pvvc.fitting import Fitter
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    t0 = time.time()
+    syn = pvvc.Synth(pvvc.config("seq300", nframes=30, qp_i=args.qp, qp_p=args.qp, seed=0))
+    src = ef.GopSource(syn, 0, seed=3)
+    gops = []
+    for p in range(src.npatch):
+        pats = [src.fit[p]]
+        for f in range(1, src.nframes):
+            inv = np.linalg.inv(src.true_mv[p][f].astype(np.float64))
+            pats.append((src.frames[p][f][0].astype(np.float64) @ inv[:3, :3].T + inv[:3, 3]).astype(np.float32))
+        gops.append(pats)
+    setup = time.time() - t0
+    seeds = np.arange(1, len(gops) + 1, dtype=np.uint32)
+    fitter = Fitter()
+    fitter.fit(gops[:4], seeds=seeds[:4])
+    times = []
+    for _ in range(3):
+        c0 = time.perf_counter()
+        clouds, st = fitter.fit(gops, seeds=seeds)
+        times.append(time.perf_counter() - c0)
+    sec = float(np.median(times))
+    pts = sum(x.shape[0] for g in gops for x in g)
+    o = Oracle()
+    c0 = time.perf_counter()
+    ns = same = 0
+    cpts = 0
+    while ns < len(gops) and time.perf_counter() - c0 < args.cpu_seconds / 3:
+        want, _ = o.fitting_cloud(gops[ns], seed=int(seeds[ns]))
+        same += int(np.array_equal(want.view(np.uint32), clouds[ns].view(np.uint32)))
+        cpts += sum(x.shape[0] for x in gops[ns])
+        ns += 1
+    cdt = time.perf_counter() - c0
+    log(f"fitting: {len(gops)} patch GoPs, {pts} points, {st['cells']} cells in {sec * 1e3:.1f} ms")
+    return {"patch_gops": len(gops), "points": pts, "fitting_points": int(sum(c.shape[0] for c in clouds)),
+            "call_ms": sec * 1e3, "call_ms_runs": [round(t * 1e3, 2) for t in times], "mpts_per_s": pts / sec / 1e6,
+            "stats": st, "setup_s": setup,
+            "parity": {"patch_gops_checked": ns, "identical_to_oracle": same},
+            "what": "host octree descent + GPU k-means of every clustering cell, per GoP seeds (srand semantics), "
+                    "host arrays in and out",
+            "cpu_baseline": {"value": cpts / cdt / 1e6, "unit": "Mpts/s", "cores": 1, "kind": "port",
+                             "sample": f"first {ns} patch GoPs (oracle restatement, one thread), {cdt:.1f}s"}}
+
+
 def measure_encode(args, torch, pvvc, synth, nframes):
     """GPU encoder back end on the decode workload: the colour payloads of all
     slices of the sequence (every GoP's patches, 30 frames each: frame 0
@@ -882,7 +939,7 @@ def measure_encode(args, torch, pvvc, synth, nframes):
 def measure_serving(args, pvvc, zstd_level=0):
     """Playback serving: --serve-streams streams, each one GoP (30 frames, an
     intra frame + 29 predicted) of a seq300-style sequence whose point count
-    is drawn U(100k, 1M) per stream, looped; frame requests arrive as a
+    per frame is drawn U(100k, 1M) per stream, looped; frame requests arrive as a
     Poisson process at 30 fps x U(0.8, 1.2) per stream, in real time, for
     --serve-seconds; the server admits streams against a 150 GB HBM budget
     and decodes with continuous batching.  Latency = request accepted ->
@@ -894,7 +951,9 @@ def measure_serving(args, pvvc, zstd_level=0):
     t0 = time.time()
     streams, pts = [], []
     for i in range(args.serve_streams):
-        tp = int(rng.uniform(100_000, 1_000_000))
+        want = rng.uniform(100_000, 1_000_000)
+        # the generator voxelises about 0.845 (at 100k) to 0.867 (at 1M) of its point target
+        tp = int(want / (0.845 + 0.0218 * (want - 100_000) / 900_000))
         syn = pvvc.Synth(pvvc.config("seq300", nframes=30, target_points=tp, qp_i=args.qp, qp_p=args.qp, seed=1000 + i,
                                      zstd_level=zstd_level))
         fr = syn.frames()
@@ -950,14 +1009,15 @@ def measure_e2e(args, pvvc, frames, P, torch, stream):
     assert (st == 0).all()
     n = max(2, min(args.steps, 8))
     per = []
-    names = ["parse", "describe", "plan", "d2h_wait", "payload_wait", "ws_alloc", "decode_enqueue", "copy_enqueue"]
+    names = ["parse", "describe", "plan", "d2h_wait", "payload_wait", "ws_alloc", "decode_enqueue", "copy_enqueue",
+             "plan_sort_records", "plan_order_tiers", "plan_groups", "plan_layout", "plan_upload"]
     per_stages = []
-    stages = (ctypes.c_double * 8)()
+    stages = (ctypes.c_double * 13)()
     for _ in range(n):
         t0 = time.perf_counter()
         call()
         per.append(time.perf_counter() - t0)
-        lib.pvvc_host_stage_times(stages, 8)
+        lib.pvvc_host_stage_times(stages, 13)
         per_stages.append([round(float(x), 2) for x in stages])
     dt = sum(per) / n  # the mean; every call's time is reported beside it
     h2d = int(sum(len(b) for b in frames))

@@ -116,6 +116,12 @@ typedef struct {
     uint64_t clear_bytes;         /* coefficient bytes zeroed by memset nodes per decode */
 } pvvc_plan_info;
 int pvvc_plan_info_get(const pvvc_plan* plan, pvvc_plan_info* info);
+/* Host milliseconds of the last build of `plan` (no reference counterpart):
+ * out[0] the split into intra and predictive slices, their size sorts and the
+ * queue records, out[1] the RLGR order and size tiers, out[2] the
+ * inverse-RAHT groups and coefficient regions, out[3] the workspace layout,
+ * out[4] the upload of the queue.  Fills min(n, 5) values. */
+int pvvc_plan_host_times(const pvvc_plan* plan, double* out, int32_t n);
 
 /* Autotuner: plans `desc` under a set of candidate launch shapes (a
  * coordinate search over the six pvvc_tune fields, starting at the
@@ -178,7 +184,11 @@ int pvvc_graph_destroy(pvvc_graph* graph);
  * read-back (src/cuda/common/slice_io.cu:143-275, manager.cc:41-72,230-270):
  * payloads are copied to the device (zstd payloads compressed, then
  * inflated there by the kernel of pvvc_zstd_inflate_batch instead of the
- * loader's host zstd stage), decoded, and xyz/rgb are copied back.  Slot =
+ * loader's host zstd stage), decoded, and xyz/rgb are copied back.  A call
+ * of several GoPs is decoded in parts whose plans are built concurrently on
+ * host threads; each part's points are copied back as soon as it is decoded,
+ * while the next part decodes.  Page-locked output arrays (cudaHostAlloc /
+ * cudaHostRegister) let those copies run at the link's full rate.  Slot =
  * patch index.  Synchronises `stream` before returning.  status_host
  * receives one entry per slice, in file order; a zstd payload that does not
  * inflate marks its slice PVVC_ERR_ZSTD and the call returns PVVC_ERR_ZSTD. */
@@ -192,7 +202,8 @@ int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* cons
  * last device-to-host copies (and, for a call decoded in one piece, its
  * decode), out[4] the wait for the payload packed into pinned memory beside
  * the planning, out[5] workspace growth, out[6] queuing the decode kernels,
- * out[7] queuing the device-to-host copies of each part.  Fills min(n, 8)
+ * out[7] queuing the device-to-host copies of each part, out[8..12] the
+ * parts' planning stages summed (pvvc_plan_host_times).  Fills min(n, 13)
  * values; zeros before any call. */
 int pvvc_host_stage_times(double* out, int32_t n);
 
@@ -345,6 +356,36 @@ int pvvc_icp_batch_noalloc(int32_t npairs, const float* src_xyz, const uint32_t*
 int pvvc_cloud_mse_batch(int32_t npairs, const float* src_xyz, const uint32_t* src_off, const float* tgt_xyz,
                          const uint32_t* tgt_off, const float* T, float* mse_out, void* workspace,
                          uint64_t workspace_bytes, uint64_t total_src_points, uint64_t total_tgt_points, void* stream);
+
+/* ---- fitting cloud of the GoP encoder ------------------------------------
+ * Replaces PatchFitting::Compute with the direct clustering that every
+ * reference config selects (src/patch/patch_fitting.cc:92-381): the
+ * registered patches of a GoP (one per frame, in frame order) -> the fitting
+ * cloud, the centroids of k-means runs over the clustering cells of an
+ * octree descent.  The descent runs on the host; every cell's k-means on the
+ * GPU (exact nearest centroids, FP32 sums in point order, the reference's
+ * seeding and empty-cluster redraws).  The reference draws from the
+ * process-wide rand(); here GoP g draws from its own generator -- glibc's
+ * rand() algorithm seeded like srand(seeds[g]) -- so a GoP's fitting cloud
+ * equals the reference's Compute after srand(seeds[g]).
+ *   gop_patch   int32[ngops+1]: GoP g = patches [gop_patch[g], gop_patch[g+1])
+ *   patch_off   uint32[npatches+1]: patch p = points [patch_off[p], patch_off[p+1])
+ *   xyz         HOST float[3*points], the registered patches' points
+ *   out_xyz     HOST float[3*out_cap]; out_off HOST uint64[ngops+1] receives
+ *               each GoP's range of the fitting clouds
+ *   stats       optional int32[4]: clustering cells, k-means iterations,
+ *               empty-cluster redraws, device rounds
+ * Parameters as in PVVCParam_t::patch (the configs: 1.0, 0.1, 100).  A cell
+ * whose k would be zero (fewer points than half the patches) gives no
+ * centroid, and one whose k equals its point count takes every point; the
+ * reference reads past its containers in both.  Synchronises `stream`. */
+typedef struct pvvc_fitter pvvc_fitter;
+int pvvc_fitter_create(pvvc_fitter** out);
+int pvvc_fitter_destroy(pvvc_fitter* fitter);
+int pvvc_fitting_clouds(pvvc_fitter* fitter, int32_t ngops, const int32_t* gop_patch, const uint32_t* patch_off,
+                        const float* xyz, const uint32_t* seeds, float clustering_ths, float clustering_err_ths,
+                        int32_t max_iter, float* out_xyz, uint64_t out_cap, uint64_t* out_off, int32_t* stats,
+                        void* stream);
 
 /* ---- reconstruction quality --------------------------------------------
  * Replaces common::MSE::SetClouds + Compute + GetGeoMSEs/GetYMSEs/GetUMSEs/

@@ -118,6 +118,9 @@ class Oracle:
                                           C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int]
             lib.pvo_cloud_mse.restype = C.c_float
             lib.pvo_cloud_mse.argtypes = [_f32p, C.c_size_t, _f32p, C.c_size_t]
+            lib.pvo_fitting_cloud.restype = C.c_long
+            lib.pvo_fitting_cloud.argtypes = [C.c_int, C.POINTER(_f32p), _u32p, C.c_float, C.c_float, C.c_int, C.c_uint,
+                                              _f32p, C.c_size_t, C.POINTER(C.c_long)]
             lib.pvo_cloud_quality.restype = C.c_int
             lib.pvo_cloud_quality.argtypes = [_f32p, _u8p, C.c_size_t, _f32p, _u8p, C.c_size_t, C.c_int,
                                               C.POINTER(C.c_double)]
@@ -322,6 +325,22 @@ class Oracle:
         b = np.ascontiguousarray(b, np.float32)
         return float(self.lib.pvo_cloud_mse(_ptr(a, _f32p), a.shape[0], _ptr(b, _f32p), b.shape[0]))
 
+    def fitting_cloud(self, patches, seed: int = 1, clustering_ths: float = 1.0, clustering_err_ths: float = 0.1,
+                      max_iter: int = 100):
+        """PatchFitting::Compute (direct clustering) of the GoP's registered
+        patches: (the fitting cloud float32 [m,3], {cells, iterations})."""
+        arrs = [np.ascontiguousarray(x, np.float32).reshape(-1, 3) for x in patches]
+        ptrs = (_f32p * len(arrs))(*[_ptr(a, _f32p) for a in arrs])
+        ns = np.array([a.shape[0] for a in arrs], np.uint32)
+        cap = int(ns.sum()) + 16
+        out = np.zeros((cap, 3), np.float32)
+        st = (C.c_long * 3)()
+        k = self.lib.pvo_fitting_cloud(len(arrs), ptrs, _ptr(ns, _u32p), clustering_ths, clustering_err_ths, max_iter, seed,
+                                       _ptr(out, _f32p), cap, st)
+        if k < 0:
+            raise RuntimeError(f"fitting_cloud status {-k}")
+        return out[:k], {"cells": int(st[0]), "iterations": int(st[1]), "empty_redraws": int(st[2])}
+
     def cloud_quality(self, p_xyz, p_rgb, q_xyz, q_rgb, brute: bool = False) -> np.ndarray:
         """common::MSE::Compute of p against q: [geo p->q, geo q->p, Y, Y, U, U, V, V]."""
         a = np.ascontiguousarray(p_xyz, np.float32).reshape(-1, 3)
@@ -452,6 +471,9 @@ class Reference:
         lib.ref_decoder_get_patch.argtypes = [C.c_void_p, _f32p, _u8p, C.c_size_t]
         lib.ref_cloud_mse.restype = C.c_float
         lib.ref_cloud_mse.argtypes = [_f32p, C.c_size_t, _f32p, C.c_size_t]
+        lib.ref_fitting_cloud.restype = C.c_long
+        lib.ref_fitting_cloud.argtypes = [C.c_int, C.POINTER(_f32p), _u32p, C.c_float, C.c_float, C.c_int, C.c_uint, _f32p,
+                                          C.c_size_t]
         lib.ref_mse_compute.restype = C.c_int
         lib.ref_mse_compute.argtypes = [_f32p, _u8p, C.c_size_t, _f32p, _u8p, C.c_size_t, C.POINTER(C.c_double)]
         lib.ref_gop_encode.restype = C.c_int
@@ -469,6 +491,20 @@ class Reference:
         a = np.ascontiguousarray(a, np.float32)
         b = np.ascontiguousarray(b, np.float32)
         return float(self.lib.ref_cloud_mse(_ptr(a, _f32p), a.shape[0], _ptr(b, _f32p), b.shape[0]))
+
+    def fitting_cloud(self, patches, seed: int = 1, clustering_ths: float = 1.0, clustering_err_ths: float = 0.1,
+                      max_iter: int = 100) -> np.ndarray:
+        """The reference's PatchFitting::Compute after srand(seed)."""
+        arrs = [np.ascontiguousarray(x, np.float32).reshape(-1, 3) for x in patches]
+        ptrs = (_f32p * len(arrs))(*[_ptr(a, _f32p) for a in arrs])
+        ns = np.array([a.shape[0] for a in arrs], np.uint32)
+        cap = int(ns.sum()) + 16
+        out = np.zeros((cap, 3), np.float32)
+        k = self.lib.ref_fitting_cloud(len(arrs), ptrs, _ptr(ns, _u32p), clustering_ths, clustering_err_ths, max_iter, seed,
+                                       _ptr(out, _f32p), cap)
+        if k < 0:
+            raise RuntimeError(f"reference PatchFitting status {k}")
+        return out[:k]
 
     def mse_compute(self, p_xyz, p_rgb, q_xyz, q_rgb) -> np.ndarray:
         """The reference's common::MSE::Compute: [geo p->q, geo q->p, Y, Y, U, U, V, V]."""

@@ -158,6 +158,15 @@ int pvo_knn_colors_batch(int npairs, const float* q, const uint64_t* qoff, const
 int pvo_libzstd_inflate_batch(int n, const uint8_t* src, const uint64_t* src_off, const uint32_t* src_len, uint8_t* dst,
                               const uint64_t* dst_off, const uint32_t* dst_cap, int32_t* status, int nthreads);
 
+
+/* PatchFitting::Compute with direct clustering (patch_fitting.cc:92-381): the
+ * GoP's registered patches -> the fitting cloud (k-means centroids, xyz into
+ * out[3 * cap]).  The rand() draws come from a private glibc generator seeded
+ * like srand(seed).  Returns the point count or -status; stats (optional):
+ * {clustering cells, k-means iterations, empty-cluster redraws}. */
+long pvo_fitting_cloud(int npatches, const float* const* xyz, const uint32_t* n, float clustering_ths,
+                       float clustering_err_ths, int max_iter, unsigned seed, float* out, size_t cap, long* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,13 @@
 
 using namespace vvc;
 
+// registration::ICP is implemented with PCL's ICP (src/registration/icp.cc),
+// which is not available here.  patch_fitting.cc names it only in
+// PatchFitting::AddPatch, which this driver never calls; these definitions
+// let the library link, and Align fails loudly if it is ever reached.
+vvc::registration::ICP::ICP() : vvc::registration::ICPBase{}, icp_{nullptr} {}
+void vvc::registration::ICP::Align() { throw __EXCEPT__(ERROR_OCCURED); }
+
 namespace {
 common::PVVCParam_t::Ptr make_params(int zstd_level) {
     auto p = std::make_shared<common::PVVCParam_t>();
@@ -374,6 +381,45 @@ int ref_mse_compute(const float* p, const uint8_t* prgb, size_t np, const float*
             out[2 * k + 1] = v[k].second;
         }
         return 0;
+    } catch (const common::Exception&) {
+        return -1;
+    }
+}
+
+/* ---- PatchFitting::Compute (src/patch/patch_fitting.cc:92-136, Split and
+ * Clustering :138-381) with the reference configs' direct clustering: the
+ * GoP's registered patches -> the fitting cloud.  srand(seed) first: the
+ * reference draws its k-means seeds and empty-cluster replacements from the
+ * process-wide rand().  Returns the fitting cloud's size (its xyz into
+ * out[3 * cap]), or -1 when the reference threw, -2 when out is too small. */
+long ref_fitting_cloud(int npatches, const float* const* xyz, const uint32_t* n, float clustering_ths,
+                       float clustering_err_ths, int max_iter, unsigned seed, float* out, size_t cap) {
+    try {
+        patch::PatchFitting fit;
+        auto prm = std::make_shared<common::PVVCParam_t>();
+        prm->patch.clustering_ths = clustering_ths;
+        prm->patch.clustering_err_ths = clustering_err_ths;
+        prm->patch.max_iter = max_iter;
+        prm->patch.split_method = common::DIRECT_CLUSTERING;
+        fit.params_ = prm;
+        for (int i = 0; i < npatches; ++i) {
+            common::Patch pt;
+            pt.cloud = make_cloud(xyz[i], n[i]);
+            pt.index = 0;
+            pt.timestamp = i;
+            fit.source_patches_.emplace_back(pt);
+        }
+        fit.fitting_cloud_.reset(new pcl::PointCloud<pcl::PointXYZRGB>());
+        srand(seed);
+        fit.Compute();
+        const auto& c = *fit.fitting_cloud_;
+        if (c.size() > cap) return -2;
+        for (size_t i = 0; i < c.size(); ++i) {
+            out[3 * i] = c[i].x;
+            out[3 * i + 1] = c[i].y;
+            out[3 * i + 2] = c[i].z;
+        }
+        return (long)c.size();
     } catch (const common::Exception&) {
         return -1;
     }

@@ -20,13 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-fmad=false", "-I", INCLUDE] + ARCH
 # -ffp-contract=off: host float code must not fuse a*b+c on any host (aarch64 would)
-# zstd_kernels.cu: built with ptxas -O1.  With the default -O3 schedule the
-# zstd kernel returned wrong results for some payloads, nondeterministically
-# and depending on the kernel instance, even with a single thread per CTA and
-# its tables in global memory; -O1 and -O0 builds of the same source were
-# exact on every run, and the same source compiled for the host is clean
-# under address and undefined-behaviour sanitisers.
-PER_FILE_FLAGS = {"zstd_kernels.cu": ["-Xptxas", "-O1"]}
+PER_FILE_FLAGS: dict[str, list[str]] = {}
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function",
              "-pthread", "-I", INCLUDE]
 

@@ -40,6 +40,18 @@ int resolve_tune(const pvvc_tune* in, pvvc_tune* out) {
 }
 
 namespace {
+// A host array left uninitialised (every element is written before it is
+// read): per-slice tables of large calls without the cost of zeroing them.
+template <class T>
+struct RawArray {
+    std::unique_ptr<T[]> a;
+    explicit RawArray(size_t n) : a(new T[n ? n : 1]) {}
+    T& operator[](size_t i) { return a[i]; }
+    const T& operator[](size_t i) const { return a[i]; }
+    T* data() { return a.get(); }
+    const T* data() const { return a.get(); }
+};
+
 // Runs fn(i) for i in [0, n) on up to `threads` host threads.
 template <class F>
 void parallel_for(int n, int threads, F fn) {
@@ -59,6 +71,10 @@ void parallel_for(int n, int threads, F fn) {
 
 // Host threads for the planner's and the host call's parallel loops.
 int host_threads() { return (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency())); }
+// The planner's share of them on this thread (several plans built at once
+// split the threads between them); 0: all.
+thread_local int g_plan_threads = 0;
+int plan_threads() { return g_plan_threads > 0 ? g_plan_threads : host_threads(); }
 
 // Stable sort of slice indices by (size descending, slot ascending): an LSD
 // radix sort over four 16-bit digits of ((~size) << 32 | slot), skipping the
@@ -93,6 +109,12 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     if (!d || d->nslices < 0) return PVVC_ERR_ARG;
     if (resolve_tune(tune, &p->tune)) return PVVC_ERR_ARG;
     if (prepare_kernels() != cudaSuccess) return PVVC_ERR_CUDA;
+    auto t_last = std::chrono::steady_clock::now();
+    auto lap = [&](int k) {  // host milliseconds of the plan's stages (pvvc_plan_host_times)
+        const auto now = std::chrono::steady_clock::now();
+        p->host_ms[k] = std::chrono::duration<double, std::milli>(now - t_last).count();
+        t_last = now;
+    };
     const int n = d->nslices;
     if (n > 0 && (!d->slot || !d->type || !d->size || !d->qp || !d->mv || !d->geo_off || !d->geo_size || !d->col_off ||
                   !d->col_size || !d->out_off))
@@ -118,14 +140,17 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     p->nslices = n;
     p->nintra = (int32_t)intra.size();
     p->max_slot = max_slot;
-    p->work.resize(n);
+    // the queue's records are built in the page-locked mirror they are
+    // uploaded from (every field of every record is written below)
+    if (p->h_work.ensure(std::max<size_t>(sizeof(SliceWork) * n, 16)) != cudaSuccess) return PVVC_ERR_NOMEM;
+    SliceWork* const W = static_cast<SliceWork*>(p->h_work.p);
     uint64_t coef = 0, fb = 0, pts = 0;
     // the queue: intra slices, then predictive ones.  The records are filled
     // in parallel (the descriptor is gathered in sorted order, so most reads
     // miss the cache); the coefficient regions are laid out further down.
     auto fill = [&](int q) {
         const int i = q < (int)intra.size() ? intra[q] : pred[q - intra.size()];
-        SliceWork& w = p->work[q];
+        SliceWork& w = W[q];
         std::memset(&w, 0, sizeof(w));
         w.col_off = d->col_off[i];
         w.geo_off = d->geo_off[i];
@@ -149,7 +174,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         uint64_t f = 0, m = 0;
         for (int q = c * kFillChunk, e = std::min(n, q + kFillChunk); q < e; ++q) {
             fill(q);
-            const SliceWork& w = p->work[q];
+            const SliceWork& w = W[q];
             if (w.n > (uint32_t)kRahtWcap) f += 6ull * w.n;
             m = std::max<uint64_t>(m, w.out_off + w.n);
         }
@@ -159,7 +184,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     if (nch < 2)
         for (int c = 0; c < nch; ++c) fill_chunk(c);
     else
-        parallel_for(nch, host_threads(), fill_chunk);
+        parallel_for(nch, plan_threads(), fill_chunk);
     for (int c = 0; c < nch; ++c) {
         ch_fb[c + 1] += ch_fb[c];
         pts = std::max(pts, ch_pts[c]);
@@ -168,7 +193,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     auto fb_chunk = [&](int c) {  // fallback-buffer offsets, in queue order from the chunk's base
         uint64_t f = ch_fb[c];
         for (int q = c * kFillChunk, e = std::min(n, q + kFillChunk); q < e; ++q) {
-            SliceWork& w = p->work[q];
+            SliceWork& w = W[q];
             if (w.n > (uint32_t)kRahtWcap) {
                 w.fb_off = f;
                 f += 6ull * w.n;
@@ -180,8 +205,9 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     if (nch < 2)
         for (int c = 0; c < nch; ++c) fb_chunk(c);
     else
-        parallel_for(nch, host_threads(), fb_chunk);
+        parallel_for(nch, plan_threads(), fb_chunk);
     p->total_points = pts;
+    lap(0);  // split, sort, queue records
     // RLGR order: all slices by size, so that a warp decodes similar lengths.
     // The queue holds the intra slices, then the predictive ones, each run
     // already sorted by (size descending, slot): merging the two runs (ties
@@ -193,8 +219,8 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         std::iota(qa.begin(), qa.end(), 0);
         std::iota(qb.begin(), qb.end(), ni);
         std::merge(qa.begin(), qa.end(), qb.begin(), qb.end(), p->order.begin(), [&](int32_t a, int32_t b) {
-            if (p->work[a].n != p->work[b].n) return p->work[a].n > p->work[b].n;
-            return p->work[a].slot < p->work[b].slot;
+            if (W[a].n != W[b].n) return W[a].n > W[b].n;
+            return W[a].slot < W[b].slot;
         });
     }
     // the head of that order goes to the long-slice launch (at most a quarter
@@ -211,6 +237,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         }
     }
     if (!intra.empty() && p->tree.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+    lap(1);  // RLGR order and tiers
     // inverse-RAHT schedule: slices grouped by slot (largest slots first)
     {
         // queue indices bucketed by slot (slots in order of first appearance,
@@ -218,7 +245,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         std::vector<int32_t> where(max_slot + 1, -1), slot_of, cnt_of;
         std::vector<int32_t> bucket_of(n);
         for (int q2 = 0; q2 < n; ++q2) {
-            const int32_t sl = p->work[q2].slot;
+            const int32_t sl = W[q2].slot;
             if (where[sl] < 0) {
                 where[sl] = (int32_t)slot_of.size();
                 slot_of.push_back(sl);
@@ -237,14 +264,14 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         std::vector<int32_t> ord(nb);
         std::iota(ord.begin(), ord.end(), 0);
         std::stable_sort(ord.begin(), ord.end(),
-                         [&](int32_t a, int32_t b) { return p->work[flat[bstart[a]]].n > p->work[flat[bstart[b]]].n; });
+                         [&](int32_t a, int32_t b) { return W[flat[bstart[a]]].n > W[flat[bstart[b]]].n; });
         std::vector<GroupDesc> ga, gb;
         std::vector<int32_t> items, la, lb;
         items.reserve(n);
         for (int32_t si : ord) {
             const int32_t* L = flat.data() + bstart[si];  // the slot's queue indices
             const size_t Ln = (size_t)(bstart[si + 1] - bstart[si]);
-            const bool has_intra = !(p->work[L[0]].type & PVVC_TYPE_PREDICT);
+            const bool has_intra = !(W[L[0]].type & PVVC_TYPE_PREDICT);
             for (size_t c0 = 0; c0 < Ln; c0 += 32) {
                 const int cnt = (int)std::min<size_t>(32, Ln - c0);
                 const bool first = c0 == 0;
@@ -292,9 +319,9 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         // (stride 32), every other slice owns contiguous planes
         uint64_t c = 0;
         for (const auto& g : p->groups) {
-            const uint32_t gn = p->work[p->idx[g.first]].n;
+            const uint32_t gn = W[p->idx[g.first]].n;
             for (int l = 0; l < g.count; ++l) {
-                SliceWork& w = p->work[p->idx[g.first + l]];
+                SliceWork& w = W[p->idx[g.first + l]];
                 w.coef_off = c;
                 w.coef_stride = 32;
                 w.coef_lane = (uint32_t)l;
@@ -302,7 +329,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
             c += 3ull * gn * 32;
         }
         for (int li = p->list_a_off; li < (int)p->idx.size(); ++li) {
-            SliceWork& w = p->work[p->idx[li]];
+            SliceWork& w = W[p->idx[li]];
             w.coef_off = c;
             w.coef_stride = 1;
             w.coef_lane = 0;
@@ -315,12 +342,13 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         p->coef_long_floats = 0;
         p->coef_mid_floats = 0;
         for (int i = 0; i < p->nlong + p->nmid; ++i) {
-            const SliceWork& w = p->work[p->order[i]];
+            const SliceWork& w = W[p->order[i]];
             const uint64_t e = w.coef_off + 3ull * w.n * w.coef_stride;
             if (i < p->nlong) p->coef_long_floats = std::max(p->coef_long_floats, e);
             p->coef_mid_floats = std::max(p->coef_mid_floats, e);
         }
     }
+    lap(2);  // groups and coefficient regions
     // workspace layout
     uint64_t off = 0;
     p->ws_coef = off;
@@ -337,7 +365,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     // floats; an internal level of a valid tree is never wider than its leaves
     {
         uint32_t maxn = 0;
-        for (const auto& g : p->groups) maxn = std::max(maxn, p->work[p->idx[g.first]].n);
+        for (const auto& g : p->groups) maxn = std::max(maxn, W[p->idx[g.first]].n);
         p->grp_ctas = std::min<int32_t>((int32_t)p->groups.size(), p->tune.group_ctas_per_sm * sm_count());
         p->grp_floats = 2ull * std::max<uint32_t>(maxn, 1) * 96;
         p->ws_grp = off;
@@ -353,6 +381,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         off = align_up(off + 16, 256);
     }
     p->ws_bytes = std::max<uint64_t>(off, 256);
+    lap(3);  // workspace layout
     // upload: synchronous from the plan's vectors, or (upload != nullptr)
     // stream-ordered from pinned mirrors that stay untouched until the plan is
     // rebuilt (the caller orders that after the copies)
@@ -365,14 +394,17 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         auto put = [&](DevBuf& d, HostBuf& h, const void* src, size_t bytes) -> bool {
             if (!bytes) return true;
             if (!upload) return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
-            if (h.ensure(bytes) != cudaSuccess) return false;
-            std::memcpy(h.p, src, bytes);
+            if (src != h.p) {
+                if (h.ensure(bytes) != cudaSuccess) return false;
+                std::memcpy(h.p, src, bytes);
+            }
             return cudaMemcpyAsync(d.p, h.p, bytes, cudaMemcpyHostToDevice, upload) == cudaSuccess;
         };
-        if (!put(p->d_work, p->h_work, p->work.data(), wb) || !put(p->d_order, p->h_order, p->order.data(), ob) ||
+        if (!put(p->d_work, p->h_work, W, wb) || !put(p->d_order, p->h_order, p->order.data(), ob) ||
             !put(p->d_groups, p->h_groups, p->groups.data(), gb) || !put(p->d_idx, p->h_idx, p->idx.data(), ib))
             return PVVC_ERR_CUDA;
     }
+    lap(4);  // upload
     return PVVC_OK;
 }
 
@@ -756,6 +788,12 @@ extern "C" int pvvc_plan_destroy(pvvc_plan* p) {
     return PVVC_OK;
 }
 
+extern "C" int pvvc_plan_host_times(const pvvc_plan* p, double* out, int32_t n) {
+    if (!p || !out || n < 0) return PVVC_ERR_ARG;
+    for (int k = 0; k < n && k < 5; ++k) out[k] = p->host_ms[k];
+    return PVVC_OK;
+}
+
 extern "C" int pvvc_plan_query(const pvvc_plan* p, uint64_t* total_points, uint64_t* workspace_bytes) {
     if (!p) return PVVC_ERR_ARG;
     if (total_points) *total_points = p->total_points;
@@ -778,7 +816,7 @@ extern "C" int pvvc_decode_profiled(const pvvc_plan* plan, pvvc_state* st, const
 
 
 namespace {
-constexpr int kStages = 8;
+constexpr int kStages = 13;
 thread_local double g_stage_ms[kStages] = {};  // see pvvc_host_stage_times
 
 // A zstd payload of a parsed frame, left compressed for the GPU.
@@ -860,15 +898,34 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         nsl += (int32_t)frames[f].count();
     }
     ffirst[nframes] = nsl;
-    std::vector<int32_t> slot(nsl), index(nsl);
-    std::vector<uint8_t> type(nsl), qp(nsl);
-    std::vector<uint32_t> size(nsl), gsz(nsl), csz(nsl);
-    std::vector<float> mv(16ull * nsl);
-    std::vector<uint64_t> goff(nsl), coff(nsl), oo(nsl);
+    RawArray<int32_t> slot(nsl), index(nsl);
+    RawArray<uint8_t> type(nsl), qp(nsl);
+    RawArray<uint32_t> size(nsl), gsz(nsl), csz(nsl);
+    RawArray<float> mv(16ull * nsl);
+    RawArray<uint64_t> goff(nsl), coff(nsl), oo(nsl);
     {
-        int32_t k = 0;
-        for (auto& fr : frames)
-            for (size_t i = 0; i < fr.count(); ++i, ++k) {
+        // per frame its payload bytes and points, a prefix over frames, then
+        // every frame's slices filled in parallel
+        std::vector<uint64_t> fbytes(nframes + 1, 0), fpts(nframes + 1, 0);
+        parallel_for(nframes, threads, [&](int f) {
+            const FrameView& fr = frames[f];
+            uint64_t b = 0, q = 0;
+            for (size_t i = 0; i < fr.count(); ++i) {
+                b += align_up(fr.gsz[i], 4) + align_up(fr.csz[i], 4);
+                q += fr.size[i];
+            }
+            fbytes[f + 1] = b;
+            fpts[f + 1] = q;
+        });
+        for (int f = 0; f < nframes; ++f) {
+            fbytes[f + 1] += fbytes[f];
+            fpts[f + 1] += fpts[f];
+        }
+        parallel_for(nframes, threads, [&](int f) {
+            const FrameView& fr = frames[f];
+            uint64_t b = fbytes[f], q = fpts[f];
+            for (size_t i = 0; i < fr.count(); ++i) {
+                const int32_t k = ffirst[f] + (int32_t)i;
                 index[k] = fr.index[i];
                 type[k] = fr.type[i];
                 qp[k] = fr.qp[i];
@@ -876,13 +933,16 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
                 std::memcpy(&mv[16ull * k], &fr.mv[16 * i], 64);
                 gsz[k] = fr.gsz[i];
                 csz[k] = fr.csz[i];
-                goff[k] = bytes;
-                bytes = align_up(bytes + gsz[k], 4);
-                coff[k] = bytes;
-                bytes = align_up(bytes + csz[k], 4);
-                oo[k] = pts;
-                pts += size[k];
+                goff[k] = b;
+                b = align_up(b + gsz[k], 4);
+                coff[k] = b;
+                b = align_up(b + csz[k], 4);
+                oo[k] = q;
+                q += size[k];
             }
+        });
+        bytes = fbytes[nframes];
+        pts = fpts[nframes];
     }
     if (npoints_out) *npoints_out = pts;
     if (pts > cap_points || (status_host && status_cap < nsl)) return PVVC_ERR_CAPACITY;
@@ -1064,24 +1124,53 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         return sent_ok;
     };
     g_stage_ms[1] = clk.lap();
-    int rc = PVVC_OK;
-    for (int h = 0; h < nparts && rc == PVVC_OK; ++h) {
+    // the decode writes device buffers; each part's points go back to the host
+    // with a copy as soon as the part is decoded.  (Decode kernels writing
+    // page-locked host memory straight over the link were measured slower:
+    // their stores reach the host as partial lines.)
+    float* out_xyz = static_cast<float*>(st->xyz.p);
+    uint8_t* out_rgb = static_cast<uint8_t*>(st->rgb.p);
+    // The parts' plans are built at once: part 0 on this thread, the others
+    // on worker threads (each with its share of the host threads), and each
+    // part's decode is queued as soon as its plan is ready.
+    std::vector<int> plan_rc(std::max(nparts, 1), PVVC_OK);
+    auto plan_part = [&](int h, int nthreads) {
+        g_plan_threads = nthreads;
         const int32_t first = cuts[h], cnt = cuts[h + 1] - first;
         pvvc_plan* pl = h ? &st->part_plan[h - 1] : &st->plan;
         pvvc_batch_desc d{cnt,          slot.data() + first, type.data() + first, size.data() + first, qp.data() + first,
                           mv.data() + 16ull * first, goff.data() + first, gsz.data() + first, coff.data() + first,
                           csz.data() + first, oo.data() + first};
-        rc = build_plan(&d, pl, nullptr, s);
+        plan_rc[h] = build_plan(&d, pl, nullptr, s);
+        g_plan_threads = 0;
+    };
+    std::vector<std::thread> planners;
+    struct JoinAll {
+        std::vector<std::thread>& v;
+        ~JoinAll() {
+            for (auto& t : v)
+                if (t.joinable()) t.join();
+        }
+    } join_planners{planners};
+    const int share = std::max(1, threads / std::max(nparts, 1));
+    for (int h = 1; h < nparts; ++h) planners.emplace_back(plan_part, h, share);
+    if (nparts > 0) plan_part(0, share);
+    int rc = PVVC_OK;
+    for (int h = 0; h < nparts && rc == PVVC_OK; ++h) {
+        const int32_t first = cuts[h], cnt = cuts[h + 1] - first;
+        pvvc_plan* pl = h ? &st->part_plan[h - 1] : &st->plan;
+        if (h > 0) planners[h - 1].join();
+        rc = plan_rc[h];
         if (rc) break;
+        for (int k = 0; k < 5; ++k) g_stage_ms[8 + k] += pl->host_ms[k];
         g_stage_ms[2] += clk.lap();
         if (st->ws.ensure(pl->ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
         g_stage_ms[5] += clk.lap();
         if (!payload_queued()) return PVVC_ERR_CUDA;
         if (h > 0 && nz && cudaStreamWaitEvent(s, st->zdone[h], 0) != cudaSuccess) return PVVC_ERR_CUDA;
         g_stage_ms[4] += clk.lap();
-        rc = run_decode(pl, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
-                        static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
-                        st->ws.cap, s, nullptr);
+        rc = run_decode(pl, st, static_cast<const uint8_t*>(st->payload.p), out_xyz, out_rgb, nullptr,
+                        static_cast<int32_t*>(st->status.p) + first, st->ws.p, st->ws.cap, s, nullptr);
         if (rc) break;
         g_stage_ms[6] += clk.lap();
         // this part's points: [oo[first], end of its last slice), contiguous in frame order
@@ -1116,9 +1205,8 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         if (st->ws.ensure(st->plan.ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
         if (!payload_queued()) return PVVC_ERR_CUDA;
         g_stage_ms[2] += clk.lap();
-        rc = run_decode(&st->plan, st, static_cast<const uint8_t*>(st->payload.p), static_cast<float*>(st->xyz.p),
-                        static_cast<uint8_t*>(st->rgb.p), nullptr, static_cast<int32_t*>(st->status.p) + first, st->ws.p,
-                        st->ws.cap, s, nullptr);
+        rc = run_decode(&st->plan, st, static_cast<const uint8_t*>(st->payload.p), out_xyz, out_rgb, nullptr,
+                        static_cast<int32_t*>(st->status.p) + first, st->ws.p, st->ws.cap, s, nullptr);
         // the plan's host arrays are rebuilt by the next run: finish this one first
         if (rc == PVVC_OK && runs.size() > 2 && cudaStreamSynchronize(s) != cudaSuccess) rc = PVVC_ERR_CUDA;
         g_stage_ms[3] += clk.lap();

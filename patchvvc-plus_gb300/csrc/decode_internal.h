@@ -119,6 +119,7 @@ struct HostBuf {  // pinned, grow-only
 
 struct pvvc_plan {
     pvvc_tune tune{};  // resolved launch shapes
+    double host_ms[5] = {};  // host time of the last build's stages (pvvc_plan_host_times)
     int32_t nslices = 0, nintra = 0, max_slot = -1;
     uint64_t total_points = 0;
     uint64_t ws_coef = 0, ws_fb = 0, ws_tstatus = 0, ws_rstatus = 0, ws_fstatus = 0, ws_bytes = 0;
@@ -128,7 +129,6 @@ struct pvvc_plan {
     uint64_t coef_floats = 0;
     uint64_t coef_long_floats = 0;  // planes prefix the long-slice RLGR launch writes
     uint64_t coef_mid_floats = 0;   // ... and the medium tier
-    std::vector<pvvc::SliceWork> work;
     std::vector<int32_t> order;
     // inverse-RAHT schedule: phase A needs only this batch's trees; phase B
     // also needs phase A's intra colours.  Groups go to the warp kernel,
@@ -140,7 +140,8 @@ struct pvvc_plan {
     std::vector<int32_t> idx;             // [group items | slice list A | slice list B]
     int32_t nlist_a = 0, nlist_b = 0, list_a_off = 0, list_b_off = 0;
     pvvc::DevBuf d_work, d_order, d_groups, d_idx;
-    pvvc::HostBuf h_work, h_order, h_groups, h_idx;  // pinned mirrors of stream-ordered uploads
+    pvvc::HostBuf h_work;  // the queue's records, built here (page-locked) and uploaded from here
+    pvvc::HostBuf h_order, h_groups, h_idx;  // pinned mirrors of stream-ordered uploads
     int32_t nlong = 0;       // the first nlong slices of `order` go to the long-slice RLGR launch
     int32_t nmid = 0;        // the next nmid slices to the medium tier
     pvvc::SideStream side;   // the long tier's stream
@@ -155,7 +156,10 @@ struct pvvc_state {
     pvvc::HostBuf h_payload;
     pvvc_plan plan;
     static constexpr int kParts = 3;        // a multi-GoP call is decoded in up to this many parts
-    static constexpr double kCutAt[kParts - 1] = {1.0 / 3, 2.0 / 3};  // part boundaries, as fractions of the slices
+    // part boundaries, as fractions of the slices: a small first part starts
+    // the device work (and its outputs' trip to the host) early, while the
+    // other parts are still being planned
+    static constexpr double kCutAt[kParts - 1] = {0.1, 0.45};
     pvvc_plan part_plan[kParts - 1];        // the plans of parts 1.. (part 0 uses `plan`)
     cudaStream_t copy = nullptr;            // device-to-host copies that overlap the next part's decode
     cudaEvent_t part_done[kParts] = {};

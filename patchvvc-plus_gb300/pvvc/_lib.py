@@ -82,6 +82,7 @@ SIGNATURES = [
     ("pvvc_plan_destroy", C.c_int, [vp]),
     ("pvvc_plan_query", C.c_int, [vp, u64p, u64p]),
     ("pvvc_plan_create_tuned", C.c_int, [C.POINTER(BatchDesc), C.POINTER(Tune), C.POINTER(vp)]),
+    ("pvvc_plan_host_times", C.c_int, [vp, C.POINTER(C.c_double), C.c_int32]),
     ("pvvc_plan_info_get", C.c_int, [vp, C.POINTER(PlanInfo)]),
     ("pvvc_plan_autotune", C.c_int, [C.POINTER(BatchDesc), vp, vp, C.c_int32, vp, C.POINTER(Tune), f32p]),
     ("pvvc_graph_create", C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.POINTER(vp)]),
@@ -112,6 +113,10 @@ SIGNATURES = [
     ("pvvc_icp_batch_noalloc", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, C.POINTER(IcpParams), vp, vp, vp, vp,
                                          C.c_uint64, vp]),
     ("pvvc_cloud_mse_batch", C.c_int, [C.c_int32, vp, vp, vp, vp, vp, vp, vp, C.c_uint64, C.c_uint64, C.c_uint64, vp]),
+    ("pvvc_fitter_create", C.c_int, [C.POINTER(vp)]),
+    ("pvvc_fitter_destroy", C.c_int, [vp]),
+    ("pvvc_fitting_clouds", C.c_int, [vp, C.c_int32, i32p, u32p, f32p, u32p, C.c_float, C.c_float, C.c_int32, f32p,
+                                      C.c_uint64, u64p, i32p, vp]),
     ("pvvc_cloud_quality_workspace_size", C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint64)]),
     ("pvvc_cloud_quality", C.c_int, [C.c_uint64, vp, vp, C.c_uint64, vp, vp, vp, vp, C.c_uint64, vp]),
     ("pvvc_knn_colors_workspace_size", C.c_int, [C.c_int32, C.c_uint64, u64p]),

@@ -91,9 +91,11 @@ class Decoder:
     def reset(self, stream: int = 0):
         L.check(L.lib().pvvc_state_reset(self.h, stream), "pvvc_state_reset")
 
-    def decode_frames(self, frames: list[bytes], stream: int = 0):
+    def decode_frames(self, frames: list[bytes], stream: int = 0, out=None):
         """End-to-end host call: .frame bytes in, (xyz float32 [P,3], rgb
-        uint8 [P,3], per-slice status int32) out."""
+        uint8 [P,3], per-slice status int32) out.  out: optional (xyz, rgb)
+        host arrays of at least P rows to decode into (page-locked ones are
+        written by the GPU directly)."""
         nf = len(frames)
         bufs = [np.frombuffer(b, np.uint8) for b in frames]
         ptrs = (L.u8p * max(nf, 1))(*[_p(b, L.u8p) for b in bufs])
@@ -107,11 +109,19 @@ class Decoder:
         from .frame import parse_frame
         nsl = sum(parse_frame(b).n for b in frames)
         P = int(npts.value)
-        xyz = np.zeros((max(P, 1), 3), np.float32)
-        rgb = np.zeros((max(P, 1), 3), np.uint8)
+        if out is not None:
+            xyz, rgb = out
+            if xyz.shape[0] < P or rgb.shape[0] < P or xyz.dtype != np.float32 or rgb.dtype != np.uint8:
+                raise ValueError("out arrays too small or of the wrong type")
+            if not (xyz.flags.c_contiguous and rgb.flags.c_contiguous):
+                raise ValueError("out arrays must be contiguous")
+        else:
+            xyz = np.zeros((max(P, 1), 3), np.float32)
+            rgb = np.zeros((max(P, 1), 3), np.uint8)
         st = np.zeros(max(nsl, 1), np.int32)
-        L.check(L.lib().pvvc_decode_frames_host(self.h, nf, ptrs, _p(lens, L.u64p), _p(xyz, L.f32p), _p(rgb, L.u8p), P,
-                                                C.byref(npts), _p(st, L.i32p), nsl, stream), "pvvc_decode_frames_host")
+        L.check(L.lib().pvvc_decode_frames_host(self.h, nf, ptrs, _p(lens, L.u64p), _p(xyz, L.f32p), _p(rgb, L.u8p),
+                                                xyz.shape[0] if out is not None else P, C.byref(npts), _p(st, L.i32p), nsl,
+                                                stream), "pvvc_decode_frames_host")
         return xyz[:P], rgb[:P], st[:nsl]
 
 

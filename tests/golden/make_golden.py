@@ -32,8 +32,14 @@ It compiles the reference's sources against the oracle's shim headers
                    160-223) of 6 coloured cloud pairs: geometric and Y/U/V
                    errors both ways, summed in float as the reference does.
 
+  fitting.npz      PatchFitting::Compute (src/patch/patch_fitting.cc:92-381,
+                   direct clustering, the configs' 1.0 / 0.1 / 100) after
+                   srand(seed): registered synthetic patch GoPs, and small
+                   GoPs of repeated points whose k-means empties clusters and
+                   redraws them from rand().
+
 `python tests/golden/make_golden.py gop_encode` (or `cloud_mse`,
-`cloud_quality`) writes only that fixture.
+`cloud_quality`, `fitting`) writes only that fixture.
 
 Patches: 4 from the seeded synthetic surface generator plus 4 edge cases
 (a single point, two distant points, a full 8^3 cube, and points that share
@@ -241,9 +247,48 @@ def make_cloud_quality(ref: Reference, seed: int = 47):
                         mse=mse)
 
 
+def make_fitting(ref: Reference):
+    """GoPs of registered patches -> the reference's fitting clouds."""
+    import pvvc
+    s = pvvc.Synth(pvvc.config("gof8", seed=21))
+    cases = []  # (list of patches, seed)
+    for p in range(3):
+        xyz, yuv, mv = s.patch(0, p)
+        rng = np.random.default_rng(100 + p)
+        pats = [xyz.astype(np.float32)]
+        for f in range(1, mv.shape[0]):
+            # the frame's patch (moved, jittered, voxelised), registered back by the true motion
+            m = mv[f].astype(np.float64)
+            moved = np.round(xyz @ m[:3, :3].T + m[:3, 3] + rng.normal(0, 0.3, xyz.shape))
+            inv = np.linalg.inv(m)
+            pats.append((moved @ inv[:3, :3].T + inv[:3, 3]).astype(np.float32))
+        cases.append((pats, 1 + p))
+        cases.append((pats[:3], 7))
+    rng = np.random.default_rng(0)
+    for t in range(12):  # repeated points: empty clusters, redrawn from rand()
+        base = rng.integers(0, 6, (int(rng.integers(4, 30)), 3)).astype(np.float32)
+        pats = [base[rng.integers(0, base.shape[0], int(rng.integers(5, 40)))] for _ in range(int(rng.integers(3, 6)))]
+        if t in (0, 2, 4):
+            cases.append((pats, t))
+    allp, poff, gop, seeds, outs, ooff = [], [0], [0], [], [], [0]
+    for pats, seed in cases:
+        for x in pats:
+            allp.append(x)
+            poff.append(poff[-1] + x.shape[0])
+        gop.append(gop[-1] + len(pats))
+        seeds.append(seed)
+        y = ref.fitting_cloud(pats, seed=seed)
+        outs.append(y)
+        ooff.append(ooff[-1] + y.shape[0])
+    np.savez_compressed(os.path.join(HERE, "fitting.npz"), xyz=np.concatenate(allp), patch_off=np.array(poff, np.int64),
+                        gop_patch=np.array(gop, np.int64), seeds=np.array(seeds, np.uint32), fit=np.concatenate(outs),
+                        fit_off=np.array(ooff, np.int64))
+
+
 def main():
     ref = Reference()
-    one = {"gop_encode": make_gop_encode, "cloud_mse": make_cloud_mse, "cloud_quality": make_cloud_quality}
+    one = {"gop_encode": make_gop_encode, "cloud_mse": make_cloud_mse, "cloud_quality": make_cloud_quality,
+           "fitting": make_fitting}
     if len(sys.argv) == 2 and sys.argv[1] in one:
         one[sys.argv[1]](ref)
         print(sys.argv[1] + ".npz written to", HERE)
@@ -251,6 +296,7 @@ def main():
     make_gop_encode(ref)
     make_cloud_mse(ref)
     make_cloud_quality(ref)
+    make_fitting(ref)
     rng = np.random.default_rng(2024)
     make_rlgr(ref, rng)
 

@@ -277,6 +277,27 @@ def test_host_call_decodes_gops_in_one_plan_identically(pvvc_lib, torch, nframes
         assert np.array_equal(x, y)
 
 
+def test_host_call_pinned_and_pageable_outputs_agree(pvvc_lib, torch):
+    """Page-locked and pageable output arrays receive the same bytes, for a
+    call of several GoPs decoded in parts and for a single-GoP call, and
+    nothing is written past the decoded points."""
+    s = pvvc_lib.Synth(pvvc_lib.config("tiny", nframes=20, gof=4, seed=5))
+    frames = s.frames()
+    nidx = max(int(pvvc_lib.parse_frame(b).index.max()) + 1 for b in frames)
+    P = sum(pvvc_lib.parse_frame(b).points for b in frames)
+    for part in (frames, frames[:4]):
+        d1 = pvvc_lib.Decoder(nslots=5 * nidx, max_leaves=4096)
+        d2 = pvvc_lib.Decoder(nslots=5 * nidx, max_leaves=4096)
+        xp = torch.full((P + 7, 3), -1.0, dtype=torch.float32).pin_memory()
+        rp = torch.zeros((P + 7, 3), dtype=torch.uint8).pin_memory()
+        x1, r1, s1 = d1.decode_frames(part, out=(xp.numpy(), rp.numpy()))
+        x2, r2, s2 = d2.decode_frames(part)
+        n = x2.shape[0]
+        assert (s1 == 0).all() and (s2 == 0).all() and x1.shape[0] == n
+        assert np.array_equal(x1[:n].view(np.uint32), x2.view(np.uint32)) and np.array_equal(r1[:n], r2)
+        assert (xp.numpy()[n:] == -1.0).all()  # nothing written past the decoded points
+
+
 def test_host_call_zstd_sequence_matches_raw(pvvc_lib, torch):
     """A synthetic GoP whose payloads are zstd-compressed by the reference
     encoder's rule (GoP_encoding.cc:158-200: level 22, kept only when smaller)
