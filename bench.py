@@ -266,7 +266,7 @@ class DecodePass:
             self.tune, self.tune_ms = {"group_ctas_per_sm": g, "min_group": m, "rlgr_block": b, "rlgr_long_ctas": l,
                                        "rlgr_mid_pct": mid, "rlgr_long_lanes": ln}, None
         else:
-            self.tune, self.tune_ms = pvvc.autotune(self.batch, self.dec, self.pay.data_ptr(), reps=2, stream=self.sp)
+            self.tune, self.tune_ms = pvvc.autotune(self.batch, self.dec, self.pay.data_ptr(), reps=5, stream=self.sp)
         log(f"[rank {rank}] q={qp}: launch shapes {self.tune} ({self.tune_ms} ms) in {time.time() - t_tune:.1f}s")
         self.plan = pvvc.Plan(self.batch, tune=self.tune)
         self.info = self.plan.info()

@@ -91,16 +91,28 @@ int pvvc_plan_query(const pvvc_plan* plan, uint64_t* total_points, uint64_t* wor
 
 /* Launch shapes of a plan.  A zero field takes the built-in default.  No
  * reference counterpart: the reference launches one thread per slice
- * (src/cuda/render/render.cc:269-301, block = 1). */
+ * (src/cuda/render/render.cc:269-301, block = 1).
+ *
+ * RLGR runs in one of two forms.  Groups of at least 16 slices of one slot,
+ * all of one size (the frames of a patch in a GoP), form size tiers of whole
+ * groups: the long tier is decoded one thread per slice into planes cleared
+ * beforehand, the medium and short tiers one warp per group, each warp
+ * staging its coefficients in a shared-memory window and writing them as
+ * whole lines (no plane clear).  Every other slice is decoded one thread per
+ * slice into planes cleared beforehand; when no group qualifies, those
+ * slices are split into the size tiers below. */
 typedef struct {
     int32_t group_ctas_per_sm; /* persistent CTAs of the grouped inverse-RAHT kernel per SM: 1..4 (default 3)   */
     int32_t min_group;         /* a slot's predictive slices share one warp when at least this many: 1..32 (4) */
-    int32_t rlgr_block;        /* threads per CTA of the RLGR kernel: 32, 64, 128 or 256 (default 128)         */
-    int32_t rlgr_long_ctas;    /* CTAs of 128 threads that decode the longest slices alone on an SM each, side by
-                                  side with the rest: 0..152 (default 32); -1 turns the split off                 */
-    int32_t rlgr_mid_pct;      /* with the split on: percent of the other slices (the larger ones) decoded, and
-                                  their groups inverse-transformed, on a third stream: 0..90 (default 30); -1 off */
-    int32_t rlgr_long_lanes;   /* slices per warp in the long-slice launch: 8, 16 or 32 (default 32)            */
+    int32_t rlgr_block;        /* threads per CTA of the RLGR kernels: 32, 64, 128 or 256 (default 128); the
+                                  windowed form runs rlgr_block / 32 groups per CTA                               */
+    int32_t rlgr_long_ctas;    /* CTAs of 128 threads that decode the longest slices (with window groups: the
+                                  slices of the 4 x rlgr_long_ctas largest groups) alone on an SM each, side by
+                                  side with the rest: 0..152 (default 32); -1 turns the split off                */
+    int32_t rlgr_mid_pct;      /* with the split on: percent of the other slices or groups (the larger ones)
+                                  decoded, and their groups inverse-transformed, on a third stream: 0..90
+                                  (default 30); -1 off                                                            */
+    int32_t rlgr_long_lanes;   /* slices per warp in the per-slice long launch: 8, 16 or 32 (default 32)        */
 } pvvc_tune;
 int pvvc_plan_create_tuned(const pvvc_batch_desc* desc, const pvvc_tune* tune, pvvc_plan** out);
 
@@ -127,7 +139,7 @@ int pvvc_plan_host_times(const pvvc_plan* plan, double* out, int32_t n);
  * coordinate search over the six pvvc_tune fields, starting at the
  * defaults), captures one decode of the batch under each into a CUDA graph,
  * replays it `reps` times on `stream` timed with CUDA events, and returns the
- * fastest shapes and their mean device time per decode.  The
+ * fastest shapes and their median device time per decode.  The
  * decodes run for real: afterwards `st` holds what one pvvc_decode of the
  * batch leaves.  It allocates its own workspace and outputs, and
  * synchronises `stream`.  `payload` as for pvvc_decode. */

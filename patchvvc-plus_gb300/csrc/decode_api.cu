@@ -236,7 +236,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
             if (p->nmid > 0 && p->side2.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
         }
     }
-    if (!intra.empty() && p->tree.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+    if (n > 0 && p->tree.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
     lap(1);  // RLGR order and tiers
     // inverse-RAHT schedule: slices grouped by slot (largest slots first)
     {
@@ -286,23 +286,77 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
                 }
             }
         }
-        // phase-A groups that hold a slice of the long-slice RLGR launch first:
-        // the others can be inverse-transformed as soon as the short launch ends
-        // (tier 2), then those with a medium-tier slice (tier 1), then the rest
+        // Window groups: phase-A groups of at least kWinGroupMin slices, all
+        // of one size, in size tiers of whole groups (ga is already largest
+        // first), so a tier's inverse RAHT waits for its own RLGR only.  The
+        // long tier's slices -- the critical path -- are decoded by the
+        // per-slice long launch, whose iterations are the cheapest, into
+        // planes cleared first; the medium and short tiers by the windowed
+        // RLGR, a warp per group, whose planes need no clear.  The slices of
+        // no window group get one per-slice RLGR launch.
+        p->nwin = 0;
+        p->nwin_slices = 0;
         {
-            std::vector<uint8_t> tier(n, 0);
-            for (int i = 0; i < p->nlong + p->nmid; ++i) tier[p->order[i]] = i < p->nlong ? 2 : 1;
-            std::vector<GroupDesc> gl, gm, gs;
+            std::vector<GroupDesc> gw, gr;
             for (const GroupDesc& g : ga) {
-                int t = 0;
-                for (int l = 0; l < g.count; ++l) t = std::max<int>(t, tier[items[g.first + l]]);
-                (t == 2 ? gl : t == 1 ? gm : gs).push_back(g);
+                bool ok = g.count >= kWinGroupMin;
+                for (int l = 1; ok && l < g.count; ++l) ok = W[items[g.first + l]].n == W[items[g.first]].n;
+                (ok ? gw : gr).push_back(g);
             }
-            p->ngroups_a_long = (int32_t)gl.size();
-            p->ngroups_a_mid = (int32_t)gm.size();
-            ga = gl;
-            ga.insert(ga.end(), gm.begin(), gm.end());
-            ga.insert(ga.end(), gs.begin(), gs.end());
+            if (!gw.empty()) {
+                const int nw = (int)gw.size();
+                p->nwin = nw;
+                p->ngroups_a_long = (p->tune.rlgr_long_ctas > 0 && nw >= 8)
+                                        ? std::min(kWinGroupsPerLongCta * p->tune.rlgr_long_ctas, nw / 4)
+                                        : 0;
+                p->ngroups_a_mid = p->tune.rlgr_mid_pct > 0
+                                       ? (int32_t)((int64_t)(nw - p->ngroups_a_long) * p->tune.rlgr_mid_pct / 100)
+                                       : 0;
+                if (p->ngroups_a_long > 0 && p->side.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+                if (p->ngroups_a_mid > 0 && p->side2.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+                ga = gw;
+                ga.insert(ga.end(), gr.begin(), gr.end());
+                // RLGR order: the window groups' slices in group order (sizes
+                // descending; the long tier's slices first, their count in
+                // nlong), then the other slices, largest first
+                std::vector<uint8_t> inw(n, 0);
+                std::vector<int32_t> ord2;
+                ord2.reserve(n);
+                p->nlong = 0;
+                p->nmid = 0;
+                for (int gi = 0; gi < nw; ++gi) {
+                    const GroupDesc& g = gw[gi];
+                    for (int l = 0; l < g.count; ++l) {
+                        inw[items[g.first + l]] = 1;
+                        ord2.push_back(items[g.first + l]);
+                    }
+                    if (gi < p->ngroups_a_long) p->nlong += g.count;
+                }
+                p->nwin_slices = (int32_t)ord2.size();
+                for (int32_t q : p->order)
+                    if (!inw[q]) ord2.push_back(q);
+                p->order.swap(ord2);
+            }
+        }
+        if (p->nwin == 0) {
+            // phase-A groups that hold a slice of the long-slice RLGR launch first:
+            // the others can be inverse-transformed as soon as the short launch ends
+            // (tier 2), then those with a medium-tier slice (tier 1), then the rest
+            {
+                std::vector<uint8_t> tier(n, 0);
+                for (int i = 0; i < p->nlong + p->nmid; ++i) tier[p->order[i]] = i < p->nlong ? 2 : 1;
+                std::vector<GroupDesc> gl, gm, gs;
+                for (const GroupDesc& g : ga) {
+                    int t = 0;
+                    for (int l = 0; l < g.count; ++l) t = std::max<int>(t, tier[items[g.first + l]]);
+                    (t == 2 ? gl : t == 1 ? gm : gs).push_back(g);
+                }
+                p->ngroups_a_long = (int32_t)gl.size();
+                p->ngroups_a_mid = (int32_t)gm.size();
+                ga = gl;
+                ga.insert(ga.end(), gm.begin(), gm.end());
+                ga.insert(ga.end(), gs.begin(), gs.end());
+            }
         }
         p->groups = ga;
         p->groups.insert(p->groups.end(), gb.begin(), gb.end());
@@ -317,16 +371,21 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         p->nlist_b = (int32_t)lb.size();
         // coefficient regions: a group shares one frame-interleaved region
         // (stride 32), every other slice owns contiguous planes
+        // (window groups first; a region holds the largest slice of its group)
         uint64_t c = 0;
-        for (const auto& g : p->groups) {
-            const uint32_t gn = W[p->idx[g.first]].n;
+        p->coef_win_floats = 0;
+        for (size_t gi = 0; gi < p->groups.size(); ++gi) {
+            const GroupDesc& g = p->groups[gi];
+            uint32_t gn = 0;
             for (int l = 0; l < g.count; ++l) {
                 SliceWork& w = W[p->idx[g.first + l]];
                 w.coef_off = c;
                 w.coef_stride = 32;
                 w.coef_lane = (uint32_t)l;
+                gn = std::max(gn, w.n);
             }
             c += 3ull * gn * 32;
+            if ((int32_t)gi + 1 == p->nwin) p->coef_win_floats = c;
         }
         for (int li = p->list_a_off; li < (int)p->idx.size(); ++li) {
             SliceWork& w = W[p->idx[li]];
@@ -371,10 +430,10 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         p->ws_grp = off;
         off = align_up(off + 4ull * p->grp_floats * std::max(p->grp_ctas, 1), 256);
         // the long-slice groups run beside the others, with level buffers of their own
-        p->grp_ctas_long = p->nlong > 0 ? std::min<int32_t>(p->ngroups_a_long, p->grp_ctas) : 0;
+        p->grp_ctas_long = p->ngroups_a_long > 0 ? std::min<int32_t>(p->ngroups_a_long, p->grp_ctas) : 0;
         p->ws_grp_long = off;
         off = align_up(off + 4ull * p->grp_floats * p->grp_ctas_long, 256);
-        p->grp_ctas_mid = p->nmid > 0 ? std::min<int32_t>(p->ngroups_a_mid, p->grp_ctas) : 0;
+        p->grp_ctas_mid = p->ngroups_a_mid > 0 ? std::min<int32_t>(p->ngroups_a_mid, p->grp_ctas) : 0;
         p->ws_grp_mid = off;
         off = align_up(off + 4ull * p->grp_floats * p->grp_ctas_mid, 256);
         p->ws_counter = off;
@@ -428,16 +487,22 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     };
     if (!mark(0)) return PVVC_ERR_CUDA;
     // The tree expansion reads only geometry payloads and writes only slot
-    // tables, the coefficient clear and RLGR only colour payloads and
-    // coefficient planes: without stage markers the tree runs beside them on
-    // a stream of its own, joined before the inverse RAHT.
-    const bool tree_aside = !events && p->nintra > 0;
+    // tables, and the output coordinates need only the trees; the coefficient
+    // clear and RLGR touch only colour payloads and coefficient planes:
+    // without stage markers the trees and then the coordinates are computed
+    // beside them on a stream of their own.  The inverse RAHT waits for the
+    // trees (event `mid`), the end of the decode for the coordinates
+    // (event `join`).
+    const bool tree_aside = !events;
     if (tree_aside) {
         const SideStream& tr = p->tree;
         if (cudaEventRecord(tr.fork, s) != cudaSuccess || cudaStreamWaitEvent(tr.s, tr.fork, 0) != cudaSuccess ||
-            launch_tree(dw, p->nintra, payload, st->v, ts, tr.s) != cudaSuccess || cudaEventRecord(tr.join, tr.s) != cudaSuccess)
+            launch_tree(dw, p->nintra, payload, st->v, ts, tr.s) != cudaSuccess || cudaEventRecord(tr.mid, tr.s) != cudaSuccess ||
+            launch_xyz(dw, p->nslices, st->v, ts, xyz, p24, tr.s) != cudaSuccess ||
+            cudaEventRecord(tr.join, tr.s) != cudaSuccess)
             return PVVC_ERR_CUDA;
-    } else if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) {
+    } else if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess ||
+               launch_xyz(dw, p->nslices, st->v, ts, xyz, p24, s) != cudaSuccess || !mark(1)) {
         return PVVC_ERR_CUDA;
     }
     float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
@@ -454,12 +519,60 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     auto fork = [&](const SideStream& sd) {
         return cudaEventRecord(sd.fork, s) == cudaSuccess && cudaStreamWaitEvent(sd.s, sd.fork, 0) == cudaSuccess;
     };
-    if (p->nlong == 0) {
+    if (p->nwin > 0) {
+        // RLGR in size tiers of whole window groups: the long tier (the
+        // per-slice long launch, its planes cleared first) on SMs of its own
+        // (stream `side`), the medium tier windowed (stream `side2`), the
+        // short tier windowed and then the per-slice launch of the other
+        // slices (this stream; only their planes are cleared).  Each tier's
+        // groups are inverse-transformed on its stream once that tier is
+        // decoded and the trees are built.
+        const SideStream& L = p->side;
+        const SideStream& M = p->side2;
+        const int nl = p->ngroups_a_long, nm = p->ngroups_a_mid, nw = p->nwin;
+        const int nrest = p->nslices - p->nwin_slices;
+        const int wwarps = std::max(1, p->tune.rlgr_block / 32);
+        if (nl > 0 && (!clear(0, p->coef_long_floats) || !fork(L) ||
+                       launch_rlgr_long(dw, ord, p->nlong, payload, coef, rs, p->tune.rlgr_long_lanes, kRlgrLongSmem, L.s) !=
+                           cudaSuccess))
+            return PVVC_ERR_CUDA;
+        if (nm > 0 &&
+            (!fork(M) || launch_rlgr_win(dw, dg + nl, nm, di, payload, coef, rs, wwarps, M.s) != cudaSuccess))
+            return PVVC_ERR_CUDA;
+        if (launch_rlgr_win(dw, dg + nl + nm, nw - nl - nm, di, payload, coef, rs, wwarps, s) != cudaSuccess)
+            return PVVC_ERR_CUDA;
+        if (nrest > 0 && (!clear(p->coef_win_floats, p->coef_floats) ||
+                          launch_rlgr(dw, ord + p->nwin_slices, nrest, payload, coef, rs, p->tune.rlgr_block, kRlgrShortSmem,
+                                      s) != cudaSuccess))
+            return PVVC_ERR_CUDA;
+        if (events) {
+            // stage markers: every tier decoded, then every group
+            if ((nl > 0 && (cudaEventRecord(L.join, L.s) != cudaSuccess || cudaStreamWaitEvent(s, L.join, 0) != cudaSuccess)) ||
+                (nm > 0 && (cudaEventRecord(M.join, M.s) != cudaSuccess || cudaStreamWaitEvent(s, M.join, 0) != cudaSuccess)) ||
+                !mark(2) || !raht_groups(0, p->ngroups_a, cnt, gsc, p->grp_ctas, s))
+                return PVVC_ERR_CUDA;
+        } else {
+            if (nl > 0 && ((tree_aside && cudaStreamWaitEvent(L.s, p->tree.mid, 0) != cudaSuccess) ||
+                           !raht_groups(0, nl, cnt, reinterpret_cast<float*>(w + p->ws_grp_long), p->grp_ctas_long, L.s) ||
+                           cudaEventRecord(L.join, L.s) != cudaSuccess))
+                return PVVC_ERR_CUDA;
+            if (nm > 0 && ((tree_aside && cudaStreamWaitEvent(M.s, p->tree.mid, 0) != cudaSuccess) ||
+                           !raht_groups(nl, nm, cnt + 3, reinterpret_cast<float*>(w + p->ws_grp_mid), p->grp_ctas_mid,
+                                        M.s) ||
+                           cudaEventRecord(M.join, M.s) != cudaSuccess))
+                return PVVC_ERR_CUDA;
+            if ((tree_aside && cudaStreamWaitEvent(s, p->tree.mid, 0) != cudaSuccess) ||
+                !raht_groups(nl + nm, p->ngroups_a - nl - nm, cnt + 2, gsc, p->grp_ctas, s) ||
+                (nl > 0 && cudaStreamWaitEvent(s, L.join, 0) != cudaSuccess) ||
+                (nm > 0 && cudaStreamWaitEvent(s, M.join, 0) != cudaSuccess))
+                return PVVC_ERR_CUDA;
+        }
+    } else if (p->nlong == 0) {
         // zero symbols are not written by the decoder: clear the planes first
         if (!clear(0, p->coef_floats) ||
             launch_rlgr(dw, ord, p->nslices, payload, coef, rs, p->tune.rlgr_block, 0, s) != cudaSuccess || !mark(2))
             return PVVC_ERR_CUDA;
-        if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;
+        if (tree_aside && cudaStreamWaitEvent(s, p->tree.mid, 0) != cudaSuccess) return PVVC_ERR_CUDA;
         if (!raht_groups(0, p->ngroups_a, cnt, gsc, p->grp_ctas, s)) return PVVC_ERR_CUDA;
     } else {
         // Size tiers, largest first in `order`: the long slices on SMs of their
@@ -491,7 +604,7 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
             // Each tier's groups follow its decode on its stream.  A group can
             // straddle a size cut, so a tier's groups also wait for the
             // smaller tiers' decode (which ends sooner); all wait for the trees.
-            if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;
+            if (tree_aside && cudaStreamWaitEvent(s, p->tree.mid, 0) != cudaSuccess) return PVVC_ERR_CUDA;
             if (cudaEventRecord(L.mid, s) != cudaSuccess) return PVVC_ERR_CUDA;  // the small tier decoded, trees built
             if (nm > 0 && (cudaStreamWaitEvent(M.s, L.mid, 0) != cudaSuccess ||
                            !raht_groups(na_l, na_m, cnt + 3, reinterpret_cast<float*>(w + p->ws_grp_mid), p->grp_ctas_mid,
@@ -520,6 +633,7 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
             cudaSuccess ||
         !mark(4))
         return PVVC_ERR_CUDA;
+    if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;  // the coordinates
     return PVVC_OK;
 }
 
@@ -625,9 +739,18 @@ extern "C" int pvvc_plan_info_get(const pvvc_plan* p, pvvc_plan_info* info) {
     info->singles_b = p->nlist_b;
     info->group_ctas = p->grp_ctas;
     info->tune = p->tune;
-    info->clear_bytes = 4ull * p->coef_floats;
-    if (p->nslices > 0)
-        info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) + (p->nmid > 0) +
+    info->clear_bytes =
+        p->nwin > 0
+            ? 4ull * p->coef_long_floats + (p->nslices > p->nwin_slices ? 4ull * (p->coef_floats - p->coef_win_floats) : 0ull)
+            : 4ull * p->coef_floats;
+    if (p->nslices > 0 && p->nwin > 0)
+        info->kernels = (p->nintra > 0) + 1 + (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
+                        (p->nwin > p->ngroups_a_long + p->ngroups_a_mid) + (p->nslices > p->nwin_slices) +
+                        (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
+                        (p->ngroups_a > p->ngroups_a_long + p->ngroups_a_mid) + (p->nlist_a > 0) + (p->ngroups_b > 0) +
+                        (p->nlist_b > 0);
+    else if (p->nslices > 0)
+        info->kernels = (p->nintra > 0) + 2 + (p->nlong > 0) + (p->nmid > 0) +
                         (p->nlong > 0 ? (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
                                             (p->ngroups_a > p->ngroups_a_long + p->ngroups_a_mid)
                                       : (p->ngroups_a > 0)) +
@@ -642,11 +765,15 @@ namespace {
 // differently where a plan runs kernels side by side).
 float time_plan(pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb, int32_t* status,
                 DevBuf& ws, int reps, cudaStream_t s) {
+    // the median of `reps` timed replays of the plan's graph (one untimed
+    // replay first): robust to the odd slow replay, so that the search does
+    // not chase noise
     if (ws.ensure(p->ws_bytes) != cudaSuccess) return -1.f;
+    reps = std::max(1, std::min(reps, 64));
     cudaStream_t cs = nullptr;
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<cudaEvent_t> ev(reps + 1, nullptr);
     float ms = -1.f;
     bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
@@ -655,17 +782,21 @@ float time_plan(pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz
         ok = cudaStreamEndCapture(cs, &g) == cudaSuccess && rc == PVVC_OK && g;
     }
     ok = ok && cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
-    ok = ok && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess;
+    for (auto& e : ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
     ok = ok && cudaGraphLaunch(ge, s) == cudaSuccess;  // untimed: first touch of the workspace, L2 state
-    ok = ok && cudaEventRecord(e0, s) == cudaSuccess;
-    for (int r = 0; ok && r < reps; ++r) ok = cudaGraphLaunch(ge, s) == cudaSuccess;
-    if (ok && cudaEventRecord(e1, s) == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess &&
-        cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
-        ms /= reps;
-    else
-        ms = -1.f;
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
+    ok = ok && cudaEventRecord(ev[0], s) == cudaSuccess;
+    for (int r = 0; ok && r < reps; ++r)
+        ok = cudaGraphLaunch(ge, s) == cudaSuccess && cudaEventRecord(ev[r + 1], s) == cudaSuccess;
+    if (ok && cudaEventSynchronize(ev[reps]) == cudaSuccess) {
+        std::vector<float> t(reps);
+        for (int r = 0; ok && r < reps; ++r) ok = cudaEventElapsedTime(&t[r], ev[r], ev[r + 1]) == cudaSuccess;
+        if (ok) {
+            std::sort(t.begin(), t.end());
+            ms = (reps & 1) ? t[reps / 2] : 0.5f * (t[reps / 2 - 1] + t[reps / 2]);
+        }
+    }
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
     if (ge) cudaGraphExecDestroy(ge);
     if (g) cudaGraphDestroy(g);
     if (cs) cudaStreamDestroy(cs);

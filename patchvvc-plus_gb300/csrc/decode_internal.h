@@ -20,10 +20,15 @@ int pvvc_zstd_merge_status(int32_t njobs, const int32_t* zstatus, const int32_t*
 namespace pvvc {
 cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payload, const StateView& st, int32_t* tstatus,
                         cudaStream_t s);
+// output coordinates of every slice of the queue whose geometry is in place
+cudaError_t launch_xyz(const SliceWork* work, int nslices, const StateView& st, const int32_t* tstatus, float* xyz,
+                       float* p24, cudaStream_t s);
 cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
                         int32_t* rstatus, int block, int smem, cudaStream_t s);
 cudaError_t launch_rlgr_long(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
                              int32_t* rstatus, int lanes, int smem, cudaStream_t s);
+cudaError_t launch_rlgr_win(const SliceWork* work, const GroupDesc* groups, int ngroups, const int32_t* items,
+                            const uint8_t* payload, float* coef, int32_t* rstatus, int warps, cudaStream_t s);
 cudaError_t prepare_kernels();
 cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int count, const StateView& st, const float* coef,
                               float* fallback, const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz,
@@ -137,6 +142,11 @@ struct pvvc_plan {
     int32_t ngroups_a = 0, ngroups_b = 0;
     int32_t ngroups_a_long = 0;           // leading phase-A groups that hold a long-launch slice
     int32_t ngroups_a_mid = 0;            // the next phase-A groups: a medium-tier slice, no long one
+    // leading phase-A groups decoded by the windowed RLGR (then ngroups_a_long
+    // and ngroups_a_mid count its long and medium tiers), their slices (the
+    // head of `order`) and their coefficient planes (never cleared)
+    int32_t nwin = 0, nwin_slices = 0;
+    uint64_t coef_win_floats = 0;
     std::vector<int32_t> idx;             // [group items | slice list A | slice list B]
     int32_t nlist_a = 0, nlist_b = 0, list_a_off = 0, list_b_off = 0;
     pvvc::DevBuf d_work, d_order, d_groups, d_idx;

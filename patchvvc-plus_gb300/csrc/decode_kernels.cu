@@ -278,11 +278,11 @@ __global__ void __launch_bounds__(T) k_tree(const SliceWork* __restrict__ work, 
 // word into the window when `o` passes 32.  Words come from 16-byte payload
 // blocks staged in shared memory: each thread owns a ring of kRing block
 // slots (slot j of thread t at s_ring[j * blockDim + t], so a warp's 16-byte
-// reads are conflict-free), filled by cp.async kRing - 1 blocks -- about 180
+// reads are conflict-free), filled by cp.async kRing - 1 blocks -- about 75
 // loop iterations -- ahead of their use, so the serial chain does not wait
 // on global memory.  `cur` holds the words of the current block not yet
 // taken (the next one in cur.x).  Blocks past the payload are zero-filled.
-constexpr int kRing = 8;
+constexpr int kRing = 4;
 
 __device__ __forceinline__ void ring_fetch(uint4* slot, const uint4* src, bool valid) {
     const uint32_t d = (uint32_t)__cvta_generic_to_shared(slot);
@@ -562,6 +562,298 @@ __global__ void __launch_bounds__(T) k_rlgr(const SliceWork* __restrict__ work, 
 }
 
 // ---------------------------------------------------------------------------
+// k_rlgr_win: RLGR of the slices of one group (the frames of one patch, all
+// of the same size N), one warp per group, lane l decoding the group's slice
+// l.  The group's coefficients live in its frame-interleaved region: stream
+// position s of every lane's slice (plane s / N, coefficient N-1 - s % N)
+// is one 128-byte line, lane l's word at offset l.
+//
+// Instead of scattered 4-byte stores into planes cleared beforehand, each
+// lane stages its nonzero symbols in a shared-memory window of WROWS rows
+// (row r = stream position r: the 32 lanes' words of that line, their eight
+// 16-byte chunks XOR-swizzled by r & 7).  Every kWinCheck iterations the
+// warp takes the smallest position any lane can still write
+// (__reduce_min_sync); rows below it are final for every lane.  Each full
+// unit of 32 final rows is written out with lane l taking row unit + l:
+// eight 16-byte loads of its row (conflict-free thanks to the swizzle), eight
+// 16-byte stores of the whole line, zeros included, and the row cleared.  A
+// lane whose next symbol lands beyond the window keeps it pending and pauses
+// until the window reaches it.  So the planes need no clear, every line is
+// written once, in full, and no partially written line ever leaves L2.
+//
+// The decode loop is k_rlgr's with linear stream positions: the common path
+// also takes runs that cross a plane boundary.  Every round of the loop
+// either consumes a symbol in some lane or moves the window forward (a
+// paused lane's position is at least WROWS rows ahead of the window, so the
+// minimum has passed a whole unit), so the loop ends after at most 3N rounds
+// per lane plus one flush per unit of rows.
+constexpr uint32_t kWinCheck = 4;        // iterations between window checks (a multiple of 2)
+constexpr uint32_t kWinUnit = 32;        // rows written out together (one per lane)
+constexpr int kWinRows = 64;             // window rows (8 KB per warp)
+
+// shared memory of a windowed CTA: rings and windows, at least 16 KB (with
+// the 1 KB the SM keeps per CTA, more than the 15 KB a long per-slice CTA's
+// SM has left)
+constexpr int kWinMinSmem = 16 * 1024;
+__host__ __device__ constexpr int win_smem(int warps, int rows) {
+    return warps * (32 * kRing * 16 + rows * 32 * 4) > kWinMinSmem ? warps * (32 * kRing * 16 + rows * 32 * 4)
+                                                                   : kWinMinSmem;
+}
+
+template <int WARPS, int WROWS>
+__global__ void __launch_bounds__(32 * WARPS) k_rlgr_win(const SliceWork* __restrict__ work,
+                                                         const GroupDesc* __restrict__ groups, int ngroups,
+                                                         const int32_t* __restrict__ items,
+                                                         const uint8_t* __restrict__ payload, float* __restrict__ coef,
+                                                         int32_t* __restrict__ rstatus) {
+    static_assert((WROWS & (WROWS - 1)) == 0 && WROWS >= 2 * (int)kWinUnit, "window rows: a power of two");
+    extern __shared__ uint4 s_dyn[];  // [kRing][blockDim] payload blocks, then [WARPS][WROWS][32] floats
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int gi = blockIdx.x * WARPS + wid;
+    if (gi >= ngroups) return;  // the whole warp
+    float* const win = reinterpret_cast<float*>(s_dyn + kRing * blockDim.x) + (size_t)wid * WROWS * 32;
+    // word of (row r, lane) in the window: chunk (lane / 4) ^ (r & 7), word lane % 4
+    auto slot = [&](uint32_t r) { return ((r & (WROWS - 1)) << 5) + ((((uint32_t)lane >> 2) ^ (r & 7u)) << 2) + (lane & 3); };
+    const GroupDesc G = groups[gi];
+    const int item0 = items[G.first];
+    const uint32_t N = work[item0].n;
+    const uint32_t total = 3u * N;
+    const uint64_t region = work[item0].coef_off;
+    const int item = lane < G.count ? items[G.first + lane] : -1;
+    for (int i = lane; i < WROWS * 8; i += 32) reinterpret_cast<float4*>(win)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();  // rows are cleared by all lanes, then written by their owners
+    BitReader br;
+    bool done = true, pend = false;
+    int err = PVVC_OK;
+    int32_t qp = 0;
+    uint64_t off = 0;
+    uint32_t csz = 0;
+    if (item >= 0) {
+        const SliceWork& wk = work[item];
+        if (wk.n != N) {
+            rstatus[item] = PVVC_ERR_SIZE;  // the planner keeps such slices out of window groups
+        } else if (N == 0) {
+            rstatus[item] = PVVC_OK;
+        } else {
+            qp = wk.qp;
+            off = wk.col_off;
+            csz = wk.csz;
+            br.init(payload, off, csz, s_dyn + threadIdx.x, blockDim.x);
+            done = false;
+        }
+    }
+    uint32_t s = 0;                 // stream position of this lane's next symbol
+    uint32_t kP = 0, kRP = 8;
+    uint32_t pend_q = 0;            // a pending symbol's position and value
+    float pend_v = 0.f;
+    uint32_t base = 0;              // rows below `base` are written out (warp-uniform)
+    uint32_t bp = 0, bc = N - 1;    // plane and coefficient index of row `base`
+    for (uint32_t it = 1;; ++it) {
+        if (!done && !pend) {
+            uint32_t q = 0xFFFFFFFFu;  // position of a nonzero symbol decoded in this iteration
+            float val = 0.f;
+            // ---- common case: the whole iteration within the next 32 bits ----
+            const uint32_t v = br.peek();
+            const bool run = kP >= 4;
+            const uint32_t c = run ? __clz(~v) : 0u;
+            const uint32_t kP2 = kP + 2 * c;
+            const uint32_t k = run ? (kP2 >> 2) : 0u;
+            const uint32_t r = run ? c + 1 + k : 0u;
+            const uint32_t v2 = __funnelshift_lc(0u, v, r);
+            const uint32_t qq = __clz(~v2);
+            const uint32_t kR = kRP >> 2;
+            const uint32_t nb = r + qq + 1 + kR;
+            const uint32_t u = (qq << kR) | field(v2, qq + 1, kR);
+            const uint32_t m = run ? run_ones_length(kP, c) + field(v, c + 1, k) : 0u;
+            if (nb <= 32 && u < (1u << 23) && m < total - s) {
+                br.advance(nb);
+                const uint32_t zz = u + (uint32_t)run;
+                const int32_t sym = (int32_t)(zz >> 1) ^ -(int32_t)(zz & 1);
+                if (sym) {
+                    q = s + m;
+                    val = __int2float_rn(sym * qp);
+                }
+                kRP = qq ? min(kRP + qq - 1, kRlMaxRP) : (kRP < 2 ? 0u : kRP - 2);
+                kP = (run || u) ? (kP2 ? kP2 - kRlD1 : 0u) : kP2 + kRlU0;
+                s += m + 1;
+            } else {
+                // ---- general path: the codes read piece by piece ----
+                uint32_t mm = 0, kPr = kP;
+                if (run) {
+                    uint64_t m64 = 0;
+                    uint32_t kk = kP >> 2;
+                    uint32_t cc;
+                    int guard = 0;
+                    do {
+                        cc = __clz(~br.peek());
+                        for (uint32_t i = 0; i < cc; ++i) {
+                            m64 += 1ull << (kk & 31);
+                            kPr += kRlU1;
+                            kk = kPr >> 2;
+                        }
+                        br.advance(cc);
+                    } while (cc == 32 && ++guard < 64);
+                    br.advance(1);
+                    if (kk > 31) {
+                        err = PVVC_ERR_OVERRUN;
+                    } else {
+                        m64 += br.peek() >> (32 - kk);
+                        br.advance(kk);
+                        mm = m64 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (uint32_t)m64;
+                    }
+                }
+                if (!err) {
+                    s += min(mm, total - s);  // zeros, possibly across planes
+                    if (s < total) {
+                        const uint32_t w = br.peek();
+                        const uint32_t qw = __clz(~w);
+                        uint64_t uw;
+                        uint32_t pw;
+                        if (qw < 32) {
+                            br.advance(qw + 1);
+                            uint32_t rr = 0;
+                            if (kR) {
+                                rr = kR >= 32 ? br.peek() : (br.peek() >> (32 - kR));
+                                br.advance(kR >= 32 ? 32u : kR);
+                            }
+                            uw = ((uint64_t)qw << kR) | rr;
+                            pw = qw;
+                        } else {  // 32 ones: a raw 32-bit value follows (see k_rlgr on the clamp)
+                            br.advance(32);
+                            const uint32_t raw = br.peek();
+                            br.advance(32);
+                            uw = raw;
+                            const uint32_t t2 = kR >= 32 ? 0u : (raw >> kR);
+                            pw = t2 > kRlMaxRP ? kRlMaxRP + 1 : t2;
+                        }
+                        kRP = pw ? min(kRP + pw - 1, kRlMaxRP) : (kRP < 2 ? 0u : kRP - 2);
+                        kP = (run || uw) ? (kPr ? kPr - kRlD1 : 0u) : kPr + kRlU0;
+                        const uint64_t zz = uw + (uint64_t)run;
+                        const long long sym = (long long)(zz >> 1) ^ -(long long)(zz & 1);
+                        if (sym) {
+                            q = s;
+                            val = __ll2float_rn(sym * (long long)qp);
+                        }
+                        ++s;
+                    }
+                }
+            }
+            if (q != 0xFFFFFFFFu) {
+                if (q - base < (uint32_t)WROWS) {
+                    win[slot(q)] = val;
+                } else {
+                    pend = true;
+                    pend_q = q;
+                    pend_v = val;
+                }
+            }
+            if (err || s >= total) {
+                done = true;
+                // bits consumed vs the payload (the reference reads past it, which is undefined)
+                if (!err && br.consumed(off) > 8ll * csz) err = PVVC_ERR_OVERRUN;
+                br.drain();
+                rstatus[item] = err;
+            }
+        }
+        if (it % kWinCheck) continue;
+        // ---- the window (warp-uniform) ----
+        const uint32_t lb = pend ? pend_q : (done ? total : s);  // this lane writes no row below lb
+        const uint32_t mn = __reduce_min_sync(0xffffffffu, lb);
+        if (mn - base < kWinUnit && mn < total) continue;
+        // write out whole units of final rows (and at the end the last,
+        // partial one); rows from base + WROWS on were never staged: zeros
+        const uint32_t lim = base + WROWS;
+        const uint32_t stop = mn == total ? total : base + (mn - base) / kWinUnit * kWinUnit;
+        __syncwarp();  // every lane's staged words are visible to the row's owner
+        while (base < stop) {
+            const uint32_t r = base + (uint32_t)lane;  // this lane's row
+            if (r < stop) {
+                // its plane and coefficient, from row base's: lane rows down
+                uint32_t p = bp, c = bc;
+                uint32_t d = (uint32_t)lane;
+                while (d > c) {  // past the plane's coefficient 0: to the top of the next
+                    d -= c + 1;
+                    c = N - 1;
+                    ++p;
+                }
+                c -= d;
+                float4* dst = reinterpret_cast<float4*>(coef + region + (((uint64_t)p * N + c) << 5));
+                if (r < lim) {
+                    float4* row = reinterpret_cast<float4*>(win + ((r & (WROWS - 1)) << 5));
+#pragma unroll
+                    for (uint32_t j = 0; j < 8; ++j) {
+                        const uint32_t pj = j ^ (r & 7u);
+                        dst[j] = row[pj];
+                        row[pj] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    }
+                } else {
+#pragma unroll
+                    for (uint32_t j = 0; j < 8; ++j) dst[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+            // row base += one unit (warp-uniform)
+            uint32_t d = kWinUnit;
+            while (d > bc) {
+                d -= bc + 1;
+                bc = N - 1;
+                ++bp;
+            }
+            bc -= d;
+            base += kWinUnit;
+        }
+        base = stop;
+        __syncwarp();  // cleared rows before their owners' next writes
+        if (pend && pend_q - base < (uint32_t)WROWS) {
+            win[slot(pend_q)] = pend_v;
+            pend = false;
+        }
+        if (mn == total) break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// k_xyz: the output coordinates of every slice whose geometry is in place --
+// its slot's leaf centres through the slice's rigid transform
+// (pvvc_decompression.cc:141-150; GPU CUDA2OpenGL.cu:46-48), in the
+// reference's left-to-right FP32 order.  They depend on the trees only, so
+// this runs right after k_tree, beside RLGR, and the inverse RAHT writes
+// colours only.  A CTA per slice; a slice whose tree or slot is not valid
+// is skipped (the inverse RAHT reports its status).
+template <int T>
+__global__ void __launch_bounds__(T) k_xyz(const SliceWork* __restrict__ work, StateView st,
+                                           const int32_t* __restrict__ tstatus, float* __restrict__ xyz,
+                                           float* __restrict__ p24) {
+    const int item = blockIdx.x;
+    const SliceWork& w = work[item];
+    if (!(w.type & PVVC_TYPE_VALID)) return;
+    if (!(w.type & PVVC_TYPE_PREDICT) && tstatus[item] != PVVC_OK) return;
+    const SlotInfo* si = st.info + w.slot;
+    if (!si->valid || (uint32_t)si->leaves != w.n) return;
+    float m[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) m[k] = w.mv[k];
+    const float* c = st.xyz + (size_t)w.slot * st.max_leaves * 3;
+    for (uint32_t i = threadIdx.x; i < w.n; i += T) {
+        const float x0 = __ldg(c + 3ull * i), y0 = __ldg(c + 3ull * i + 1), z0 = __ldg(c + 3ull * i + 2);
+        const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
+        const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
+        const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
+        const uint64_t oi = w.out_off + i;
+        if (xyz) {
+            xyz[oi * 3 + 0] = X;
+            xyz[oi * 3 + 1] = Y;
+            xyz[oi * 3 + 2] = Z;
+        }
+        if (p24) {
+            float* q = p24 + oi * 6;
+            q[0] = X;
+            q[1] = Y;
+            q[2] = Z;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // k_raht
 struct OutPtrs {
     float* xyz;
@@ -570,12 +862,17 @@ struct OutPtrs {
     int32_t* status;  // caller's status, indexed by SliceWork::orig (may be null)
 };
 
+// std::round (half away from zero), clamped to [0, 255].  Clamping first
+// commutes with the rounding (it is monotone and 0 and 255 are integers);
+// for a clamped c >= 0, round(c) = floor(c + 0.5), and the sum rounded
+// toward -inf keeps that floor exact, since every integer is a float.  NaN
+// clamps to 0, as fmaxf(roundf(NaN), 0) does.
 __device__ __forceinline__ uint8_t to_u8(float v) {
-    const float r = roundf(v);  // std::round: half away from zero
-    return (uint8_t)fminf(fmaxf(r, 0.0f), 255.0f);
+    const float c = fminf(fmaxf(v, 0.0f), 255.0f);
+    return (uint8_t)__float2uint_rd(__fadd_rd(c, 0.5f));
 }
 
-// one leaf: reference add / store, YUV->RGB, transform, output
+// one leaf: reference add / store, YUV->RGB, colour output (the coordinates come from k_xyz)
 __device__ __forceinline__ void emit_leaf(const SliceWork& w, const StateView& st, size_t lb, uint32_t leaf, float y,
                                           float u, float v, bool predict, const OutPtrs& o) {
     float* ref = st.ref + (lb + leaf) * 3;
@@ -588,33 +885,19 @@ __device__ __forceinline__ void emit_leaf(const SliceWork& w, const StateView& s
         ref[1] = u;
         ref[2] = v;
     }
-    const float* p = st.xyz + (lb + leaf) * 3;
-    const float x0 = p[0], y0 = p[1], z0 = p[2];
-    const float* m = w.mv;
-    const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
-    const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
-    const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
     const float du = __fsub_rn(u, 128.0f), dv = __fsub_rn(v, 128.0f);
     const float R = __fadd_rn(y, __fmul_rn(1.4020f, dv));
     const float G = __fsub_rn(__fsub_rn(y, __fmul_rn(0.3441f, du)), __fmul_rn(0.7141f, dv));
     const float B = __fadd_rn(y, __fmul_rn(1.7720f, du));
     const uint64_t oi = w.out_off + leaf;
-    if (o.xyz) {
-        o.xyz[oi * 3 + 0] = X;
-        o.xyz[oi * 3 + 1] = Y;
-        o.xyz[oi * 3 + 2] = Z;
-    }
     if (o.rgb) {
         o.rgb[oi * 3 + 0] = to_u8(R);
         o.rgb[oi * 3 + 1] = to_u8(G);
         o.rgb[oi * 3 + 2] = to_u8(B);
     }
-    if (o.p24) {  // CUDA2OpenGL.cu:44-58: unrounded /255, patches under 10 points white
+    if (o.p24) {  // CUDA2OpenGL.cu:44-58: unrounded /255, patches under 10 points white (x, y, z: k_xyz)
         float* q = o.p24 + oi * 6;
         const bool white = w.n < 10;
-        q[0] = X;
-        q[1] = Y;
-        q[2] = Z;
         q[3] = white ? 1.0f : __fdiv_rn(R, 255.0f);
         q[4] = white ? 1.0f : __fdiv_rn(G, 255.0f);
         q[5] = white ? 1.0f : __fdiv_rn(B, 255.0f);
@@ -764,76 +1047,18 @@ __global__ void __launch_bounds__(T) k_raht_slice(const SliceWork* __restrict__ 
     }
 }
 
-// ---------------------------------------------------------------------------
-// k_raht_group: one warp per group of slices that share a slot (the frames of
-// one patch in a GoP).  All lanes walk the same tree depth first in lockstep
-// (node records are warp-wide broadcast loads, control flow is uniform); lane
-// f owns frame f's coefficients, signal and output.  The intra slice, when
-// the group has one, is lane 0, and its leaf colours reach the predictive
-// lanes by shuffle (the reference add of invert_raht_octree.cc:304-308).
-
-__device__ __forceinline__ void group_emit(const SliceWork& w, bool act, bool intra_lane, bool ref_lane0, const StateView& st,
-                                           size_t lb, uint32_t leaf, float y, float u, float v, const OutPtrs& o) {
-    float ry, ru, rv;
-    if (ref_lane0) {  // lane 0 holds the intra colours of this leaf
-        ry = __shfl_sync(0xffffffffu, y, 0);
-        ru = __shfl_sync(0xffffffffu, u, 0);
-        rv = __shfl_sync(0xffffffffu, v, 0);
-    } else {
-        const float* r = st.ref + (lb + leaf) * 3;
-        ry = r[0];
-        ru = r[1];
-        rv = r[2];
-    }
-    if (!act) return;
-    if (intra_lane) {
-        float* r = st.ref + (lb + leaf) * 3;
-        r[0] = y;
-        r[1] = u;
-        r[2] = v;
-    } else {
-        y = __fadd_rn(y, ry);
-        u = __fadd_rn(u, ru);
-        v = __fadd_rn(v, rv);
-    }
-    const float* p = st.xyz + (lb + leaf) * 3;
-    const float x0 = p[0], y0 = p[1], z0 = p[2];
-    const float* m = w.mv;
-    const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
-    const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
-    const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
-    const float du = __fsub_rn(u, 128.0f), dv = __fsub_rn(v, 128.0f);
-    const float R = __fadd_rn(y, __fmul_rn(1.4020f, dv));
-    const float G = __fsub_rn(__fsub_rn(y, __fmul_rn(0.3441f, du)), __fmul_rn(0.7141f, dv));
-    const float B = __fadd_rn(y, __fmul_rn(1.7720f, du));
-    const uint64_t oi = w.out_off + leaf;
-    if (o.xyz) {
-        o.xyz[oi * 3 + 0] = X;
-        o.xyz[oi * 3 + 1] = Y;
-        o.xyz[oi * 3 + 2] = Z;
-    }
-    if (o.rgb) {
-        o.rgb[oi * 3 + 0] = to_u8(R);
-        o.rgb[oi * 3 + 1] = to_u8(G);
-        o.rgb[oi * 3 + 2] = to_u8(B);
-    }
-    if (o.p24) {
-        float* q = o.p24 + oi * 6;
-        const bool white = w.n < 10;
-        q[0] = X;
-        q[1] = Y;
-        q[2] = Z;
-        q[3] = white ? 1.0f : __fdiv_rn(R, 255.0f);
-        q[4] = white ? 1.0f : __fdiv_rn(G, 255.0f);
-        q[5] = white ? 1.0f : __fdiv_rn(B, 255.0f);
-    }
-}
-
 // inverse_node for a lane that may be inactive (no coefficient loads then),
 // given the node's coded-slot mask `m`, first coefficient `ci` and butterfly
 // pairs ab[i * AS] (AS = 1: the state's node record; 32: a warp's staged
 // rows).  Coded slot i reads coefficient ci + (coded slots below i), so the
 // node's coefficient loads are independent and issue together.
+//
+// `m` is the same in every lane (the lanes share the tree), so each slot's
+// branch is uniform.  An uncoded butterfly has a zero weight on one side
+// and h = 0: with (a, b) = (1, 0), G = g*1 + 0*(-0) = g exactly and H feeds
+// only the empty side; with (0, 1), H = g*1 + 0*0 = g + 0 (+0 for g = -0)
+// and G feeds only the empty side; with both weights zero neither is read.
+// So G = g, H = g + 0 reproduce every value a child can see.
 template <int S, int AS>  // coefficient stride (32 in frame-interleaved group regions), ab stride
 __device__ __forceinline__ void lane_node_md(uint32_t m, uint32_t ci, const float2* ab, bool act, const float* cy,
                                              const float* cu, const float* cv, float gy, float gu, float gv,
@@ -853,16 +1078,26 @@ __device__ __forceinline__ void lane_node_md(uint32_t m, uint32_t ci, const floa
     sv[1] = gv;
 #pragma unroll
     for (int i = 1; i < 8; ++i) {
-        const float2 t = ab[(i - 1) * AS];
         const float ay = sy[i], au = su[i], av = sv[i];
-        const float nbv = -t.y;
-        // [G;H] = [[a,-b],[b,a]] [g;h]   (InvertHaarTransform, octree_base.cc:186-206)
-        const float Gy = __fadd_rn(__fmul_rn(ay, t.x), __fmul_rn(hy[i], nbv));
-        const float Gu = __fadd_rn(__fmul_rn(au, t.x), __fmul_rn(hu[i], nbv));
-        const float Gv = __fadd_rn(__fmul_rn(av, t.x), __fmul_rn(hv[i], nbv));
-        const float Hy = __fadd_rn(__fmul_rn(ay, t.y), __fmul_rn(hy[i], t.x));
-        const float Hu = __fadd_rn(__fmul_rn(au, t.y), __fmul_rn(hu[i], t.x));
-        const float Hv = __fadd_rn(__fmul_rn(av, t.y), __fmul_rn(hv[i], t.x));
+        float Gy, Gu, Gv, Hy, Hu, Hv;
+        if (m & (1u << i)) {
+            const float2 t = ab[(i - 1) * AS];
+            const float nbv = -t.y;
+            // [G;H] = [[a,-b],[b,a]] [g;h]   (InvertHaarTransform, octree_base.cc:186-206)
+            Gy = __fadd_rn(__fmul_rn(ay, t.x), __fmul_rn(hy[i], nbv));
+            Gu = __fadd_rn(__fmul_rn(au, t.x), __fmul_rn(hu[i], nbv));
+            Gv = __fadd_rn(__fmul_rn(av, t.x), __fmul_rn(hv[i], nbv));
+            Hy = __fadd_rn(__fmul_rn(ay, t.y), __fmul_rn(hy[i], t.x));
+            Hu = __fadd_rn(__fmul_rn(au, t.y), __fmul_rn(hu[i], t.x));
+            Hv = __fadd_rn(__fmul_rn(av, t.y), __fmul_rn(hv[i], t.x));
+        } else {
+            Gy = ay;
+            Gu = au;
+            Gv = av;
+            Hy = __fadd_rn(ay, 0.0f);
+            Hu = __fadd_rn(au, 0.0f);
+            Hv = __fadd_rn(av, 0.0f);
+        }
         if (pair0(i) < 8) {
             sy[pair0(i)] = Gy; su[pair0(i)] = Gu; sv[pair0(i)] = Gv;
             sy[pair1(i)] = Hy; su[pair1(i)] = Hu; sv[pair1(i)] = Hv;
@@ -908,8 +1143,7 @@ constexpr int kWarpLeaves = 16;              // staged leaves per warp (a node a
 constexpr int kStageRow = kWarpLeaves + 1;   // odd row length: the 32 lanes' column stores hit 32 banks
 static_assert(kWarpLeaves == 16, "the flush maps a frame's staged leaves onto a half-warp");
 
-// A warp stages colours only: leaf centres are the same in every frame of
-// the group, and the flush transforms them with each frame's matrix.
+// A warp stages colours only (k_xyz writes the coordinates).
 template <bool P24>
 struct WarpStage {
     uint32_t rgb[32][kStageRow];
@@ -939,7 +1173,6 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
     __shared__ int s_g, s_H, s_ls[kMaxLevels + 1];
     __shared__ uint64_t s_out[32];
     __shared__ int s_act[32], s_white[32];
-    __shared__ float s_mv[32][13];  // each frame's transform rows (odd stride: the lanes' row fills hit 32 banks)
     __shared__ NodeRows s_nodes[kGrpWarps];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     WarpStage<P24>& ws = sg.w[wid];
@@ -968,8 +1201,6 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
             s_act[lane] = act;
             s_out[lane] = act ? w.out_off : 0;
             s_white[lane] = act && w.n < 10;
-#pragma unroll
-            for (int i = 0; i < 12; ++i) s_mv[lane][i] = act ? w.mv[i] : 0.f;
         }
         const bool any = __any_sync(0xffffffffu, act);  // the same in every warp
         const bool ref_lane0 = G.intra && !ierr;
@@ -1025,31 +1256,14 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
             };
             // the warp writes its staged leaves [base, base + cnt) of every active
             // frame, two frames per pass: half-warp h writes frame f0 + h, its
-            // lanes consecutive points of that frame.  The leaf centre (read
-            // once) goes through the frame's transform here.
+            // lanes consecutive points of that frame.
             auto flush = [&](uint32_t base, uint32_t cnt) {
                 __syncwarp();
                 const uint32_t i = lane & 15, h = lane >> 4;
-                float x0 = 0.f, y0 = 0.f, z0 = 0.f;
-                if (i < cnt) {
-                    const float* p = st.xyz + (lb + base + i) * 3;
-                    x0 = __ldg(p);
-                    y0 = __ldg(p + 1);
-                    z0 = __ldg(p + 2);
-                }
                 for (uint32_t f0 = 0; f0 < 32; f0 += 2) {
                     const uint32_t f = f0 + h;
                     if (i >= cnt || !s_act[f]) continue;
                     const uint64_t oi = s_out[f] + base + i;
-                    const float* m = s_mv[f];
-                    const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
-                    const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
-                    const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
-                    if (o.xyz) {
-                        o.xyz[oi * 3 + 0] = X;
-                        o.xyz[oi * 3 + 1] = Y;
-                        o.xyz[oi * 3 + 2] = Z;
-                    }
                     const uint32_t c = ws.rgb[f][i];
                     if (o.rgb) {
                         o.rgb[oi * 3 + 0] = (uint8_t)c;
@@ -1059,9 +1273,6 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
                     if constexpr (P24) {
                         float* q = o.p24 + oi * 6;
                         const bool white = s_white[f];
-                        q[0] = X;
-                        q[1] = Y;
-                        q[2] = Z;
                         q[3] = white ? 1.0f : ws.fr[f][i];
                         q[4] = white ? 1.0f : ws.fg[f][i];
                         q[5] = white ? 1.0f : ws.fb[f][i];
@@ -1211,6 +1422,14 @@ cudaError_t prepare_kernels() {
         e = cudaFuncSetAttribute(k_rlgr<256, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_rlgr<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, kRlgrLongSmem);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rlgr_win<1, kWinRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, win_smem(1, kWinRows));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rlgr_win<2, kWinRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, win_smem(2, kWinRows));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rlgr_win<4, kWinRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, win_smem(4, kWinRows));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_rlgr_win<8, kWinRows>, cudaFuncAttributeMaxDynamicSharedMemorySize, win_smem(8, kWinRows));
     if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
     return e;
 }
@@ -1219,6 +1438,14 @@ cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payloa
                         cudaStream_t s) {
     if (nintra <= 0) return cudaSuccess;
     k_tree<kTreeThreads><<<nintra, kTreeThreads, 0, s>>>(work, payload, st, tstatus);
+    return cudaGetLastError();
+}
+
+constexpr int kXyzThreads = 128;
+cudaError_t launch_xyz(const SliceWork* work, int nslices, const StateView& st, const int32_t* tstatus, float* xyz,
+                       float* p24, cudaStream_t s) {
+    if (nslices <= 0 || (!xyz && !p24)) return cudaSuccess;
+    k_xyz<kXyzThreads><<<nslices, kXyzThreads, 0, s>>>(work, st, tstatus, xyz, p24);
     return cudaGetLastError();
 }
 
@@ -1251,6 +1478,25 @@ cudaError_t launch_rlgr_long(const SliceWork* work, const int32_t* order, int ns
         case 8: k_rlgr<512, 8><<<grid, 512, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
         case 16: k_rlgr<256, 16><<<grid, 256, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
         case 32: k_rlgr<128><<<grid, 128, smem, s>>>(work, order, nslices, payload, coef, rstatus); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// Windowed RLGR of `ngroups` groups, one warp each, `warps` per CTA; a
+// warp's rings and window take 10 KB, a CTA at least kWinMinSmem, more than
+// the SM of a long per-slice CTA has left.
+cudaError_t launch_rlgr_win(const SliceWork* work, const GroupDesc* groups, int ngroups, const int32_t* items,
+                            const uint8_t* payload, float* coef, int32_t* rstatus, int warps, cudaStream_t s) {
+    if (ngroups <= 0) return cudaSuccess;
+    static_assert(win_smem(1, kWinRows) + 1024 > 228 * 1024 - (kRlgrLongSmem + 1024),
+                  "a windowed CTA must not fit beside a long CTA");
+    const int grid = (ngroups + warps - 1) / warps;
+    switch (warps) {
+        case 1: k_rlgr_win<1, kWinRows><<<grid, 32, win_smem(1, kWinRows), s>>>(work, groups, ngroups, items, payload, coef, rstatus); break;
+        case 2: k_rlgr_win<2, kWinRows><<<grid, 64, win_smem(2, kWinRows), s>>>(work, groups, ngroups, items, payload, coef, rstatus); break;
+        case 4: k_rlgr_win<4, kWinRows><<<grid, 128, win_smem(4, kWinRows), s>>>(work, groups, ngroups, items, payload, coef, rstatus); break;
+        case 8: k_rlgr_win<8, kWinRows><<<grid, 256, win_smem(8, kWinRows), s>>>(work, groups, ngroups, items, payload, coef, rstatus); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

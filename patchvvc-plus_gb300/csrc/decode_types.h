@@ -19,6 +19,11 @@ constexpr int kMaxLevels = 32;  // octree height limit (the header stores a u8)
 constexpr int kRlgrLongSmem = 212 * 1024;
 constexpr int kRlgrShortSmem = 32 * 1024;
 constexpr int kRlgrLongBlock = 128;
+// Window groups (decoded by the windowed RLGR, one warp per group, unless
+// they are in the long tier): at least this many slices, all of one size;
+// the long tier takes kWinGroupsPerLongCta of them per long CTA.
+constexpr int kWinGroupMin = 16;
+constexpr int kWinGroupsPerLongCta = 4;
 
 struct SliceWork {
     uint64_t col_off;   // colour payload byte offset

@@ -153,7 +153,7 @@ def tune_dict(t: L.Tune) -> dict:
 
 def autotune(b: Batch, dec: "Decoder", payload_ptr: int, reps: int = 3, stream: int = 0) -> tuple[dict, float]:
     """pvvc_plan_autotune: the fastest launch shapes for this batch and their
-    mean device time (ms).  Decodes the batch for real into `dec`."""
+    median device time (ms).  Decodes the batch for real into `dec`."""
     d, keep = _desc(b)
     best = L.Tune(0, 0, 0)
     ms = C.c_float(0)

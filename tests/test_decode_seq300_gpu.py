@@ -6,7 +6,10 @@ octrees 10-11 levels deep) at every quantisation step of the sweep
 the long-slice RLGR split forced on, and with a three-tier split, through
 pvvc_decode and through a CUDA-graph replay; geometry (uint32 view) and
 colours must equal the oracle's restatement of the reference CPU decoder
-(invert_raht_octree.cc:22-120, pvvc_decompression.cc:141-150) bit for bit."""
+(invert_raht_octree.cc:22-120, pvvc_decompression.cc:141-150) bit for bit.
+Every group here (the 30 frames of a patch) is a window group: the long
+tier's slices are decoded one thread per slice, the others by the windowed
+RLGR, a warp per group."""
 import os
 
 import numpy as np
@@ -75,6 +78,11 @@ def test_seq300_gop_bit_exact(pvvc_lib, oracle, torch, qp):
     for tune, graph in shapes:
         xyz, rgb, st, info = _decode(torch, pvvc, batch, dec, pay, tune, graph)
         assert (st == 0).all(), (tune, np.unique(st))
+        # every group holds the 30 frames of a patch: all but the long tier's go to the windowed RLGR, which writes
+        # every coefficient itself, so only the long tier's planes (the largest patches) are cleared -- less than
+        # all of them (3 planes x 32 lanes x 4 bytes per leaf of each group's tree)
+        full = 384 * int(batch.size[(batch.type & 0x02) == 0].astype(np.int64).sum())
+        assert 0 < info["clear_bytes"] < full, (info["clear_bytes"], full)
         if tune is not auto:
             assert info["tune"]["rlgr_long_ctas"] > 0
         bad = np.flatnonzero((xyz.view(np.uint32) != want_xyz.view(np.uint32)).any(1))

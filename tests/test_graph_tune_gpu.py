@@ -50,7 +50,10 @@ def test_plan_info_counts(pvvc_lib, gop):
     ones = pvvc_lib.Plan(gop, tune=(3, 32, 128, -1, -1, 32)).info()
     assert ones["groups_a"] == default["nintra"] and ones["singles_a"] == 0
     k = ones
-    assert k["kernels"] == 2 + (k["groups_a"] > 0) + (k["singles_a"] > 0) + (k["groups_b"] > 0) + (k["singles_b"] > 0)
+    # trees, coordinates, one per-slice RLGR launch (8-frame groups are below the windowed RLGR's 16), then the
+    # inverse-RAHT launches
+    assert k["kernels"] == 3 + (k["groups_a"] > 0) + (k["singles_a"] > 0) + (k["groups_b"] > 0) + (k["singles_b"] > 0)
+    assert k["clear_bytes"] > 0
 
 
 def test_autotune_returns_a_valid_shape(pvvc_lib, torch, gop):
