@@ -7,8 +7,10 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <thread>
 #include <vector>
@@ -40,17 +42,6 @@ int resolve_tune(const pvvc_tune* in, pvvc_tune* out) {
 }
 
 namespace {
-// A host array left uninitialised (every element is written before it is
-// read): per-slice tables of large calls without the cost of zeroing them.
-template <class T>
-struct RawArray {
-    std::unique_ptr<T[]> a;
-    explicit RawArray(size_t n) : a(new T[n ? n : 1]) {}
-    T& operator[](size_t i) { return a[i]; }
-    const T& operator[](size_t i) const { return a[i]; }
-    T* data() { return a.get(); }
-    const T* data() const { return a.get(); }
-};
 
 // Runs fn(i) for i in [0, n) on up to `threads` host threads.
 template <class F>
@@ -702,8 +693,11 @@ extern "C" int pvvc_state_destroy(pvvc_state* st) {
         if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : st->zdone)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : st->up_done)
+        if (e) cudaEventDestroy(e);
     if (st->copy) cudaStreamDestroy(st->copy);
     if (st->zside) cudaStreamDestroy(st->zside);
+    if (st->up) cudaStreamDestroy(st->up);
     delete st;
     return PVVC_OK;
 }
@@ -1029,15 +1023,41 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         nsl += (int32_t)frames[f].count();
     }
     ffirst[nframes] = nsl;
-    RawArray<int32_t> slot(nsl), index(nsl);
-    RawArray<uint8_t> type(nsl), qp(nsl);
-    RawArray<uint32_t> size(nsl), gsz(nsl), csz(nsl);
-    RawArray<float> mv(16ull * nsl);
-    RawArray<uint64_t> goff(nsl), coff(nsl), oo(nsl);
+    // the call's description arrays, carved from one grow-only host buffer
+    // that the state keeps (a fresh allocation of this size would come from
+    // new pages each call, and their first-touch faults cost milliseconds)
+    int32_t *slot, *index;
+    uint8_t *type, *qp;
+    uint32_t *size, *gsz, *csz;
+    float* mv;
+    uint64_t *goff, *coff, *oo;
+    {
+        const size_t n = (size_t)std::max(nsl, 1);
+        uint64_t at[11], o = 0;
+        const size_t bytes[11] = {4 * n, 4 * n, n, n, 4 * n, 4 * n, 4 * n, 64 * n, 8 * n, 8 * n, 8 * n};
+        for (int i = 0; i < 11; ++i) {
+            at[i] = o;
+            o = align_up(o + bytes[i], 64);
+        }
+        unsigned char* b = st->host_desc.get(o);
+        if (!b) return PVVC_ERR_NOMEM;
+        slot = reinterpret_cast<int32_t*>(b + at[0]);
+        index = reinterpret_cast<int32_t*>(b + at[1]);
+        type = b + at[2];
+        qp = b + at[3];
+        size = reinterpret_cast<uint32_t*>(b + at[4]);
+        gsz = reinterpret_cast<uint32_t*>(b + at[5]);
+        csz = reinterpret_cast<uint32_t*>(b + at[6]);
+        mv = reinterpret_cast<float*>(b + at[7]);
+        goff = reinterpret_cast<uint64_t*>(b + at[8]);
+        coff = reinterpret_cast<uint64_t*>(b + at[9]);
+        oo = reinterpret_cast<uint64_t*>(b + at[10]);
+    }
+    std::vector<uint64_t> fbytes(nframes + 1, 0);  // payload bytes before each frame
     {
         // per frame its payload bytes and points, a prefix over frames, then
         // every frame's slices filled in parallel
-        std::vector<uint64_t> fbytes(nframes + 1, 0), fpts(nframes + 1, 0);
+        std::vector<uint64_t> fpts(nframes + 1, 0);
         parallel_for(nframes, threads, [&](int f) {
             const FrameView& fr = frames[f];
             uint64_t b = 0, q = 0;
@@ -1210,7 +1230,49 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     // inflation on `s`, so both run on the GPU during planning; the decode
     // is queued after the packer has finished.
     bool sent_ok = true;
+    // Raw payloads of a call decoded in parts go up part by part: the packer
+    // packs a part's frames, queues their copy on the upload stream and
+    // records the part's event, so that part 0's decode can start while the
+    // later parts are still being packed (each decode waits for its part's
+    // event; the main thread waits for `packed` to pass the part before it
+    // queues that wait, so the event is recorded first).
+    const bool by_part = nz == 0 && nparts >= 2 && bytes > 0;
+    std::vector<int> fcut;
+    std::mutex pk_mu;
+    std::condition_variable pk_cv;
+    int packed = 0;  // parts whose copy (and event) is queued
+    if (by_part) {
+        if (!st->up && cudaStreamCreateWithFlags(&st->up, cudaStreamNonBlocking) != cudaSuccess) return PVVC_ERR_CUDA;
+        for (cudaEvent_t& e : st->up_done)
+            if (!e && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return PVVC_ERR_CUDA;
+        for (int h = 0; h <= nparts; ++h)  // every cut is the first slice of a frame
+            fcut.push_back((int)(std::lower_bound(ffirst.begin(), ffirst.end(), cuts[h]) - ffirst.begin()));
+    }
     std::thread packer([&] {
+        if (by_part) {
+            for (int h = 0; h < nparts; ++h) {
+                const int f0 = fcut[h], f1 = fcut[h + 1];
+                parallel_for(f1 - f0, std::max(1, threads / 2), [&](int q) {
+                    const int f = f0 + q;
+                    FrameView& fr = frames[f];
+                    for (size_t i = 0; i < fr.count(); ++i) {
+                        const int32_t k = ffirst[f] + (int32_t)i;
+                        if (gsz[k] && fr.geo[i]) std::memcpy(hp + goff[k], fr.geo[i], gsz[k]);
+                        if (csz[k] && fr.col[i]) std::memcpy(hp + coff[k], fr.col[i], csz[k]);
+                    }
+                });
+                const uint64_t a = fbytes[f0], e = h + 1 == nparts ? bytes + 16 : fbytes[f1];
+                const bool ok = e <= a || (cudaMemcpyAsync(static_cast<uint8_t*>(st->payload.p) + a, hp + a, e - a,
+                                                           cudaMemcpyHostToDevice, st->up) == cudaSuccess &&
+                                           cudaEventRecord(st->up_done[h], st->up) == cudaSuccess);
+                std::lock_guard<std::mutex> g(pk_mu);
+                if (!ok) sent_ok = false;
+                packed = ok ? h + 1 : nparts;  // a failure releases the waiter, which then sees sent_ok
+                pk_cv.notify_all();
+                if (!ok) return;
+            }
+            return;
+        }
         parallel_for(nframes, std::max(1, threads / 2), [&](int f) {
             FrameView& fr = frames[f];
             for (size_t i = 0; i < fr.count(); ++i) {
@@ -1269,9 +1331,8 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         g_plan_threads = nthreads;
         const int32_t first = cuts[h], cnt = cuts[h + 1] - first;
         pvvc_plan* pl = h ? &st->part_plan[h - 1] : &st->plan;
-        pvvc_batch_desc d{cnt,          slot.data() + first, type.data() + first, size.data() + first, qp.data() + first,
-                          mv.data() + 16ull * first, goff.data() + first, gsz.data() + first, coff.data() + first,
-                          csz.data() + first, oo.data() + first};
+        pvvc_batch_desc d{cnt,          slot + first, type + first, size + first, qp + first, mv + 16ull * first,
+                          goff + first, gsz + first, coff + first, csz + first, oo + first};
         plan_rc[h] = build_plan(&d, pl, nullptr, s);
         g_plan_threads = 0;
     };
@@ -1297,7 +1358,15 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         g_stage_ms[2] += clk.lap();
         if (st->ws.ensure(pl->ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
         g_stage_ms[5] += clk.lap();
-        if (!payload_queued()) return PVVC_ERR_CUDA;
+        if (by_part) {
+            std::unique_lock<std::mutex> g(pk_mu);
+            pk_cv.wait(g, [&] { return packed > h; });
+            if (!sent_ok) return PVVC_ERR_CUDA;
+            g.unlock();
+            if (cudaStreamWaitEvent(s, st->up_done[h], 0) != cudaSuccess) return PVVC_ERR_CUDA;
+        } else if (!payload_queued()) {
+            return PVVC_ERR_CUDA;
+        }
         if (h > 0 && nz && cudaStreamWaitEvent(s, st->zdone[h], 0) != cudaSuccess) return PVVC_ERR_CUDA;
         g_stage_ms[4] += clk.lap();
         rc = run_decode(pl, st, static_cast<const uint8_t*>(st->payload.p), out_xyz, out_rgb, nullptr,
@@ -1326,9 +1395,8 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
     for (size_t b = 0; b + 1 < runs.size() && rc == PVVC_OK; ++b) {
         const int32_t first = runs[b], cnt = runs[b + 1] - first;
         if (cnt <= 0) continue;
-        pvvc_batch_desc d{cnt,          slot.data() + first, type.data() + first, size.data() + first, qp.data() + first,
-                          mv.data() + 16ull * first, goff.data() + first, gsz.data() + first, coff.data() + first,
-                          csz.data() + first, oo.data() + first};
+        pvvc_batch_desc d{cnt,          slot + first, type + first, size + first, qp + first, mv + 16ull * first,
+                          goff + first, gsz + first, coff + first, csz + first, oo + first};
         // the plan's arrays go up on `s` from pinned mirrors that stay as
         // they are until the next plan, which follows a synchronisation
         rc = build_plan(&d, &st->plan, nullptr, s);

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
+#include <new>
 #include <vector>
 
 #include "decode_types.h"
@@ -104,6 +106,17 @@ struct SideStream {
         return e;
     }
 };
+struct GrowBuf {  // pageable host memory, grow-only (its pages stay mapped between uses)
+    std::unique_ptr<unsigned char[]> p;
+    size_t cap = 0;
+    unsigned char* get(size_t n) {
+        if (n > cap) {
+            p.reset(new (std::nothrow) unsigned char[n]);
+            cap = p ? n : 0;
+        }
+        return p.get();
+    }
+};
 struct HostBuf {  // pinned, grow-only
     void* p = nullptr;
     size_t cap = 0;
@@ -164,6 +177,7 @@ struct pvvc_state {
     // buffers of the end-to-end host call, kept across calls
     pvvc::DevBuf payload, xyz, rgb, ws, status;
     pvvc::HostBuf h_payload;
+    pvvc::GrowBuf host_desc;  // the host call's description arrays
     pvvc_plan plan;
     static constexpr int kParts = 3;        // a multi-GoP call is decoded in up to this many parts
     // part boundaries, as fractions of the slices: a small first part starts
@@ -174,6 +188,8 @@ struct pvvc_state {
     cudaStream_t copy = nullptr;            // device-to-host copies that overlap the next part's decode
     cudaEvent_t part_done[kParts] = {};
     cudaStream_t zside = nullptr;           // zstd inflation of the parts after the first
+    cudaStream_t up = nullptr;              // host-to-device copies of the parts' raw payloads
+    cudaEvent_t up_done[kParts] = {};
     cudaEvent_t zdone[kParts] = {};
 };
 
