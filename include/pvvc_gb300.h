@@ -102,16 +102,16 @@ int pvvc_plan_query(const pvvc_plan* plan, uint64_t* total_points, uint64_t* wor
  * slice into planes cleared beforehand; when no group qualifies, those
  * slices are split into the size tiers below. */
 typedef struct {
-    int32_t group_ctas_per_sm; /* persistent CTAs of the grouped inverse-RAHT kernel per SM: 1..4 (default 3)   */
+    int32_t group_ctas_per_sm; /* persistent CTAs of the grouped inverse-RAHT kernel per SM: 1..4 (default 4)   */
     int32_t min_group;         /* a slot's predictive slices share one warp when at least this many: 1..32 (4) */
-    int32_t rlgr_block;        /* threads per CTA of the RLGR kernels: 32, 64, 128 or 256 (default 128); the
+    int32_t rlgr_block;        /* threads per CTA of the RLGR kernels: 32, 64, 128 or 256 (default 64); the
                                   windowed form runs rlgr_block / 32 groups per CTA                               */
     int32_t rlgr_long_ctas;    /* CTAs of 128 threads that decode the longest slices (with window groups: the
                                   slices of the 4 x rlgr_long_ctas largest groups) alone on an SM each, side by
-                                  side with the rest: 0..152 (default 32); -1 turns the split off                */
+                                  side with the rest: 0..152 (default 16); -1 turns the split off                */
     int32_t rlgr_mid_pct;      /* with the split on: percent of the other slices or groups (the larger ones)
                                   decoded, and their groups inverse-transformed, on a third stream: 0..90
-                                  (default 30); -1 off                                                            */
+                                  (default 50); -1 off                                                            */
     int32_t rlgr_long_lanes;   /* slices per warp in the per-slice long launch: 8, 16 or 32 (default 32)        */
 } pvvc_tune;
 int pvvc_plan_create_tuned(const pvvc_batch_desc* desc, const pvvc_tune* tune, pvvc_plan** out);

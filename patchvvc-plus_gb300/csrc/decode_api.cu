@@ -96,7 +96,22 @@ void sort_by_size_slot(const uint32_t* size, const int32_t* slot, std::vector<in
 }
 }  // namespace
 
-int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload) {
+int upload_plan(pvvc_plan* p, cudaStream_t s) {
+    if (!p->upload_pending) return PVVC_OK;
+    p->upload_pending = false;
+    const size_t n = (size_t)p->nslices;
+    const size_t wb = sizeof(SliceWork) * n, ob = 4ull * n;
+    const size_t gb = sizeof(GroupDesc) * p->groups.size(), ib = 4ull * p->idx.size();
+    auto put = [&](DevBuf& d, HostBuf& h, size_t bytes) {
+        return !bytes || cudaMemcpyAsync(d.p, h.p, bytes, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    };
+    if (!put(p->d_work, p->h_work, wb) || !put(p->d_order, p->h_order, ob) || !put(p->d_groups, p->h_groups, gb) ||
+        !put(p->d_idx, p->h_idx, ib))
+        return PVVC_ERR_CUDA;
+    return PVVC_OK;
+}
+
+int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload, bool defer) {
     if (!d || d->nslices < 0) return PVVC_ERR_ARG;
     if (resolve_tune(tune, &p->tune)) return PVVC_ERR_ARG;
     if (prepare_kernels() != cudaSuccess) return PVVC_ERR_CUDA;
@@ -227,7 +242,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
             if (p->nmid > 0 && p->side2.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
         }
     }
-    if (n > 0 && p->tree.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+    if (!intra.empty() && p->tree.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
     lap(1);  // RLGR order and tiers
     // inverse-RAHT schedule: slices grouped by slot (largest slots first)
     {
@@ -448,11 +463,12 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
                 if (h.ensure(bytes) != cudaSuccess) return false;
                 std::memcpy(h.p, src, bytes);
             }
-            return cudaMemcpyAsync(d.p, h.p, bytes, cudaMemcpyHostToDevice, upload) == cudaSuccess;
+            return defer || cudaMemcpyAsync(d.p, h.p, bytes, cudaMemcpyHostToDevice, upload) == cudaSuccess;
         };
         if (!put(p->d_work, p->h_work, W, wb) || !put(p->d_order, p->h_order, p->order.data(), ob) ||
             !put(p->d_groups, p->h_groups, p->groups.data(), gb) || !put(p->d_idx, p->h_idx, p->idx.data(), ib))
             return PVVC_ERR_CUDA;
+        p->upload_pending = upload && defer;  // the copies are queued later by upload_plan
     }
     lap(4);  // upload
     return PVVC_OK;
@@ -478,22 +494,16 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
     };
     if (!mark(0)) return PVVC_ERR_CUDA;
     // The tree expansion reads only geometry payloads and writes only slot
-    // tables, and the output coordinates need only the trees; the coefficient
-    // clear and RLGR touch only colour payloads and coefficient planes:
-    // without stage markers the trees and then the coordinates are computed
-    // beside them on a stream of their own.  The inverse RAHT waits for the
-    // trees (event `mid`), the end of the decode for the coordinates
-    // (event `join`).
-    const bool tree_aside = !events;
+    // tables, the coefficient clear and RLGR only colour payloads and
+    // coefficient planes: without stage markers the tree runs beside them on
+    // a stream of their own, joined (event `mid`) before the inverse RAHT.
+    const bool tree_aside = !events && p->nintra > 0;
     if (tree_aside) {
         const SideStream& tr = p->tree;
         if (cudaEventRecord(tr.fork, s) != cudaSuccess || cudaStreamWaitEvent(tr.s, tr.fork, 0) != cudaSuccess ||
-            launch_tree(dw, p->nintra, payload, st->v, ts, tr.s) != cudaSuccess || cudaEventRecord(tr.mid, tr.s) != cudaSuccess ||
-            launch_xyz(dw, p->nslices, st->v, ts, xyz, p24, tr.s) != cudaSuccess ||
-            cudaEventRecord(tr.join, tr.s) != cudaSuccess)
+            launch_tree(dw, p->nintra, payload, st->v, ts, tr.s) != cudaSuccess || cudaEventRecord(tr.mid, tr.s) != cudaSuccess)
             return PVVC_ERR_CUDA;
-    } else if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess ||
-               launch_xyz(dw, p->nslices, st->v, ts, xyz, p24, s) != cudaSuccess || !mark(1)) {
+    } else if (launch_tree(dw, p->nintra, payload, st->v, ts, s) != cudaSuccess || !mark(1)) {
         return PVVC_ERR_CUDA;
     }
     float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
@@ -624,7 +634,6 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
             cudaSuccess ||
         !mark(4))
         return PVVC_ERR_CUDA;
-    if (tree_aside && cudaStreamWaitEvent(s, p->tree.join, 0) != cudaSuccess) return PVVC_ERR_CUDA;  // the coordinates
     return PVVC_OK;
 }
 
@@ -738,13 +747,13 @@ extern "C" int pvvc_plan_info_get(const pvvc_plan* p, pvvc_plan_info* info) {
             ? 4ull * p->coef_long_floats + (p->nslices > p->nwin_slices ? 4ull * (p->coef_floats - p->coef_win_floats) : 0ull)
             : 4ull * p->coef_floats;
     if (p->nslices > 0 && p->nwin > 0)
-        info->kernels = (p->nintra > 0) + 1 + (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
+        info->kernels = (p->nintra > 0) + (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
                         (p->nwin > p->ngroups_a_long + p->ngroups_a_mid) + (p->nslices > p->nwin_slices) +
                         (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
                         (p->ngroups_a > p->ngroups_a_long + p->ngroups_a_mid) + (p->nlist_a > 0) + (p->ngroups_b > 0) +
                         (p->nlist_b > 0);
     else if (p->nslices > 0)
-        info->kernels = (p->nintra > 0) + 2 + (p->nlong > 0) + (p->nmid > 0) +
+        info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) + (p->nmid > 0) +
                         (p->nlong > 0 ? (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
                                             (p->ngroups_a > p->ngroups_a_long + p->ngroups_a_mid)
                                       : (p->ngroups_a > 0)) +
@@ -1333,7 +1342,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         pvvc_plan* pl = h ? &st->part_plan[h - 1] : &st->plan;
         pvvc_batch_desc d{cnt,          slot + first, type + first, size + first, qp + first, mv + 16ull * first,
                           goff + first, gsz + first, coff + first, csz + first, oo + first};
-        plan_rc[h] = build_plan(&d, pl, nullptr, s);
+        plan_rc[h] = build_plan(&d, pl, nullptr, s, true);  // copies queued by this thread below
         g_plan_threads = 0;
     };
     std::vector<std::thread> planners;
@@ -1357,6 +1366,7 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         for (int k = 0; k < 5; ++k) g_stage_ms[8 + k] += pl->host_ms[k];
         g_stage_ms[2] += clk.lap();
         if (st->ws.ensure(pl->ws_bytes) != cudaSuccess) return PVVC_ERR_NOMEM;
+        if (upload_plan(pl, s) != PVVC_OK) return PVVC_ERR_CUDA;
         g_stage_ms[5] += clk.lap();
         if (by_part) {
             std::unique_lock<std::mutex> g(pk_mu);

@@ -22,9 +22,6 @@ int pvvc_zstd_merge_status(int32_t njobs, const int32_t* zstatus, const int32_t*
 namespace pvvc {
 cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payload, const StateView& st, int32_t* tstatus,
                         cudaStream_t s);
-// output coordinates of every slice of the queue whose geometry is in place
-cudaError_t launch_xyz(const SliceWork* work, int nslices, const StateView& st, const int32_t* tstatus, float* xyz,
-                       float* p24, cudaStream_t s);
 cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
                         int32_t* rstatus, int block, int smem, cudaStream_t s);
 cudaError_t launch_rlgr_long(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
@@ -43,11 +40,11 @@ cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, in
 // default launch shapes: persistent CTAs of the group kernel per SM (its
 // registers allow four), the group threshold, the RLGR block, and
 // the CTAs that decode the longest slices on SMs of their own
-constexpr int kGroupCtasPerSm = 3;
+constexpr int kGroupCtasPerSm = 4;
 constexpr int kMinGroup = 4;
-constexpr int kRlgrBlock = 128;
-constexpr int kRlgrLongCtas = 32;
-constexpr int kRlgrMidPct = 30;
+constexpr int kRlgrBlock = 64;
+constexpr int kRlgrLongCtas = 16;
+constexpr int kRlgrMidPct = 50;
 constexpr int kRlgrLongLanes = 32;
 
 // the SM count (queried once)
@@ -170,6 +167,7 @@ struct pvvc_plan {
     pvvc::SideStream side;   // the long tier's stream
     pvvc::SideStream side2;  // the medium tier's stream
     pvvc::SideStream tree;   // the tree expansion's stream (beside the coefficient clear and RLGR)
+    bool upload_pending = false;  // built with deferred copies, not yet queued
 };
 
 struct pvvc_state {
@@ -197,8 +195,11 @@ namespace pvvc {
 // zero tune fields -> defaults; out-of-range fields -> PVVC_ERR_ARG
 int resolve_tune(const pvvc_tune* in, pvvc_tune* out);
 // Sort a batch into the work queue and upload it: synchronously, or with
-// `upload` set, stream-ordered on that stream from pinned mirrors.
-int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload);
+// `upload` set, stream-ordered on that stream from pinned mirrors; with
+// `defer` as well, the copies are left for upload_plan (so that one thread
+// queues every CUDA call of a host call while others plan).
+int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload, bool defer = false);
+int upload_plan(pvvc_plan* p, cudaStream_t s);
 // Enqueue one planned decode on `s` (events: optional stage markers).
 int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb, float* p24,
                int32_t* status, void* ws, uint64_t ws_bytes, cudaStream_t s, void* const* events);

@@ -812,48 +812,6 @@ __global__ void __launch_bounds__(32 * WARPS) k_rlgr_win(const SliceWork* __rest
 }
 
 // ---------------------------------------------------------------------------
-// k_xyz: the output coordinates of every slice whose geometry is in place --
-// its slot's leaf centres through the slice's rigid transform
-// (pvvc_decompression.cc:141-150; GPU CUDA2OpenGL.cu:46-48), in the
-// reference's left-to-right FP32 order.  They depend on the trees only, so
-// this runs right after k_tree, beside RLGR, and the inverse RAHT writes
-// colours only.  A CTA per slice; a slice whose tree or slot is not valid
-// is skipped (the inverse RAHT reports its status).
-template <int T>
-__global__ void __launch_bounds__(T) k_xyz(const SliceWork* __restrict__ work, StateView st,
-                                           const int32_t* __restrict__ tstatus, float* __restrict__ xyz,
-                                           float* __restrict__ p24) {
-    const int item = blockIdx.x;
-    const SliceWork& w = work[item];
-    if (!(w.type & PVVC_TYPE_VALID)) return;
-    if (!(w.type & PVVC_TYPE_PREDICT) && tstatus[item] != PVVC_OK) return;
-    const SlotInfo* si = st.info + w.slot;
-    if (!si->valid || (uint32_t)si->leaves != w.n) return;
-    float m[12];
-#pragma unroll
-    for (int k = 0; k < 12; ++k) m[k] = w.mv[k];
-    const float* c = st.xyz + (size_t)w.slot * st.max_leaves * 3;
-    for (uint32_t i = threadIdx.x; i < w.n; i += T) {
-        const float x0 = __ldg(c + 3ull * i), y0 = __ldg(c + 3ull * i + 1), z0 = __ldg(c + 3ull * i + 2);
-        const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
-        const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
-        const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
-        const uint64_t oi = w.out_off + i;
-        if (xyz) {
-            xyz[oi * 3 + 0] = X;
-            xyz[oi * 3 + 1] = Y;
-            xyz[oi * 3 + 2] = Z;
-        }
-        if (p24) {
-            float* q = p24 + oi * 6;
-            q[0] = X;
-            q[1] = Y;
-            q[2] = Z;
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
 // k_raht
 struct OutPtrs {
     float* xyz;
@@ -872,7 +830,7 @@ __device__ __forceinline__ uint8_t to_u8(float v) {
     return (uint8_t)__float2uint_rd(__fadd_rd(c, 0.5f));
 }
 
-// one leaf: reference add / store, YUV->RGB, colour output (the coordinates come from k_xyz)
+// one leaf: reference add / store, YUV->RGB, transform, output
 __device__ __forceinline__ void emit_leaf(const SliceWork& w, const StateView& st, size_t lb, uint32_t leaf, float y,
                                           float u, float v, bool predict, const OutPtrs& o) {
     float* ref = st.ref + (lb + leaf) * 3;
@@ -885,19 +843,33 @@ __device__ __forceinline__ void emit_leaf(const SliceWork& w, const StateView& s
         ref[1] = u;
         ref[2] = v;
     }
+    const float* p = st.xyz + (lb + leaf) * 3;
+    const float x0 = p[0], y0 = p[1], z0 = p[2];
+    const float* m = w.mv;
+    const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
+    const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
+    const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
     const float du = __fsub_rn(u, 128.0f), dv = __fsub_rn(v, 128.0f);
     const float R = __fadd_rn(y, __fmul_rn(1.4020f, dv));
     const float G = __fsub_rn(__fsub_rn(y, __fmul_rn(0.3441f, du)), __fmul_rn(0.7141f, dv));
     const float B = __fadd_rn(y, __fmul_rn(1.7720f, du));
     const uint64_t oi = w.out_off + leaf;
+    if (o.xyz) {
+        o.xyz[oi * 3 + 0] = X;
+        o.xyz[oi * 3 + 1] = Y;
+        o.xyz[oi * 3 + 2] = Z;
+    }
     if (o.rgb) {
         o.rgb[oi * 3 + 0] = to_u8(R);
         o.rgb[oi * 3 + 1] = to_u8(G);
         o.rgb[oi * 3 + 2] = to_u8(B);
     }
-    if (o.p24) {  // CUDA2OpenGL.cu:44-58: unrounded /255, patches under 10 points white (x, y, z: k_xyz)
+    if (o.p24) {  // CUDA2OpenGL.cu:44-58: unrounded /255, patches under 10 points white
         float* q = o.p24 + oi * 6;
         const bool white = w.n < 10;
+        q[0] = X;
+        q[1] = Y;
+        q[2] = Z;
         q[3] = white ? 1.0f : __fdiv_rn(R, 255.0f);
         q[4] = white ? 1.0f : __fdiv_rn(G, 255.0f);
         q[5] = white ? 1.0f : __fdiv_rn(B, 255.0f);
@@ -1143,7 +1115,8 @@ constexpr int kWarpLeaves = 16;              // staged leaves per warp (a node a
 constexpr int kStageRow = kWarpLeaves + 1;   // odd row length: the 32 lanes' column stores hit 32 banks
 static_assert(kWarpLeaves == 16, "the flush maps a frame's staged leaves onto a half-warp");
 
-// A warp stages colours only (k_xyz writes the coordinates).
+// A warp stages colours only: leaf centres are the same in every frame of
+// the group, and the flush transforms them with each frame's matrix.
 template <bool P24>
 struct WarpStage {
     uint32_t rgb[32][kStageRow];
@@ -1173,6 +1146,7 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
     __shared__ int s_g, s_H, s_ls[kMaxLevels + 1];
     __shared__ uint64_t s_out[32];
     __shared__ int s_act[32], s_white[32];
+    __shared__ float s_mv[32][13];  // each frame's transform rows (odd stride: the lanes' row fills hit 32 banks)
     __shared__ NodeRows s_nodes[kGrpWarps];
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     WarpStage<P24>& ws = sg.w[wid];
@@ -1201,6 +1175,8 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
             s_act[lane] = act;
             s_out[lane] = act ? w.out_off : 0;
             s_white[lane] = act && w.n < 10;
+#pragma unroll
+            for (int i = 0; i < 12; ++i) s_mv[lane][i] = act ? w.mv[i] : 0.f;
         }
         const bool any = __any_sync(0xffffffffu, act);  // the same in every warp
         const bool ref_lane0 = G.intra && !ierr;
@@ -1256,14 +1232,31 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
             };
             // the warp writes its staged leaves [base, base + cnt) of every active
             // frame, two frames per pass: half-warp h writes frame f0 + h, its
-            // lanes consecutive points of that frame.
+            // lanes consecutive points of that frame.  The leaf centre (read
+            // once) goes through the frame's transform here.
             auto flush = [&](uint32_t base, uint32_t cnt) {
                 __syncwarp();
                 const uint32_t i = lane & 15, h = lane >> 4;
+                float x0 = 0.f, y0 = 0.f, z0 = 0.f;
+                if (i < cnt) {
+                    const float* p = st.xyz + (lb + base + i) * 3;
+                    x0 = __ldg(p);
+                    y0 = __ldg(p + 1);
+                    z0 = __ldg(p + 2);
+                }
                 for (uint32_t f0 = 0; f0 < 32; f0 += 2) {
                     const uint32_t f = f0 + h;
                     if (i >= cnt || !s_act[f]) continue;
                     const uint64_t oi = s_out[f] + base + i;
+                    const float* m = s_mv[f];
+                    const float X = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[0]), __fmul_rn(y0, m[1])), __fmul_rn(z0, m[2])), m[3]);
+                    const float Y = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[4]), __fmul_rn(y0, m[5])), __fmul_rn(z0, m[6])), m[7]);
+                    const float Z = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(x0, m[8]), __fmul_rn(y0, m[9])), __fmul_rn(z0, m[10])), m[11]);
+                    if (o.xyz) {
+                        o.xyz[oi * 3 + 0] = X;
+                        o.xyz[oi * 3 + 1] = Y;
+                        o.xyz[oi * 3 + 2] = Z;
+                    }
                     const uint32_t c = ws.rgb[f][i];
                     if (o.rgb) {
                         o.rgb[oi * 3 + 0] = (uint8_t)c;
@@ -1273,6 +1266,9 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
                     if constexpr (P24) {
                         float* q = o.p24 + oi * 6;
                         const bool white = s_white[f];
+                        q[0] = X;
+                        q[1] = Y;
+                        q[2] = Z;
                         q[3] = white ? 1.0f : ws.fr[f][i];
                         q[4] = white ? 1.0f : ws.fg[f][i];
                         q[5] = white ? 1.0f : ws.fb[f][i];
@@ -1438,14 +1434,6 @@ cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payloa
                         cudaStream_t s) {
     if (nintra <= 0) return cudaSuccess;
     k_tree<kTreeThreads><<<nintra, kTreeThreads, 0, s>>>(work, payload, st, tstatus);
-    return cudaGetLastError();
-}
-
-constexpr int kXyzThreads = 128;
-cudaError_t launch_xyz(const SliceWork* work, int nslices, const StateView& st, const int32_t* tstatus, float* xyz,
-                       float* p24, cudaStream_t s) {
-    if (nslices <= 0 || (!xyz && !p24)) return cudaSuccess;
-    k_xyz<kXyzThreads><<<nslices, kXyzThreads, 0, s>>>(work, st, tstatus, xyz, p24);
     return cudaGetLastError();
 }
 

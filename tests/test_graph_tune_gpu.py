@@ -42,17 +42,17 @@ def test_every_launch_shape_decodes_identically(pvvc_lib, torch, gop):
 
 def test_plan_info_counts(pvvc_lib, gop):
     default = pvvc_lib.Plan(gop).info()
-    assert default["tune"] == {"group_ctas_per_sm": 3, "min_group": 4, "rlgr_block": 128, "rlgr_long_ctas": 32,
-                               "rlgr_mid_pct": 30, "rlgr_long_lanes": 32}
+    assert default["tune"] == {"group_ctas_per_sm": 4, "min_group": 4, "rlgr_block": 64, "rlgr_long_ctas": 16,
+                               "rlgr_mid_pct": 50, "rlgr_long_lanes": 32}
     assert default["nslices"] == gop.nslices
     assert default["nintra"] == int(((gop.type & 0x02) == 0).sum())
     # every slot's intra slice heads a phase-A group; 8 frames -> its 7 P slices join it
     ones = pvvc_lib.Plan(gop, tune=(3, 32, 128, -1, -1, 32)).info()
     assert ones["groups_a"] == default["nintra"] and ones["singles_a"] == 0
     k = ones
-    # trees, coordinates, one per-slice RLGR launch (8-frame groups are below the windowed RLGR's 16), then the
-    # inverse-RAHT launches
-    assert k["kernels"] == 3 + (k["groups_a"] > 0) + (k["singles_a"] > 0) + (k["groups_b"] > 0) + (k["singles_b"] > 0)
+    # trees, one per-slice RLGR launch (8-frame groups are below the windowed RLGR's 16), then the inverse-RAHT
+    # launches
+    assert k["kernels"] == 2 + (k["groups_a"] > 0) + (k["singles_a"] > 0) + (k["groups_b"] > 0) + (k["singles_b"] > 0)
     assert k["clear_bytes"] > 0
 
 
