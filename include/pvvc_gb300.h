@@ -210,13 +210,18 @@ int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const uint8_t* cons
 /* Wall-clock milliseconds of the stages of the calling thread's last
  * pvvc_decode_frames_host (no counterpart in the reference):
  * out[0] parse (with the zstd frame headers), out[1] the batch description and the split into
- * runs, out[2] planning (host) and plan upload, out[3] the wait for the
+ * runs (for a call decoded in parts, only the indices and types: each part's
+ * sizes, motions and offsets are described by its planner, so they count in
+ * out[2]), out[2] planning (host) and plan upload, out[3] the wait for the
  * last device-to-host copies (and, for a call decoded in one piece, its
  * decode), out[4] the wait for the payload packed into pinned memory beside
  * the planning, out[5] workspace growth, out[6] queuing the decode kernels,
  * out[7] queuing the device-to-host copies of each part, out[8..12] the
- * parts' planning stages summed (pvvc_plan_host_times).  Fills min(n, 13)
- * values; zeros before any call. */
+ * parts' planning stages summed (pvvc_plan_host_times), and for a call
+ * decoded in parts the device timeline, in milliseconds after the call's
+ * start on `stream`: out[13 + 3h] part h's payload uploaded, out[14 + 3h]
+ * part h decoded, out[15 + 3h] part h's points copied back (h = 0..2).
+ * Fills min(n, 22) values; zeros before any call. */
 int pvvc_host_stage_times(double* out, int32_t n);
 
 /* ---- zstd payloads on the GPU ----------------------------------------------

@@ -94,9 +94,18 @@ struct SideStream {
         if (mid) cudaEventDestroy(mid);
         if (s) cudaStreamDestroy(s);
     }
-    cudaError_t ensure() {
+    // urgent: the stream gets the device's greatest priority, so that its
+    // CTAs are dispatched ahead of the other streams' (the decode's longest
+    // chain of dependent work runs on it)
+    cudaError_t ensure(bool urgent = false) {
         cudaError_t e = cudaSuccess;
-        if (!s) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (!s) {
+            int least = 0, greatest = 0;
+            if (urgent && cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess)
+                e = cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest);
+            else
+                e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        }
         if (e == cudaSuccess && !fork) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
         if (e == cudaSuccess && !join) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
         if (e == cudaSuccess && !mid) e = cudaEventCreateWithFlags(&mid, cudaEventDisableTiming);
@@ -168,6 +177,13 @@ struct pvvc_plan {
     pvvc::SideStream side2;  // the medium tier's stream
     pvvc::SideStream tree;   // the tree expansion's stream (beside the coefficient clear and RLGR)
     bool upload_pending = false;  // built with deferred copies, not yet queued
+    // the layout of the last full build (slots, types, sizes, shapes): a
+    // build of the same layout refreshes the records only
+    bool cache_valid = false;
+    std::vector<int32_t> key_slot;
+    std::vector<uint8_t> key_type;
+    std::vector<uint32_t> key_size;
+    pvvc_tune key_tune{};
 };
 
 struct pvvc_state {
@@ -188,6 +204,9 @@ struct pvvc_state {
     cudaStream_t zside = nullptr;           // zstd inflation of the parts after the first
     cudaStream_t up = nullptr;              // host-to-device copies of the parts' raw payloads
     cudaEvent_t up_done[kParts] = {};
+    // timing events of the call's device timeline: its start, and per part
+    // the end of its upload, of its decode and of its copy back
+    cudaEvent_t t_start = nullptr, t_up[kParts] = {}, t_dec[kParts] = {}, t_cp[kParts] = {};
     cudaEvent_t zdone[kParts] = {};
 };
 
@@ -200,6 +219,7 @@ int resolve_tune(const pvvc_tune* in, pvvc_tune* out);
 // queues every CUDA call of a host call while others plan).
 int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload, bool defer = false);
 int upload_plan(pvvc_plan* p, cudaStream_t s);
+int copy_plan(pvvc_plan* p, cudaStream_t upload, bool defer);
 // Enqueue one planned decode on `s` (events: optional stage markers).
 int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float* xyz, uint8_t* rgb, float* p24,
                int32_t* status, void* ws, uint64_t ws_bytes, cudaStream_t s, void* const* events);

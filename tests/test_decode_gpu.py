@@ -277,6 +277,35 @@ def test_host_call_decodes_gops_in_one_plan_identically(pvvc_lib, torch, nframes
         assert np.array_equal(x, y)
 
 
+def test_host_call_same_layout_new_content(pvvc_lib, torch):
+    """A call whose frames have the layout of the previous call (slots,
+    types and sizes) reuses the parts' queue structure and refreshes only
+    the per-call fields: new motions and quantisation steps must decode as a
+    fresh state decodes them."""
+    s = pvvc_lib.Synth(pvvc_lib.config("tiny", nframes=12, gof=4, seed=33))
+    frames = s.frames()
+    nidx = max(int(pvvc_lib.parse_frame(b).index.max()) + 1 for b in frames)
+    rng = np.random.default_rng(3)
+    changed = []
+    for b in frames:
+        f = pvvc_lib.parse_frame(b)
+        f.mv = f.mv.copy()
+        f.mv[:, 3] += rng.integers(-5, 6, f.n).astype(np.float32)  # new translations
+        f.mv[:, 0] *= np.float32(1.5)
+        f.qp = np.where(f.qp > 2, f.qp - 1, f.qp + 1).astype(np.uint8)  # new steps, same symbols
+        changed.append(pvvc_lib.write_frame(f))
+    reused = pvvc_lib.Decoder(nslots=3 * nidx, max_leaves=4096)
+    a0 = reused.decode_frames(frames)
+    assert (a0[2] == 0).all()
+    a = reused.decode_frames(changed)
+    fresh = pvvc_lib.Decoder(nslots=3 * nidx, max_leaves=4096)
+    b = fresh.decode_frames(changed)
+    assert (a[2] == 0).all() and (b[2] == 0).all()
+    assert not np.array_equal(a[0], a0[0]) and not np.array_equal(a[1], a0[1])  # the content did change
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+
+
 def test_host_call_pinned_and_pageable_outputs_agree(pvvc_lib, torch):
     """Page-locked and pageable output arrays receive the same bytes, for a
     call of several GoPs decoded in parts and for a single-GoP call, and
