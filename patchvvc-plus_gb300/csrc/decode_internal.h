@@ -197,7 +197,7 @@ struct pvvc_state {
     // part boundaries, as fractions of the slices: a small first part starts
     // the device work (and its outputs' trip to the host) early, while the
     // other parts are still being planned
-    static constexpr double kCutAt[kParts - 1] = {0.1, 0.45};
+    static constexpr double kCutAt[kParts - 1] = {0.1, 0.35};
     pvvc_plan part_plan[kParts - 1];        // the plans of parts 1.. (part 0 uses `plan`)
     cudaStream_t copy = nullptr;            // device-to-host copies that overlap the next part's decode
     cudaEvent_t part_done[kParts] = {};
