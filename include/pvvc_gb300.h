@@ -102,7 +102,7 @@ int pvvc_plan_query(const pvvc_plan* plan, uint64_t* total_points, uint64_t* wor
  * slice into planes cleared beforehand; when no group qualifies, those
  * slices are split into the size tiers below. */
 typedef struct {
-    int32_t group_ctas_per_sm; /* persistent CTAs of the grouped inverse-RAHT kernel per SM: 1..4 (default 4)   */
+    int32_t group_ctas_per_sm; /* persistent CTAs of the grouped inverse-RAHT kernel per SM: 1..4 (default 3)   */
     int32_t min_group;         /* a slot's predictive slices share one warp when at least this many: 1..32 (4) */
     int32_t rlgr_block;        /* threads per CTA of the RLGR kernels: 32, 64, 128 or 256 (default 64); the
                                   windowed form runs rlgr_block / 32 groups per CTA                               */

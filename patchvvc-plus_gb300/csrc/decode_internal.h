@@ -40,7 +40,7 @@ cudaError_t launch_raht_group(const SliceWork* work, const GroupDesc* groups, in
 // default launch shapes: persistent CTAs of the group kernel per SM (its
 // registers allow four), the group threshold, the RLGR block, and
 // the CTAs that decode the longest slices on SMs of their own
-constexpr int kGroupCtasPerSm = 4;
+constexpr int kGroupCtasPerSm = 3;
 constexpr int kMinGroup = 4;
 constexpr int kRlgrBlock = 64;
 constexpr int kRlgrLongCtas = 16;

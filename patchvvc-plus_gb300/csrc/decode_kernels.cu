@@ -1088,10 +1088,11 @@ __device__ __forceinline__ void lane_node(const StateView& st, size_t node, bool
                        ov);
 }
 
-// A warp's staged node records: 32 consecutive nodes of one level.
+// A warp's staged node records: kRowNodes consecutive nodes of one level.
+constexpr int kRowNodes = 32;
 struct NodeRows {
-    uint32_t occ[32], cb[32], mask[32], coff[32];
-    float2 ab[7][32];
+    uint32_t occ[kRowNodes], cb[kRowNodes], mask[kRowNodes], coff[kRowNodes];
+    float2 ab[7][kRowNodes];
 };
 
 // k_raht_group: persistent CTAs; each takes the next group of slices that
@@ -1100,16 +1101,23 @@ struct NodeRows {
 // loads).  The intra slice, when the group has one, is lane 0 and hands its
 // leaf colours to the predictive lanes by shuffle.
 //
-// Levels above the last internal one: the 8 warps split each level's nodes
-// and the CTA synchronises per level.  The level signal lives in the CTA's
-// own scratch region as [node][yuv][lane], so each warp access is one
+// Levels above the last two internal ones: the 8 warps split each level's
+// nodes and the CTA synchronises per level.  The level signal lives in the
+// CTA's own scratch region as [node][yuv][lane], so each warp access is one
 // 128-byte line.
 //
-// Last internal level (most of the nodes): warp w takes a contiguous range
-// of nodes, whose leaves are contiguous too, and stages its finished points
-// in its own shared-memory rows [frame][leaf]; when the next node's leaves
-// would not fit, the warp writes the staged leaves of every frame as
-// contiguous runs and goes on -- no CTA-wide barrier at this level.
+// The last two internal levels (most of the nodes) go without a barrier or
+// a level buffer: warp w takes a contiguous range of last-level nodes, whose
+// leaves are contiguous too, and walks their parents alongside -- each
+// parent's children DCs go to the warp's shared-memory rows [yuv][child]
+// [lane] (a lane reads back only its own column), the first parent found by
+// a 32-way search of the parents' child offsets.  A parent whose children
+// straddle two warps' ranges is transformed by both.  The warp stages its
+// finished points in its own rows [frame][leaf]; when the next node's leaves
+// would not fit, it writes the staged leaves of every frame as contiguous
+// runs and goes on.  Against a level buffer in global memory for the last
+// internal level too, this cut the kernel's DRAM bytes by a quarter.  The
+// kernel needs 80 registers without spills: 3 CTAs of 8 warps per SM.
 constexpr int kGrpWarps = 8;
 constexpr int kWarpLeaves = 16;              // staged leaves per warp (a node adds <= 8)
 constexpr int kStageRow = kWarpLeaves + 1;   // odd row length: the 32 lanes' column stores hit 32 banks
@@ -1132,7 +1140,7 @@ struct GroupStage {
 };
 
 template <bool P24>
-__global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWork* __restrict__ work,
+__global__ void __launch_bounds__(32 * kGrpWarps, 3) k_raht_group(const SliceWork* __restrict__ work,
                                                                const GroupDesc* __restrict__ groups, int ngroups,
                                                                const int32_t* __restrict__ items, StateView st,
                                                                const float* __restrict__ coef,
@@ -1148,6 +1156,7 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
     __shared__ int s_act[32], s_white[32];
     __shared__ float s_mv[32][13];  // each frame's transform rows (odd stride: the lanes' row fills hit 32 banks)
     __shared__ NodeRows s_nodes[kGrpWarps];
+    __shared__ float s_dc[kGrpWarps][3][8][32];  // each warp's current parent: its children's DCs [yuv][child][lane]
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     WarpStage<P24>& ws = sg.w[wid];
     float* const bufA = scratch + (uint64_t)blockIdx.x * scratch_floats;
@@ -1291,7 +1300,7 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
                     gA[64 + lane] = act ? cv[0] : 0.f;
                 }
                 __syncthreads();
-                for (int l = 0; l < H - 2; ++l) {  // internal levels above the last
+                for (int l = 0; l < H - 3; ++l) {  // internal levels above the last two
                     const int a = s_ls[l], b = s_ls[l + 1];
                     for (int j = wid; j < b - a; j += kGrpWarps) {
                         const size_t node = nb + a + j;
@@ -1315,35 +1324,82 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
                     gA = gB;
                     gB = t;
                 }
-                // last internal level: a contiguous node range per warp
-                const int a = s_ls[H - 2], cnt = s_ls[H - 1] - a;
+                // gA: the DCs of level H - 3 (the parents), or for H = 2 the root's
+                const int a = s_ls[H - 2], cnt = s_ls[H - 1] - a;                       // last internal level
+                const int pa = H >= 3 ? s_ls[H - 3] : 0, pcnt = H >= 3 ? s_ls[H - 2] - pa : 1;  // its parents
+                float(&dc)[3][8][32] = s_dc[wid];
+                uint32_t pc0 = 0, pc1 = 0;  // the current parent's children [pc0, pc1) of the last level
+                // parent pj: its children's DCs into dc, compacted (child pc0 + r at row r)
+                auto parent = [&](int pj) {
+                    if (H == 2) {  // the root is the only last-level node: its DC as the one child
+                        dc[0][0][lane] = gA[lane];
+                        dc[1][0][lane] = gA[32 + lane];
+                        dc[2][0][lane] = gA[64 + lane];
+                        pc0 = 0;
+                        pc1 = 1;
+                        return;
+                    }
+                    const size_t node = nb + pa + pj;
+                    const uint32_t byte = __ldg(st.occ + node), cb = __ldg(st.cbase + node);
+                    const float* g3 = gA + (size_t)pj * 96 + lane;
+                    float oy[8], ou[8], ov[8];
+                    lane_node<32>(st, node, act, cy, cu, cv, g3[0], g3[32], g3[64], oy, ou, ov);
+                    uint32_t r = 0;
+#pragma unroll
+                    for (int c = 0; c < 8; ++c) {
+                        if (!(byte & (0x80u >> c))) continue;
+                        dc[0][r][lane] = oy[c];
+                        dc[1][r][lane] = ou[c];
+                        dc[2][r][lane] = ov[c];
+                        ++r;
+                    }
+                    pc0 = cb;
+                    pc1 = cb + r;
+                };
                 // the group's region (every lane's frame shares it) and plane
                 // stride, from lane 0, which always holds a slice
                 const uint64_t g_off = __shfl_sync(0xffffffffu, have ? w.coef_off : 0ull, 0);
                 const uint32_t g_n = __shfl_sync(0xffffffffu, have ? w.n : 0u, 0);
                 const float* const g_coef = coef + g_off;
-                // Node t+1's lines into L1 while node t is transformed: lane
-                // l < 21 takes coefficient line (plane l / 7, coded slot
-                // l % 7), lanes 21-23 the node's three level-signal lines.
-                auto prefetch_node = [&](const NodeRows& r, int t, int jnode) {
+                // Node t+1's coefficient lines into L1 while node t is
+                // transformed: lane l < 21 takes line (plane l / 7, coded slot
+                // l % 7).
+                auto prefetch_node = [&](const NodeRows& r, int t) {
                     const uint32_t nc = __popc(r.mask[t] & 0xFEu);
-                    const float* line = nullptr;
                     if (lane < 21) {
                         const uint32_t k = (uint32_t)lane % 7u, pl = (uint32_t)lane / 7u;
-                        if (k < nc) line = g_coef + ((size_t)pl * g_n + r.coff[t] + k) * 32;
-                    } else if (lane < 24) {
-                        line = gA + (size_t)jnode * 96 + (lane - 21) * 32;
+                        if (k < nc) {
+                            const float* line = g_coef + ((size_t)pl * g_n + r.coff[t] + k) * 32;
+                            asm volatile("prefetch.global.L1 [%0];" ::"l"(line));
+                        }
                     }
-                    if (line) asm volatile("prefetch.global.L1 [%0];" ::"l"(line));
                 };
                 const int per = (cnt + kGrpWarps - 1) / kGrpWarps;
                 const int j0 = min(cnt, wid * per), j1 = min(cnt, j0 + per);
                 uint32_t base = 0, staged = 0;
-                if (j0 < j1) base = __ldg(st.cbase + nb + a + j0);
+                int pj = 0;
+                if (j0 < j1) {
+                    base = __ldg(st.cbase + nb + a + j0);
+                    if (H >= 3) {
+                        // the parent of node j0: the last parent whose first
+                        // child is at or below j0 (child offsets ascend)
+                        int lo = 0, hi = pcnt;
+                        while (hi - lo > 1) {
+                            const int step = (hi - lo + 31) >> 5;
+                            const int idx = lo + lane * step;
+                            const bool le = idx < hi && (int)__ldg(st.cbase + nb + pa + idx) <= j0;
+                            const uint32_t bal = __ballot_sync(0xffffffffu, le);  // lanes 0.. k hold; lane 0 always
+                            lo += (bal ? 31 - __clz(bal) : 0) * step;
+                            hi = min(hi, lo + step);
+                        }
+                        pj = lo;
+                    }
+                    parent(pj);
+                }
                 NodeRows& nr = s_nodes[wid];
-                for (int jb = j0; jb < j1; jb += 32) {
-                    // the next 32 node records, one node per lane, all loads in flight at once
-                    const int nn = min(32, j1 - jb);
+                for (int jb = j0; jb < j1; jb += kRowNodes) {
+                    // the next node records, one node per lane, all loads in flight at once
+                    const int nn = min(kRowNodes, j1 - jb);
                     __syncwarp();
                     if (lane < nn) {
                         const size_t node = nb + a + jb + lane;
@@ -1356,9 +1412,11 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
                         for (int i = 0; i < 7; ++i) nr.ab[i][lane] = __ldg(ab + i);
                     }
                     __syncwarp();
-                    if (nn > 0) prefetch_node(nr, 0, jb);
+                    if (nn > 0) prefetch_node(nr, 0);
                     for (int t = 0; t < nn; ++t) {
-                        if (t + 1 < nn) prefetch_node(nr, t + 1, jb + t + 1);
+                        if (t + 1 < nn) prefetch_node(nr, t + 1);
+                        const uint32_t jc = (uint32_t)(jb + t);
+                        while (jc >= pc1 && pj + 1 < pcnt) parent(++pj);  // the next parent with children
                         const uint32_t byte = nr.occ[t], cb = nr.cb[t];
                         const uint32_t k = __popc(byte);
                         if (staged + k > (uint32_t)kWarpLeaves) {
@@ -1366,10 +1424,10 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 4) k_raht_group(const SliceWor
                             base += staged;
                             staged = 0;
                         }
-                        const float* g3 = gA + (size_t)(jb + t) * 96 + lane;
+                        const uint32_t rc = jc - pc0 < 8u ? jc - pc0 : 0u;  // its row (in range for a well-formed tree)
                         float oy[8], ou[8], ov[8];
-                        lane_node_md<32, 32>(nr.mask[t], nr.coff[t], &nr.ab[0][t], act, cy, cu, cv, g3[0], g3[32], g3[64],
-                                             oy, ou, ov);
+                        lane_node_md<32, kRowNodes>(nr.mask[t], nr.coff[t], &nr.ab[0][t], act, cy, cu, cv, dc[0][rc][lane],
+                                                    dc[1][rc][lane], dc[2][rc][lane], oy, ou, ov);
                         uint32_t r = 0;
 #pragma unroll
                         for (int c = 0; c < 8; ++c) {

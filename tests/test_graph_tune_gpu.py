@@ -42,7 +42,7 @@ def test_every_launch_shape_decodes_identically(pvvc_lib, torch, gop):
 
 def test_plan_info_counts(pvvc_lib, gop):
     default = pvvc_lib.Plan(gop).info()
-    assert default["tune"] == {"group_ctas_per_sm": 4, "min_group": 4, "rlgr_block": 64, "rlgr_long_ctas": 16,
+    assert default["tune"] == {"group_ctas_per_sm": 3, "min_group": 4, "rlgr_block": 64, "rlgr_long_ctas": 16,
                                "rlgr_mid_pct": 50, "rlgr_long_lanes": 32}
     assert default["nslices"] == gop.nslices
     assert default["nintra"] == int(((gop.type & 0x02) == 0).sum())
