@@ -252,6 +252,62 @@ def test_rlgr_golden_vectors_through_gpu_decode(pvvc_lib, oracle, torch):
     assert rgb_matches(rgb, orgb, oyuv).all()
 
 
+
+def _large_value_frames(pvvc, nframes):
+    """Eight patches over `nframes` frames (frame 0 intra), colours and
+    residuals uniform in +-scale: at scales far above 255 the dequantised
+    coefficients reach far beyond what 8-bit colours give -- at 5e9 with
+    step 255 beyond 32 bits, through RLGR's general path (symbols above
+    2^23 and raw 32-bit escapes); two patches keep ordinary scales."""
+    rng = np.random.default_rng(11)
+    specs = [(900, 4.0e4, 2), (900, 5.0e9, 255), (600, 4.0e4, 3), (600, 2.0e5, 1),  # (voxels, scale, step)
+             (300, 100.0, 8), (300, 4.0e4, 2), (200, 60.0, 4), (200, 3.0e4, 1)]
+    patches = []
+    for n, scale, qp in specs:
+        pos = rng.choice(64 ** 3, n, replace=False)
+        xyz = np.stack([pos // 4096, (pos // 64) % 64, pos % 64], 1).astype(np.float32)
+        yuv = rng.uniform(-scale, scale, (nframes, n, 3)).astype(np.float32)
+        geo, nl, cols = pvvc.encode_patch_gop(xyz, yuv, [qp] * nframes)
+        assert nl == n
+        patches.append((geo, nl, cols, qp))
+    m = len(patches)
+    eye = np.tile(np.eye(4, dtype=np.float32).reshape(16), (m, 1))
+    return [pvvc.write_frame(pvvc.Frame(f, np.arange(m, dtype=np.int32), np.full(m, 1 if f == 0 else 3, np.uint8),
+                                        np.array([q[1] for q in patches], np.uint32),
+                                        np.array([q[3] for q in patches], np.uint8), eye,
+                                        [q[0] if f == 0 else b"" for q in patches], [q[2][f] for q in patches]))
+            for f in range(nframes)]
+
+
+@pytest.mark.parametrize("nframes,tune", [(20, None),                         # long tier + windowed RLGR
+                                          (20, (3, 4, 64, -1, -1, 32)),       # every group windowed
+                                          (8, None),                          # groups below the window size
+                                          (3, None)])                         # single slices
+def test_large_coefficients_bit_exact(pvvc_lib, oracle, torch, nframes, tune):
+    """Very large coefficients decode exactly through every RLGR form and
+    both inverse transforms: geometry bit for bit, the unrounded points24
+    colours bit for bit against the oracle's YUV, the uint8 colours by the
+    reference's cast rule."""
+    frames = _large_value_frames(pvvc_lib, nframes)
+    parsed = [pvvc_lib.parse_frame(b) for b in frames]
+    batch = pvvc_lib.pack_frames(parsed)
+    dec = pvvc_lib.Decoder(nslots=16, max_leaves=4096)
+    xyz, rgb, st, p24 = decode_batch(torch, pvvc_lib, dec, batch, points24=True, tune=tune)
+    assert (st == 0).all(), np.unique(st)
+    ref = oracle_decode(oracle, pvvc_lib, frames, 16)
+    f = np.float32
+    for fi, (ox, orgb, ost, yuv) in enumerate(ref):
+        a, b = batch.frame_first_point[fi], batch.frame_first_point[fi + 1]
+        assert (ost == 0).all()
+        assert np.array_equal(xyz[a:b].view(np.uint32), ox.view(np.uint32)), fi
+        y, u, v = yuv[:, 0], yuv[:, 1], yuv[:, 2]
+        want = np.stack([(y + f(1.402) * (v - f(128))) / f(255),
+                         ((y - f(0.3441) * (u - f(128))) - f(0.7141) * (v - f(128))) / f(255),
+                         (y + f(1.772) * (u - f(128))) / f(255)], 1).astype(np.float32)
+        assert np.array_equal(p24[a:b, 3:].view(np.uint32), want.view(np.uint32)), fi
+        assert rgb_matches(rgb[a:b], orgb, yuv).all(), fi
+    assert np.abs(ref[-1][3]).max() > 1e9  # the large scales did reach the decoder
+
 @pytest.mark.parametrize("nframes", [12, 28])
 def test_host_call_decodes_gops_in_one_plan_identically(pvvc_lib, torch, nframes):
     """pvvc_decode_frames_host with slots for one region per GoP decodes all
