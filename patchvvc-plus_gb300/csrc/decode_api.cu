@@ -53,8 +53,12 @@ namespace {
 // every item is done and no worker still holds the job.
 class HostPool {
   public:
+    // Workers: the host threads but four, which the host call's own threads
+    // (the caller, the packer and two planners) use: with one worker per
+    // core, a worker preempted in the middle of a loop held up the loop's
+    // caller for a scheduler time slice.
     static HostPool& get() {
-        static HostPool p((int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency())));
+        static HostPool p(std::max(1, (int)std::min<unsigned>(16, std::max(1u, std::thread::hardware_concurrency())) - 4));
         return p;
     }
     template <class F>
@@ -165,7 +169,10 @@ void sort_by_size_slot(const uint32_t* size, const int32_t* slot, std::vector<in
 }  // namespace
 
 // The queue to the device: synchronously (upload == nullptr), or from
-// pinned mirrors on `upload`, or (defer) left for upload_plan.
+// pinned mirrors on `upload`, or (defer, whatever `upload` is) left for
+// upload_plan on the stream the caller gives it.  (Deferred copies must not
+// fall back to synchronous ones for the default stream: a planner thread's
+// cudaMemcpy waited for the decode already queued there, 3 ms a part.)
 int copy_plan(pvvc_plan* p, cudaStream_t upload, bool defer) {
     const size_t n = (size_t)p->nslices;
     if (n == 0) return PVVC_OK;
@@ -176,21 +183,43 @@ int copy_plan(pvvc_plan* p, cudaStream_t upload, bool defer) {
         return PVVC_ERR_NOMEM;
     auto put = [&](DevBuf& d, HostBuf& h, const void* src, size_t bytes) -> bool {
         if (!bytes) return true;
-        if (!upload) return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+        if (!upload && !defer) return cudaMemcpy(d.p, src, bytes, cudaMemcpyHostToDevice) == cudaSuccess;
         if (src != h.p) {
             if (h.ensure(bytes) != cudaSuccess) return false;
             std::memcpy(h.p, src, bytes);
         }
         return defer || cudaMemcpyAsync(d.p, h.p, bytes, cudaMemcpyHostToDevice, upload) == cudaSuccess;
     };
+    p->device_records = false;
     if (!put(p->d_work, p->h_work, p->h_work.p, wb) || !put(p->d_order, p->h_order, p->order.data(), ob) ||
         !put(p->d_groups, p->h_groups, p->groups.data(), gb) || !put(p->d_idx, p->h_idx, p->idx.data(), ib))
         return PVVC_ERR_CUDA;
-    p->upload_pending = upload && defer;  // the copies are queued later by upload_plan
+    p->upload_pending = defer;  // the copies are queued later by upload_plan
+    p->device_records = !defer;
     return PVVC_OK;
 }
 
 int upload_plan(pvvc_plan* p, cudaStream_t s) {
+    if (p->refresh_pending) {
+        // the call's per-slice fields up, then gathered into the records
+        p->refresh_pending = false;
+        const pvvc_batch_desc& d = p->refresh_src;
+        const size_t n = (size_t)d.nslices;
+        const size_t a8 = align_up(8 * n, 256), a4 = align_up(4 * n, 256), a1 = align_up(n, 256);
+        const size_t total = 3 * a8 + 2 * a4 + a1 + 64 * n;
+        if (p->d_call.ensure(total) != cudaSuccess) return PVVC_ERR_NOMEM;
+        uint8_t* b = static_cast<uint8_t*>(p->d_call.p);
+        uint8_t* at[7] = {b, b + a8, b + 2 * a8, b + 3 * a8, b + 3 * a8 + a4, b + 3 * a8 + 2 * a4, b + 3 * a8 + 2 * a4 + a1};
+        const void* src[7] = {d.col_off, d.geo_off, d.out_off, d.col_size, d.geo_size, d.qp, d.mv};
+        const size_t bytes[7] = {8 * n, 8 * n, 8 * n, 4 * n, 4 * n, n, 64 * n};
+        for (int k = 0; k < 7; ++k)
+            if (cudaMemcpyAsync(at[k], src[k], bytes[k], cudaMemcpyHostToDevice, s) != cudaSuccess) return PVVC_ERR_CUDA;
+        const CallFields f{reinterpret_cast<const uint64_t*>(at[0]), reinterpret_cast<const uint64_t*>(at[1]),
+                           reinterpret_cast<const uint64_t*>(at[2]), reinterpret_cast<const uint32_t*>(at[3]),
+                           reinterpret_cast<const uint32_t*>(at[4]), at[5], reinterpret_cast<const float*>(at[6])};
+        if (launch_refresh(static_cast<SliceWork*>(p->d_work.p), (int)n, f, s) != cudaSuccess) return PVVC_ERR_CUDA;
+        return PVVC_OK;
+    }
     if (!p->upload_pending) return PVVC_OK;
     p->upload_pending = false;
     const size_t n = (size_t)p->nslices;
@@ -202,13 +231,13 @@ int upload_plan(pvvc_plan* p, cudaStream_t s) {
     if (!put(p->d_work, p->h_work, wb) || !put(p->d_order, p->h_order, ob) || !put(p->d_groups, p->h_groups, gb) ||
         !put(p->d_idx, p->h_idx, ib))
         return PVVC_ERR_CUDA;
+    p->device_records = true;
     return PVVC_OK;
 }
 
 int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cudaStream_t upload, bool defer) {
     if (!d || d->nslices < 0) return PVVC_ERR_ARG;
     if (resolve_tune(tune, &p->tune)) return PVVC_ERR_ARG;
-    if (prepare_kernels() != cudaSuccess) return PVVC_ERR_CUDA;
     auto t_last = std::chrono::steady_clock::now();
     auto lap = [&](int k) {  // host milliseconds of the plan's stages (pvvc_plan_host_times)
         const auto now = std::chrono::steady_clock::now();
@@ -219,6 +248,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     if (n > 0 && (!d->slot || !d->type || !d->size || !d->qp || !d->mv || !d->geo_off || !d->geo_size || !d->col_off ||
                   !d->col_size || !d->out_off))
         return PVVC_ERR_ARG;
+    p->refresh_pending = false;
     // The queue's structure -- order, tiers, groups, coefficient regions,
     // workspace -- depends on the slices' slots, types and sizes (and the
     // launch shapes) only.  When those equal the last build's (the same
@@ -227,6 +257,19 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     if (p->cache_valid && n > 0 && n == p->nslices && std::memcmp(&p->key_tune, &p->tune, sizeof(pvvc_tune)) == 0 &&
         std::memcmp(p->key_slot.data(), d->slot, 4ull * n) == 0 && std::memcmp(p->key_type.data(), d->type, n) == 0 &&
         std::memcmp(p->key_size.data(), d->size, 4ull * n) == 0) {
+        if (defer && p->device_records) {
+            // a host call's plan whose records are on the device: their
+            // per-call fields are gathered there by k_refresh (upload_plan),
+            // from the call's description arrays in their own order
+            uint64_t m = 0;
+            for (int i = 0; i < n; ++i) m = std::max<uint64_t>(m, d->out_off[i] + d->size[i]);
+            p->total_points = m;
+            p->refresh_src = *d;
+            p->refresh_pending = true;
+            lap(0);
+            for (int k = 1; k < 5; ++k) p->host_ms[k] = 0;
+            return PVVC_OK;
+        }
         SliceWork* const W = static_cast<SliceWork*>(p->h_work.p);
         constexpr int kChunk = 4096;
         const int nch = (n + kChunk - 1) / kChunk;
@@ -257,6 +300,10 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         return rc;
     }
     p->cache_valid = false;
+    // (after the reuse path: that one makes no CUDA call, so a planner thread
+    // of the host call -- a new thread each call -- pays no first-call setup
+    // of the CUDA runtime, which took milliseconds)
+    if (prepare_kernels() != cudaSuccess) return PVVC_ERR_CUDA;
     std::vector<int32_t> intra, pred;
     int32_t max_slot = -1;
     for (int i = 0; i < n; ++i) {
@@ -1165,9 +1212,11 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
         nsl += (int32_t)frames[f].count();
     }
     ffirst[nframes] = nsl;
-    // the call's description arrays, carved from one grow-only host buffer
-    // that the state keeps (a fresh allocation of this size would come from
-    // new pages each call, and their first-touch faults cost milliseconds)
+    // the call's description arrays, carved from one grow-only page-locked
+    // buffer that the state keeps (a fresh allocation of this size would come
+    // from new pages each call, and their first-touch faults cost
+    // milliseconds; page-locked, a reused plan's per-call fields go to the
+    // device straight from here)
     int32_t *slot, *index;
     uint8_t *type, *qp;
     uint32_t *size, *gsz, *csz;
@@ -1181,8 +1230,8 @@ extern "C" int pvvc_decode_frames_host(pvvc_state* st, int32_t nframes, const ui
             at[i] = o;
             o = align_up(o + bytes[i], 64);
         }
-        unsigned char* b = st->host_desc.get(o);
-        if (!b) return PVVC_ERR_NOMEM;
+        if (st->host_desc.ensure(o) != cudaSuccess) return PVVC_ERR_NOMEM;
+        unsigned char* b = static_cast<unsigned char*>(st->host_desc.p);
         slot = reinterpret_cast<int32_t*>(b + at[0]);
         index = reinterpret_cast<int32_t*>(b + at[1]);
         type = b + at[2];

@@ -29,6 +29,7 @@ cudaError_t launch_rlgr_long(const SliceWork* work, const int32_t* order, int ns
 cudaError_t launch_rlgr_win(const SliceWork* work, const GroupDesc* groups, int ngroups, const int32_t* items,
                             const uint8_t* payload, float* coef, int32_t* rstatus, int warps, cudaStream_t s);
 cudaError_t prepare_kernels();
+cudaError_t launch_refresh(SliceWork* work, int n, const CallFields& f, cudaStream_t s);
 cudaError_t launch_raht_slice(const SliceWork* work, const int32_t* list, int count, const StateView& st, const float* coef,
                               float* fallback, const int32_t* tstatus, const int32_t* rstatus, int32_t* fstatus, float* xyz,
                               uint8_t* rgb, float* p24, int32_t* status, int wcap, cudaStream_t s);
@@ -112,17 +113,6 @@ struct SideStream {
         return e;
     }
 };
-struct GrowBuf {  // pageable host memory, grow-only (its pages stay mapped between uses)
-    std::unique_ptr<unsigned char[]> p;
-    size_t cap = 0;
-    unsigned char* get(size_t n) {
-        if (n > cap) {
-            p.reset(new (std::nothrow) unsigned char[n]);
-            cap = p ? n : 0;
-        }
-        return p.get();
-    }
-};
 struct HostBuf {  // pinned, grow-only
     void* p = nullptr;
     size_t cap = 0;
@@ -177,6 +167,14 @@ struct pvvc_plan {
     pvvc::SideStream side2;  // the medium tier's stream
     pvvc::SideStream tree;   // the tree expansion's stream (beside the coefficient clear and RLGR)
     bool upload_pending = false;  // built with deferred copies, not yet queued
+    // d_work holds this plan's records (their upload is queued): a rebuild of
+    // the same layout for a host call may refresh them on the device instead
+    bool device_records = false;
+    // a pending device refresh: the host call's description arrays (page-
+    // locked, alive until the call ends) to upload, then k_refresh
+    bool refresh_pending = false;
+    pvvc_batch_desc refresh_src{};
+    pvvc::DevBuf d_call;  // their device copies
     // the layout of the last full build (slots, types, sizes, shapes): a
     // build of the same layout refreshes the records only
     bool cache_valid = false;
@@ -191,13 +189,13 @@ struct pvvc_state {
     // buffers of the end-to-end host call, kept across calls
     pvvc::DevBuf payload, xyz, rgb, ws, status;
     pvvc::HostBuf h_payload;
-    pvvc::GrowBuf host_desc;  // the host call's description arrays
+    pvvc::HostBuf host_desc;  // the host call's description arrays (page-locked)
     pvvc_plan plan;
     static constexpr int kParts = 3;        // a multi-GoP call is decoded in up to this many parts
     // part boundaries, as fractions of the slices: a small first part starts
     // the device work (and its outputs' trip to the host) early, while the
     // other parts are still being planned
-    static constexpr double kCutAt[kParts - 1] = {0.1, 0.35};
+    static constexpr double kCutAt[kParts - 1] = {0.15, 0.4};
     pvvc_plan part_plan[kParts - 1];        // the plans of parts 1.. (part 0 uses `plan`)
     cudaStream_t copy = nullptr;            // device-to-host copies that overlap the next part's decode
     cudaEvent_t part_done[kParts] = {};

@@ -1446,6 +1446,24 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 3) k_raht_group(const SliceWor
 }
 
 // ---------------------------------------------------------------------------
+// k_refresh: the per-call fields of a reused plan's records, gathered from
+// the call's description arrays by each record's caller index.
+__global__ void k_refresh(SliceWork* __restrict__ work, int n, CallFields f) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    SliceWork& w = work[q];
+    const int i = w.orig;
+    w.col_off = f.col_off[i];
+    w.geo_off = f.geo_off[i];
+    w.out_off = f.out_off[i];
+    w.csz = f.csz[i];
+    w.gsz = f.gsz[i];
+    w.qp = f.qp[i];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) w.mv[k] = f.mv[16ull * i + k];
+}
+
+// ---------------------------------------------------------------------------
 // launchers (host)
 constexpr int kTreeThreads = 256;
 constexpr int kRahtThreads = 128;
@@ -1497,6 +1515,12 @@ cudaError_t launch_tree(const SliceWork* work, int nintra, const uint8_t* payloa
 
 // smem: dynamic shared memory reserved per CTA (unused by the kernel; it
 // limits which CTAs share an SM, see kRlgrLongSmem)
+cudaError_t launch_refresh(SliceWork* work, int n, const CallFields& f, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_refresh<<<(n + 255) / 256, 256, 0, s>>>(work, n, f);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_rlgr(const SliceWork* work, const int32_t* order, int nslices, const uint8_t* payload, float* coef,
                         int32_t* rstatus, int block, int smem, cudaStream_t s) {
     if (nslices <= 0) return cudaSuccess;

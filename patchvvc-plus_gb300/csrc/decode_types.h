@@ -43,6 +43,19 @@ struct SliceWork {
     float mv[12];       // first three rows of the row-major 4x4
 };
 
+// The per-call fields of the records, in the caller's slice order (device
+// copies of a host call's description arrays): a plan reused for the same
+// layout takes them from here on the device (k_refresh).
+struct CallFields {
+    const uint64_t* col_off;
+    const uint64_t* geo_off;
+    const uint64_t* out_off;
+    const uint32_t* csz;
+    const uint32_t* gsz;
+    const uint8_t* qp;
+    const float* mv;  // 16 per slice (row-major 4x4)
+};
+
 // Per-slot header of a decoded tree (device).
 struct SlotInfo {
     int32_t valid;          // an intra slice populated the slot

@@ -362,6 +362,50 @@ def test_host_call_same_layout_new_content(pvvc_lib, torch):
         assert np.array_equal(x, y)
 
 
+
+def _gop_frames(pvvc, rng_colour, ngops=3, gof=4):
+    """ngops GoPs of gof frames over six patches at fixed positions; the
+    colours (and so every colour payload's size) come from rng_colour."""
+    pos_rng = np.random.default_rng(5)
+    sizes = [700, 500, 300, 200, 120, 60]
+    xyzs = []
+    for n in sizes:
+        pos = pos_rng.choice(32 ** 3, n, replace=False)
+        xyzs.append(np.stack([pos // 1024, (pos // 32) % 32, pos % 32], 1).astype(np.float32))
+    m = len(sizes)
+    frames = []
+    for g in range(ngops):
+        enc = [pvvc.encode_patch_gop(x, np.concatenate([rng_colour.uniform(0, 255, (1, len(x), 3)),
+                                                        rng_colour.uniform(-20, 20, (gof - 1, len(x), 3))]).astype(np.float32),
+                                     [8] * gof) for x in xyzs]
+        for f in range(gof):
+            frames.append(pvvc.write_frame(pvvc.Frame(
+                g * gof + f, np.arange(m, dtype=np.int32), np.full(m, 1 if f == 0 else 3, np.uint8),
+                np.array([e[1] for e in enc], np.uint32), np.full(m, 8, np.uint8),
+                np.tile(np.eye(4, dtype=np.float32).reshape(16), (m, 1)),
+                [e[0] if f == 0 else b"" for e in enc], [e[2][f] for e in enc])))
+    return frames
+
+
+def test_host_call_same_layout_new_payloads(pvvc_lib, torch):
+    """A second call with the previous call's layout (slots, types, sizes)
+    but other colours -- so other payload sizes and offsets -- reuses the
+    parts' plans and refreshes their records' per-call fields on the device:
+    it must decode as a fresh state does."""
+    a = _gop_frames(pvvc_lib, np.random.default_rng(1))
+    b = _gop_frames(pvvc_lib, np.random.default_rng(2))
+    assert [len(x) for x in a] != [len(x) for x in b]  # the payloads moved
+    reused = pvvc_lib.Decoder(nslots=64, max_leaves=4096)
+    ra = reused.decode_frames(a)
+    rb = reused.decode_frames(b)
+    rb2 = reused.decode_frames(b)  # and once more, now from the refreshed records
+    fresh = pvvc_lib.Decoder(nslots=64, max_leaves=4096)
+    fb = fresh.decode_frames(b)
+    assert (ra[2] == 0).all() and (rb[2] == 0).all() and (fb[2] == 0).all()
+    assert not np.array_equal(ra[1], rb[1])
+    for x, y, z in zip(rb, fb, rb2):
+        assert np.array_equal(x, y) and np.array_equal(x, z)
+
 def test_host_call_pinned_and_pageable_outputs_agree(pvvc_lib, torch):
     """Page-locked and pageable output arrays receive the same bytes, for a
     call of several GoPs decoded in parts and for a single-GoP call, and
