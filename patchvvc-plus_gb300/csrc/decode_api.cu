@@ -497,8 +497,11 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
                 p->ngroups_a_mid = p->tune.rlgr_mid_pct > 0
                                        ? (int32_t)((int64_t)(nw - p->ngroups_a_long) * p->tune.rlgr_mid_pct / 100)
                                        : 0;
+                p->ngroups_a_mid2 = kMidSplit > 1 && p->ngroups_a_mid >= kMidSplitMin ? p->ngroups_a_mid / 2 : 0;
+                p->ngroups_a_mid -= p->ngroups_a_mid2;
                 if (p->ngroups_a_long > 0 && p->side.ensure(true) != cudaSuccess) return PVVC_ERR_CUDA;
                 if (p->ngroups_a_mid > 0 && p->side2.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
+                if (p->ngroups_a_mid2 > 0 && p->side3.ensure() != cudaSuccess) return PVVC_ERR_CUDA;
                 ga = gw;
                 ga.insert(ga.end(), gr.begin(), gr.end());
                 // RLGR order: the window groups' slices in group order (sizes
@@ -538,6 +541,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
                 }
                 p->ngroups_a_long = (int32_t)gl.size();
                 p->ngroups_a_mid = (int32_t)gm.size();
+                p->ngroups_a_mid2 = 0;
                 ga = gl;
                 ga.insert(ga.end(), gm.begin(), gm.end());
                 ga.insert(ga.end(), gs.begin(), gs.end());
@@ -621,8 +625,11 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         p->grp_ctas_mid = p->ngroups_a_mid > 0 ? std::min<int32_t>(p->ngroups_a_mid, p->grp_ctas) : 0;
         p->ws_grp_mid = off;
         off = align_up(off + 4ull * p->grp_floats * p->grp_ctas_mid, 256);
+        p->grp_ctas_mid2 = p->ngroups_a_mid2 > 0 ? std::min<int32_t>(p->ngroups_a_mid2, p->grp_ctas) : 0;
+        p->ws_grp_mid2 = off;
+        off = align_up(off + 4ull * p->grp_floats * p->grp_ctas_mid2, 256);
         p->ws_counter = off;
-        off = align_up(off + 16, 256);
+        off = align_up(off + 32, 256);
     }
     p->ws_bytes = std::max<uint64_t>(off, 256);
     lap(3);  // workspace layout
@@ -674,7 +681,7 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
         return PVVC_ERR_CUDA;
     }
     float* gsc = reinterpret_cast<float*>(w + p->ws_grp);
-    int* cnt = reinterpret_cast<int*>(w + p->ws_counter);  // queue counters: A long, B, A short, A medium
+    int* cnt = reinterpret_cast<int*>(w + p->ws_counter);  // queue counters: A long, B, A short, A medium, A medium 2
     const GroupDesc* dg = static_cast<const GroupDesc*>(p->d_groups.p);
     const int32_t* di = static_cast<const int32_t*>(p->d_idx.p);
     auto raht_groups = [&](int first, int count, int* counter, float* scratch, int ctas, cudaStream_t on) {
@@ -697,7 +704,8 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
         // decoded and the trees are built.
         const SideStream& L = p->side;
         const SideStream& M = p->side2;
-        const int nl = p->ngroups_a_long, nm = p->ngroups_a_mid, nw = p->nwin;
+        const SideStream& M2 = p->side3;
+        const int nl = p->ngroups_a_long, nm = p->ngroups_a_mid, nm2 = p->ngroups_a_mid2, nw = p->nwin;
         const int nrest = p->nslices - p->nwin_slices;
         const int wwarps = std::max(1, p->tune.rlgr_block / 32);
         if (nl > 0 && (!clear(0, p->coef_long_floats) || !fork(L) ||
@@ -707,7 +715,11 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
         if (nm > 0 &&
             (!fork(M) || launch_rlgr_win(dw, dg + nl, nm, di, payload, coef, rs, wwarps, M.s) != cudaSuccess))
             return PVVC_ERR_CUDA;
-        if (launch_rlgr_win(dw, dg + nl + nm, nw - nl - nm, di, payload, coef, rs, wwarps, s) != cudaSuccess)
+        if (nm2 > 0 &&
+            (!fork(M2) || launch_rlgr_win(dw, dg + nl + nm, nm2, di, payload, coef, rs, wwarps, M2.s) != cudaSuccess))
+            return PVVC_ERR_CUDA;
+        const int ns0 = nl + nm + nm2;  // the short tier's first group
+        if (launch_rlgr_win(dw, dg + ns0, nw - ns0, di, payload, coef, rs, wwarps, s) != cudaSuccess)
             return PVVC_ERR_CUDA;
         if (nrest > 0 && (!clear(p->coef_win_floats, p->coef_floats) ||
                           launch_rlgr(dw, ord + p->nwin_slices, nrest, payload, coef, rs, p->tune.rlgr_block, kRlgrShortSmem,
@@ -717,6 +729,7 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
             // stage markers: every tier decoded, then every group
             if ((nl > 0 && (cudaEventRecord(L.join, L.s) != cudaSuccess || cudaStreamWaitEvent(s, L.join, 0) != cudaSuccess)) ||
                 (nm > 0 && (cudaEventRecord(M.join, M.s) != cudaSuccess || cudaStreamWaitEvent(s, M.join, 0) != cudaSuccess)) ||
+                (nm2 > 0 && (cudaEventRecord(M2.join, M2.s) != cudaSuccess || cudaStreamWaitEvent(s, M2.join, 0) != cudaSuccess)) ||
                 !mark(2) || !raht_groups(0, p->ngroups_a, cnt, gsc, p->grp_ctas, s))
                 return PVVC_ERR_CUDA;
         } else {
@@ -729,10 +742,16 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
                                         M.s) ||
                            cudaEventRecord(M.join, M.s) != cudaSuccess))
                 return PVVC_ERR_CUDA;
+            if (nm2 > 0 && ((tree_aside && cudaStreamWaitEvent(M2.s, p->tree.mid, 0) != cudaSuccess) ||
+                            !raht_groups(nl + nm, nm2, cnt + 4, reinterpret_cast<float*>(w + p->ws_grp_mid2),
+                                         p->grp_ctas_mid2, M2.s) ||
+                            cudaEventRecord(M2.join, M2.s) != cudaSuccess))
+                return PVVC_ERR_CUDA;
             if ((tree_aside && cudaStreamWaitEvent(s, p->tree.mid, 0) != cudaSuccess) ||
-                !raht_groups(nl + nm, p->ngroups_a - nl - nm, cnt + 2, gsc, p->grp_ctas, s) ||
+                !raht_groups(ns0, p->ngroups_a - ns0, cnt + 2, gsc, p->grp_ctas, s) ||
                 (nl > 0 && cudaStreamWaitEvent(s, L.join, 0) != cudaSuccess) ||
-                (nm > 0 && cudaStreamWaitEvent(s, M.join, 0) != cudaSuccess))
+                (nm > 0 && cudaStreamWaitEvent(s, M.join, 0) != cudaSuccess) ||
+                (nm2 > 0 && cudaStreamWaitEvent(s, M2.join, 0) != cudaSuccess))
                 return PVVC_ERR_CUDA;
         }
     } else if (p->nlong == 0) {
@@ -918,10 +937,12 @@ extern "C" int pvvc_plan_info_get(const pvvc_plan* p, pvvc_plan_info* info) {
             ? 4ull * p->coef_long_floats + (p->nslices > p->nwin_slices ? 4ull * (p->coef_floats - p->coef_win_floats) : 0ull)
             : 4ull * p->coef_floats;
     if (p->nslices > 0 && p->nwin > 0)
-        info->kernels = (p->nintra > 0) + (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
-                        (p->nwin > p->ngroups_a_long + p->ngroups_a_mid) + (p->nslices > p->nwin_slices) +
-                        (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
-                        (p->ngroups_a > p->ngroups_a_long + p->ngroups_a_mid) + (p->nlist_a > 0) + (p->ngroups_b > 0) +
+        info->kernels = (p->nintra > 0) + (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) + (p->ngroups_a_mid2 > 0) +
+                        (p->nwin > p->ngroups_a_long + p->ngroups_a_mid + p->ngroups_a_mid2) +
+                        (p->nslices > p->nwin_slices) + (p->ngroups_a_long > 0) + (p->ngroups_a_mid > 0) +
+                        (p->ngroups_a_mid2 > 0) +
+                        (p->ngroups_a > p->ngroups_a_long + p->ngroups_a_mid + p->ngroups_a_mid2) + (p->nlist_a > 0) +
+                        (p->ngroups_b > 0) +
                         (p->nlist_b > 0);
     else if (p->nslices > 0)
         info->kernels = (p->nintra > 0) + 1 + (p->nlong > 0) + (p->nmid > 0) +

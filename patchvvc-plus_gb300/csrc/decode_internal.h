@@ -47,6 +47,10 @@ constexpr int kRlgrBlock = 64;
 constexpr int kRlgrLongCtas = 16;
 constexpr int kRlgrMidPct = 50;
 constexpr int kRlgrLongLanes = 32;
+// window mode: the medium tier splits in kMidSplit sub-tiers (1 or 2) when it
+// has at least kMidSplitMin groups
+constexpr int kMidSplit = 2;
+constexpr int kMidSplitMin = 64;
 
 // the SM count (queried once)
 inline int sm_count() {
@@ -140,6 +144,8 @@ struct pvvc_plan {
     uint64_t ws_grp = 0, ws_counter = 0, grp_floats = 0;  // group-kernel level buffers, queue counters
     int32_t grp_ctas = 0, grp_ctas_long = 0, grp_ctas_mid = 0;
     uint64_t ws_grp_long = 0, ws_grp_mid = 0;  // level buffers of the long and medium groups' launches
+    int32_t grp_ctas_mid2 = 0;
+    uint64_t ws_grp_mid2 = 0;
     uint64_t coef_floats = 0;
     uint64_t coef_long_floats = 0;  // planes prefix the long-slice RLGR launch writes
     uint64_t coef_mid_floats = 0;   // ... and the medium tier
@@ -151,6 +157,10 @@ struct pvvc_plan {
     int32_t ngroups_a = 0, ngroups_b = 0;
     int32_t ngroups_a_long = 0;           // leading phase-A groups that hold a long-launch slice
     int32_t ngroups_a_mid = 0;            // the next phase-A groups: a medium-tier slice, no long one
+    // window mode: the medium tier's groups split in two sub-tiers (the
+    // larger first) on streams of their own, so that the second's inverse
+    // transform starts as soon as its shorter RLGR ends; the second's count
+    int32_t ngroups_a_mid2 = 0;
     // leading phase-A groups decoded by the windowed RLGR (then ngroups_a_long
     // and ngroups_a_mid count its long and medium tiers), their slices (the
     // head of `order`) and their coefficient planes (never cleared)
@@ -165,6 +175,7 @@ struct pvvc_plan {
     int32_t nmid = 0;        // the next nmid slices to the medium tier
     pvvc::SideStream side;   // the long tier's stream
     pvvc::SideStream side2;  // the medium tier's stream
+    pvvc::SideStream side3;  // window mode: the medium tier's second half
     pvvc::SideStream tree;   // the tree expansion's stream (beside the coefficient clear and RLGR)
     bool upload_pending = false;  // built with deferred copies, not yet queued
     // d_work holds this plan's records (their upload is queued): a rebuild of
