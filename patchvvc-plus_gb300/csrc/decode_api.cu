@@ -462,7 +462,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
                 const bool first = c0 == 0;
                 const bool phase_b = has_intra && !first;
                 if ((first && has_intra) || cnt >= p->tune.min_group) {
-                    GroupDesc g{slot_of[si], (int32_t)items.size(), cnt, (first && has_intra) ? 1 : 0};
+                    GroupDesc g{slot_of[si], (int32_t)items.size(), cnt, (int16_t)((first && has_intra) ? 1 : 0)};
                     items.insert(items.end(), L + c0, L + c0 + cnt);
                     (phase_b ? gb : ga).push_back(g);
                 } else {
@@ -549,6 +549,17 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         }
         p->groups = ga;
         p->groups.insert(p->groups.end(), gb.begin(), gb.end());
+        p->long_split_off = (int32_t)p->groups.size();
+        p->nlong_split = 0;
+        if (p->nwin > 0 && kLongSplit > 1)
+            for (int gi = 0; gi < p->ngroups_a_long; ++gi)
+                for (int h = 0; h < kLongSplit; ++h) {
+                    GroupDesc g = ga[gi];
+                    g.part = (uint8_t)h;
+                    g.parts = (uint8_t)kLongSplit;
+                    p->groups.push_back(g);
+                    ++p->nlong_split;
+                }
         p->ngroups_a = (int32_t)ga.size();
         p->ngroups_b = (int32_t)gb.size();
         p->idx = items;
@@ -563,7 +574,7 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
         // (window groups first; a region holds the largest slice of its group)
         uint64_t c = 0;
         p->coef_win_floats = 0;
-        for (size_t gi = 0; gi < p->groups.size(); ++gi) {
+        for (int32_t gi = 0; gi < p->ngroups_a + p->ngroups_b; ++gi) {  // (not the long groups' split copies)
             const GroupDesc& g = p->groups[gi];
             uint32_t gn = 0;
             for (int l = 0; l < g.count; ++l) {
@@ -614,12 +625,13 @@ int build_plan(const pvvc_batch_desc* d, pvvc_plan* p, const pvvc_tune* tune, cu
     {
         uint32_t maxn = 0;
         for (const auto& g : p->groups) maxn = std::max(maxn, W[p->idx[g.first]].n);
-        p->grp_ctas = std::min<int32_t>((int32_t)p->groups.size(), p->tune.group_ctas_per_sm * sm_count());
+        p->grp_ctas = std::min<int32_t>(p->ngroups_a + p->ngroups_b, p->tune.group_ctas_per_sm * sm_count());
         p->grp_floats = 2ull * std::max<uint32_t>(maxn, 1) * 96;
         p->ws_grp = off;
         off = align_up(off + 4ull * p->grp_floats * std::max(p->grp_ctas, 1), 256);
         // the long-slice groups run beside the others, with level buffers of their own
-        p->grp_ctas_long = p->ngroups_a_long > 0 ? std::min<int32_t>(p->ngroups_a_long, p->grp_ctas) : 0;
+        const int32_t nlg = p->nlong_split > 0 ? p->nlong_split : p->ngroups_a_long;  // the long groups' launch
+        p->grp_ctas_long = nlg > 0 ? std::min<int32_t>(nlg, p->grp_ctas) : 0;
         p->ws_grp_long = off;
         off = align_up(off + 4ull * p->grp_floats * p->grp_ctas_long, 256);
         p->grp_ctas_mid = p->ngroups_a_mid > 0 ? std::min<int32_t>(p->ngroups_a_mid, p->grp_ctas) : 0;
@@ -733,8 +745,10 @@ int run_decode(const pvvc_plan* p, pvvc_state* st, const uint8_t* payload, float
                 !mark(2) || !raht_groups(0, p->ngroups_a, cnt, gsc, p->grp_ctas, s))
                 return PVVC_ERR_CUDA;
         } else {
+            // the long groups, each split over several CTAs (their copies after the phase-B groups)
+            const int lf = p->nlong_split > 0 ? p->long_split_off : 0, ln = p->nlong_split > 0 ? p->nlong_split : nl;
             if (nl > 0 && ((tree_aside && cudaStreamWaitEvent(L.s, p->tree.mid, 0) != cudaSuccess) ||
-                           !raht_groups(0, nl, cnt, reinterpret_cast<float*>(w + p->ws_grp_long), p->grp_ctas_long, L.s) ||
+                           !raht_groups(lf, ln, cnt, reinterpret_cast<float*>(w + p->ws_grp_long), p->grp_ctas_long, L.s) ||
                            cudaEventRecord(L.join, L.s) != cudaSuccess))
                 return PVVC_ERR_CUDA;
             if (nm > 0 && ((tree_aside && cudaStreamWaitEvent(M.s, p->tree.mid, 0) != cudaSuccess) ||

@@ -51,6 +51,9 @@ constexpr int kRlgrLongLanes = 32;
 // has at least kMidSplitMin groups
 constexpr int kMidSplit = 2;
 constexpr int kMidSplitMin = 64;
+// window mode: the long tier's groups (the largest, the last to finish)
+// are inverse-transformed by kLongSplit CTAs each
+constexpr int kLongSplit = 2;
 
 // the SM count (queried once)
 inline int sm_count() {
@@ -146,6 +149,9 @@ struct pvvc_plan {
     uint64_t ws_grp_long = 0, ws_grp_mid = 0;  // level buffers of the long and medium groups' launches
     int32_t grp_ctas_mid2 = 0;
     uint64_t ws_grp_mid2 = 0;
+    // window mode: the long tier's groups again, each split over
+    // kLongSplit CTAs for their inverse transform (after the phase-B groups)
+    int32_t long_split_off = 0, nlong_split = 0;
     uint64_t coef_floats = 0;
     uint64_t coef_long_floats = 0;  // planes prefix the long-slice RLGR launch writes
     uint64_t coef_mid_floats = 0;   // ... and the medium tier

@@ -1286,7 +1286,7 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 3) k_raht_group(const SliceWor
                 __syncwarp();
             };
             if (H == 1) {
-                if (wid == 0) {
+                if (wid == 0 && G.part == 0) {
                     const float gy = act ? cy[0] : 0.f, gu = act ? cu[0] : 0.f, gv = act ? cv[0] : 0.f;
                     finish(0, 0, gy, gu, gv);
                     flush(0, 1);
@@ -1374,8 +1374,11 @@ __global__ void __launch_bounds__(32 * kGrpWarps, 3) k_raht_group(const SliceWor
                         }
                     }
                 };
-                const int per = (cnt + kGrpWarps - 1) / kGrpWarps;
-                const int j0 = min(cnt, wid * per), j1 = min(cnt, j0 + per);
+                // this warp's share of the last-level nodes: of all the
+                // warps of the CTAs the group is split over
+                const int parts = G.parts > 1 ? G.parts : 1, vw = G.part * kGrpWarps + wid;
+                const int per = (cnt + kGrpWarps * parts - 1) / (kGrpWarps * parts);
+                const int j0 = min(cnt, vw * per), j1 = min(cnt, j0 + per);
                 uint32_t base = 0, staged = 0;
                 int pj = 0;
                 if (j0 < j1) {

@@ -87,7 +87,11 @@ struct GroupDesc {
     int32_t slot;
     int32_t first;  // into the group item list
     int32_t count;  // <= 32
-    int32_t intra;
+    int16_t intra;
+    // the inverse transform of a group may be split over `parts` CTAs (0
+    // means 1), each repeating the levels above the last two and taking
+    // part `part` of the last-level nodes
+    uint8_t part, parts;
 };
 
 }  // namespace pvvc
