@@ -93,5 +93,6 @@ struct GroupDesc {
     // part `part` of the last-level nodes
     uint8_t part, parts;
 };
+static_assert(sizeof(GroupDesc) == 16, "GroupDesc: four words");
 
 }  // namespace pvvc
