@@ -201,9 +201,9 @@ int pvvc_graph_destroy(pvvc_graph* graph);
  * host threads; each part's points are copied back as soon as it is decoded,
  * while the next part decodes.  The state keeps the parts' plans: a call
  * with the previous call's layout (slices' slots, types and sizes) reuses
- * them, their per-call fields gathered on the device.  Every CUDA call is
- * made by the calling thread, on `stream` (the default stream included) and
- * streams the state owns.  Page-locked output arrays (cudaHostAlloc /
+ * them, their per-call fields gathered on the device.  Any stream works,
+ * the default one included (the plans' copies are queued on `stream` after
+ * planning, never synchronously).  Page-locked output arrays (cudaHostAlloc /
  * cudaHostRegister) let those copies run at the link's full rate.  Slot =
  * patch index.  Synchronises `stream` before returning.  status_host
  * receives one entry per slice, in file order; a zstd payload that does not
